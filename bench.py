@@ -1,0 +1,311 @@
+#!/usr/bin/env python
+"""Benchmark of the VMC inner loop on one GB300 (one JSON line on stdout).
+
+Workload (default): 1D chain L=64, periodic, transverse-field Ising h=J=1; RBM_Dense with
+256 hidden units (alpha 4, 16,640 float32 parameters, N(0, 0.01^2) init); LocalFlip with
+8192 chains, 64 single-spin proposals per sweep, 640 thermalisation proposals; MinSR
+(Ns = 8192 < Np, T 8192 x 8192) with diagonal shift 1e-4 (minnorm_shift_eig), FP32
+everywhere except the FP64 Cholesky solve. One step = one SR iteration: sweep, local
+energies, Obar, Gram, solve, parameter update.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun with N > 1 every rank runs an independent replica of the workload (the
+chains of different replicas never interact, no collective on the data path): weak
+scaling; timing is bracketed by barriers and the max over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SR steps/s"
+UNIT = "SR_steps/s"
+WORKLOAD = dict(workload="tfim_chain64_rbm256_minsr8192", lattice="Chain(64) PBC", hamiltonian="Ising(h=1, J=1)",
+                model="RBM_Dense(features=256)", nparams=16640, sampler="LocalFlip", chains=8192,
+                proposals_per_sweep=64, thermal_proposals=640, solver="minnorm_shift_eig(ashift=1e-4)",
+                gram="fp32", l2="Obar (545 MB) and T (537 MB) exceed the 129 MB L2 every step")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(budget_s: float = 20.0):
+    """The oracle's vectorised CPU restatement on a bounded sample of the workload, each
+    phase scaled to the full workload by its complexity (linear in the chains for the
+    sweep / E_loc / Obar, quadratic for the Gram, cubic for the Cholesky)."""
+    import numpy as np
+    import scipy.linalg as sla
+    from oracle import cpu_vmc, metropolis, rbm as orbm
+
+    cores = len(os.sched_getaffinity(0))
+    try:
+        import threadpoolctl
+        threadpoolctl.threadpool_limits(cores)
+    except Exception:
+        pass
+    N, M, NS, steps = 64, 256, 8192, 64
+    ns_s = 2048
+    W, b, _ = orbm.init_normal(N, M, 0.01, seed=0)
+    W, b = W.astype(np.float64), b.astype(np.float64)
+    s = metropolis.init_uniform(ns_s, N, 1).astype(np.float64)
+    tm = {}
+    cpu_vmc.sr_step(W, b, s, 7, 0, steps, timings=tm)  # Gram / solve at ns_s
+    t_lin = tm["sweep"] + tm["eloc"] + tm["obar"]
+    ng = 4096
+    Ob = np.random.default_rng(0).normal(size=(ng, M * N + M)) * 1e-3
+    t0 = time.perf_counter()
+    T = Ob @ Ob.T
+    t_gram = time.perf_counter() - t0
+    T[np.diag_indices_from(T)] += 1e-4
+    t0 = time.perf_counter()
+    sla.solve(T, np.ones(ng), assume_a="pos")
+    t_chol = time.perf_counter() - t0
+    total = t_lin * NS / ns_s + t_gram * (NS / ng) ** 2 + t_chol * (NS / ng) ** 3
+    return {"value": 1.0 / total, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"oracle/cpu_vmc.py: sweep+E_loc+Obar on {ns_s} of {NS} chains (x{NS // ns_s}), Gram "
+                       f"{ng}x{M * N + M} (x{(NS // ng) ** 2}), Cholesky n={ng} (x{(NS // ng) ** 3}); "
+                       f"seconds per full SR step {total:.1f}"),
+            "phases_s": {"linear": t_lin * NS / ns_s, "gram": t_gram * (NS / ng) ** 2,
+                         "cholesky": t_chol * (NS / ng) ** 3}}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    cb = cpu_baseline()
+    steps = max(1, args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(WORKLOAD, parallelism="host cores"),
+            "reference_jax": "unavailable on this box: quantax needs jax/equinox, not installed, no network",
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--gram", default="fp32", choices=["fp32", "tf32", "bf16", "3xtf32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import quantax_gb300 as qtx
+    from quantax_gb300 import _build, _lib
+
+    _build.build()
+    qtx.set_random_seed(1234 + rank)
+    qtx.sites.Chain(64)
+    H = qtx.operator.Ising(h=1.0, J=1.0)
+    state = qtx.state.Variational(qtx.model.RBM_Dense(256, init_std=0.01))
+    sampler = qtx.sampler.LocalFlip(state, 8192, thermal_steps=640, sweep_steps=64)
+    opt = qtx.optimizer.SR(state, H, solver=qtx.optimizer.minnorm_shift_eig(ashift=1e-4), gram=args.gram)
+    lr = 1e-2
+
+    def sr_step(ev=None):
+        def mark(name):
+            if ev is not None:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record()
+                ev.append((name, e))
+        samples = sampler.sweep()
+        mark("sweep")
+        Ebar = opt.get_Ebar(samples)
+        mark("eloc")
+        Obar = opt.get_Obar(samples)
+        mark("obar")
+        opt.marks = ev
+        step = opt.solve(Obar, Ebar)
+        opt.marks = None
+        mark("solve")
+        state.update(step * lr)
+        mark("update")
+
+    for _ in range(args.warmup):
+        sr_step()
+    torch.cuda.synchronize()
+
+    clocks = Clocks(local)
+    if rank == 0:
+        clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.launch_count
+    start = torch.cuda.Event(enable_timing=True)
+    start.record()
+    step_events = []
+    phase_events = []
+    for _ in range(args.steps):
+        ev = []
+        sr_step(ev)
+        phase_events.append(ev)
+        step_events.append(ev[-1][1])
+    end = torch.cuda.Event(enable_timing=True)
+    end.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop() if rank == 0 else None
+    launches = _lib.launch_count - launches0
+    elapsed = start.elapsed_time(end) / 1000.0
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+
+    # per-step latency and per-phase device time
+    lat, prev = [], start
+    for e in step_events:
+        lat.append(prev.elapsed_time(e))
+        prev = e
+    phases = {}
+    for i, ev in enumerate(phase_events):
+        prev = start if i == 0 else phase_events[i - 1][-1][1]
+        for name, e in ev:
+            phases[name] = phases.get(name, 0.0) + prev.elapsed_time(e)
+            prev = e
+    phases = {k: v / args.steps for k, v in phases.items()}
+    if "gram" in phases:
+        phases["cusolver_and_projection"] = phases.pop("solve")
+    energy = opt.energy
+
+    # end to end through the public API with host buffers: parameters in from pinned host
+    # memory, energy statistics and updated parameters back every step
+    host_params = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
+    host_params.copy_(state.params.cpu())
+    host_out = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
+    host_stats = torch.empty(3, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        state.params.copy_(host_params, non_blocking=True)
+        state._refresh()
+        sr_step()
+        host_stats.copy_(opt.stats, non_blocking=True)
+        host_out.copy_(state.params, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        host_params.copy_(host_out)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_s = e0.elapsed_time(e1) / 1000.0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank == 0:
+        hbm, bf16, src = peaks()
+        ns, npar = 8192, state.nparams
+        gram_flop = 2.0 * ns * ns * npar
+        t_gram = phases.get("gram", float("nan")) / 1000.0
+        achieved = gram_flop / t_gram / 1e12
+        roof = {"kernel": "qgx_gram (T = Obar Obar^T)", "bound": "tensor", "achieved": achieved, "peak": bf16,
+                "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": f"bf16 dense, {src}",
+                "traffic": None, "algorithmic": f"2*Ns^2*Np = {gram_flop:.3e} FLOP per launch"}
+        lat_sorted = sorted(lat)
+        p = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(round(q * (len(lat_sorted) - 1))))]
+        line = {
+            "metric": METRIC, "value": world * args.steps / elapsed, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 solve)",
+            "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas x{world}", gram=args.gram),
+            "samples_per_s": world * args.steps * ns / elapsed, "p50_step_ms": p(0.5), "p99_step_ms": p(0.99),
+            "phases_ms": {k: round(v, 4) for k, v in phases.items()}, "energy": energy,
+            "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": npar * 4,
+                    "d2h_bytes_per_step": npar * 4 + 24},
+            "gpu_launches": launches, "roofline": roof, "clocks": clk,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

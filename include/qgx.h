@@ -1,0 +1,202 @@
+/*
+ * qgx.h -- C ABI of the GB300 (sm_103a) VMC inner loop: Metropolis sampling, local
+ * energies, per-sample log-derivatives, Gram matrices and the FP64 SR / MinSR solve.
+ *
+ * Conventions for every entry point:
+ *   - all array arguments are DEVICE pointers owned by the caller (no allocation inside
+ *     the library, apart from one lazily created cuSOLVER handle per device);
+ *   - work is enqueued on the given stream and the call returns without synchronising;
+ *   - the return value is a status code (QGX_OK on success); a non-zero status means
+ *     nothing was enqueued (argument errors) or the launch failed (QGX_ERR_CUDA);
+ *   - spin configurations are bit-packed: chain c occupies words
+ *     spins[c*nw .. c*nw+nw-1], nw = (n+31)/32, bit (j%32) of word j/32 is 1 when
+ *     site j holds +1 (spin up) and 0 when it holds -1;
+ *   - random draws come from Philox4x32-10 keyed by the 64-bit seed; draw t of chain c
+ *     uses counter (c, t & 0xffffffff, t >> 32, tag << 24).
+ *
+ * The reference interfaces each entry point replaces are cited as
+ * path:line inside the reference project (ChenAo-Phys/quantax).
+ */
+#ifndef QGX_H_
+#define QGX_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
+
+#define QGX_OK 0
+#define QGX_ERR_ARG 1          /* invalid argument (size, null pointer, layout) */
+#define QGX_ERR_CUDA 2         /* a CUDA launch or runtime call failed */
+#define QGX_ERR_TIMEOUT 3      /* a bounded device wait expired */
+#define QGX_ERR_NONFINITE 4    /* non-finite value detected */
+#define QGX_ERR_UNSUPPORTED 5  /* configuration outside the compiled kernels */
+#define QGX_ERR_SOLVER 6       /* cuSOLVER returned an error */
+
+#define QGX_PROPOSAL_LOCAL_FLIP 0    /* quantax.sampler.LocalFlip */
+#define QGX_PROPOSAL_SPIN_EXCHANGE 1 /* quantax.sampler.SpinExchange */
+
+#define QGX_SOLVE_SHIFT 0  /* diagonal-shifted Cholesky (minnorm_shift_eig) */
+#define QGX_SOLVE_PINV 1   /* soft pseudo-inverse via eigh (minnorm_pinv_eig) */
+
+#define QGX_GRAM_FP32 0    /* FP32 SIMT FMA, FP32 accumulation */
+#define QGX_GRAM_TF32 1    /* tcgen05 kind::tf32, FP32 accumulation in TMEM */
+#define QGX_GRAM_BF16 2    /* tcgen05 kind::f16 with bf16 operands, FP32 accumulation */
+#define QGX_GRAM_3XTF32 3  /* tcgen05 split-TF32 (hi*hi + hi*lo + lo*hi), FP32 accuracy */
+
+/* ---- library ----------------------------------------------------------------- */
+int qgx_abi_version(void);
+const char* qgx_status_string(int status);
+/* Human-readable text of the last CUDA error seen by this thread ("" if none). */
+const char* qgx_last_error(void);
+
+/* ---- random numbers ------------------------------------------------------------ */
+/* Raw Philox4x32-10 on n counters: out[4i..4i+3] = philox(ctr[4i..4i+3], key[0..1]).
+ * Known-answer check of the generator shared by every sampler. Replaces the threefry
+ * key handling of quantax/global_defs.py:54-91. */
+int qgx_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int64_t n,
+                      qgx_stream_t stream);
+
+/* ---- configurations (quantax/utils/basis.py:121-219) ----------------------------- */
+/* Uniform +-1 configurations (_rand_states, basis.py:121-125). */
+int qgx_spins_init_uniform(uint32_t* spins, int64_t ns, int32_t n, uint64_t seed,
+                           qgx_stream_t stream);
+/* Exactly nup up spins per chain, independent uniform permutations
+ * (_rand_Nconserved, basis.py:128-133). */
+int qgx_spins_init_fixed_up(uint32_t* spins, int64_t ns, int32_t n, int32_t nup,
+                            uint64_t seed, qgx_stream_t stream);
+/* int8 +-1 <-> packed adapters for API parity with the reference's int8 spins. */
+int qgx_spins_unpack(const uint32_t* spins, int8_t* out, int64_t ns, int32_t n,
+                     qgx_stream_t stream);
+int qgx_spins_pack(const int8_t* in, uint32_t* spins, int64_t ns, int32_t n,
+                   qgx_stream_t stream);
+
+/* ---- local operators -------------------------------------------------------------- */
+/* A spin Hamiltonian compiled from a QuSpin-format op list
+ * (quantax/operator/operator.py:187-238, 30-119) into device tables:
+ *   diagonal:  c0 + sum_z Jz[k] s[iz[k]] + sum_zz Jzz[k] s[i] s[j]
+ *   one-site flips: element f1_J[2k + (s_i>0)] for flipping site f1_i[k]
+ *   two-site flips: element f2_J[4k + 2(s_i>0) + (s_j>0)] for flipping f2_ij[2k], f2_ij[2k+1]
+ * A zero element means "no connection" (the reference's NaN / isclose(0) compaction,
+ * operator.py:144-165). All pointers are device pointers. */
+typedef struct {
+  double c0;
+  int32_t n_z;
+  const int32_t* z_i;
+  const double* z_J;
+  int32_t n_zz;
+  const int32_t* zz_ij; /* 2*n_zz */
+  const double* zz_J;
+  int32_t n_f1;
+  const int32_t* f1_i;
+  const double* f1_J; /* 2*n_f1 */
+  int32_t n_f2;
+  const int32_t* f2_ij; /* 2*n_f2 */
+  const double* f2_J;   /* 4*n_f2 */
+} qgx_operator_t;
+
+/* Diagonal part only, per configuration (Operator.apply_diag, operator.py:83-93). */
+int qgx_operator_diag(const qgx_operator_t* op, const uint32_t* spins, int64_t ns, int32_t n,
+                      double* out, qgx_stream_t stream);
+
+/* ---- RBM_Dense (quantax/model/shallow_nets.py:35-126) ------------------------------- */
+/* Number of floats of the per-parameter-set table used by every RBM kernel. */
+int64_t qgx_rbm_table_floats(int32_t n, int32_t m);
+/* Build the table from W (m x n row-major, eqx Linear layout), b (m) and the optional
+ * visible bias a (n, may be NULL). Must be re-run after every parameter update. */
+int qgx_rbm_prepare(const float* W, const float* b, const float* a, int32_t n, int32_t m,
+                    float* table, qgx_stream_t stream);
+/* log|psi(s)| = sum_i log cosh(W s + b)_i (+ a.s)   (Variational.__call__,
+ * quantax/state/variational.py:325-347). */
+int qgx_rbm_log_psi(const float* table, int32_t n, int32_t m, const uint32_t* spins,
+                    int64_t ns, float* log_psi, qgx_stream_t stream);
+/* nsteps Metropolis proposals on every chain, one warp per chain, theta resident
+ * (Metropolis._partial_sweep/_single_sweep/_update, quantax/sampler/metropolis.py:246-322;
+ * LocalFlip.propose common_samplers.py:28-33; SpinExchange common_samplers.py:58-162).
+ * Draw t of chain c is step0 + t. spins are updated in place; log_psi receives
+ * log|psi| of the final configurations; accepts (may be NULL) receives per-chain accept
+ * counts. nbr (n x z int32, -1 padded) and hop are used by SPIN_EXCHANGE only. */
+int qgx_rbm_sweep(const float* table, int32_t n, int32_t m, uint32_t* spins, float* log_psi,
+                  int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0,
+                  float reweight, int32_t proposal, const int32_t* nbr, int32_t z, int32_t hop,
+                  qgx_stream_t stream);
+/* Local energies E_loc(s) = sum_s' H_ss' psi(s')/psi(s) with connected configurations
+ * generated in-kernel (Operator.Oloc, quantax/operator/operator.py:510-562). */
+int qgx_rbm_eloc(const float* table, int32_t n, int32_t m, const qgx_operator_t* op,
+                 const uint32_t* spins, int64_t ns, double* eloc, qgx_stream_t stream);
+/* Per-sample log-derivatives O (ns x np, row stride ldo floats), np = m*n + m (+ n with
+ * the visible bias), parameter order W (row-major), b, a (Variational.jacobian,
+ * quantax/state/variational.py:424-511). */
+int qgx_rbm_jacobian(const float* table, int32_t n, int32_t m, int32_t has_vbias,
+                     const uint32_t* spins, int64_t ns, float* O, int64_t ldo,
+                     qgx_stream_t stream);
+/* Workspace bytes of qgx_rbm_obar. */
+int64_t qgx_rbm_obar_workspace_bytes(int32_t n, int32_t m, int64_t ns);
+/* Centred, scaled log-derivatives Obar = (O - mean_s O) * sqrt(r_s / ns) written in one
+ * pass, and the weighted mean Omean = mean_s(O r) (np doubles)
+ * (QNGD.get_Obar/_Omat_to_Obar, quantax/optimizer/sr.py:76-88). r may be NULL (all 1). */
+int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias,
+                 const uint32_t* spins, const double* r, int64_t ns, float* Obar, int64_t ldo,
+                 double* omean, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+
+/* ---- statistics and centring (quantax/optimizer/sr.py:76-88, 180-195) ----------------- */
+/* energy = Re mean(E r), VarE = mean(|E - energy|^2 r) with compensated FP64 sums;
+ * ebar = (E - mean E) sqrt(r / ns). E_im / ebar_im may be NULL for real E.
+ * stats[0..2] = {Re energy, Im energy, VarE}. */
+int qgx_energy_stats(const double* E_re, const double* E_im, const double* r, int64_t ns,
+                     double* stats, double* ebar_re, double* ebar_im, qgx_stream_t stream);
+/* Reweight factors r_s = |psi_s|^(2-n) / mean (Sampler._get_reweight_factor,
+ * quantax/sampler/sampler.py:66-69), from log|psi|. */
+int qgx_reweight_factor(const float* log_psi, int64_t ns, float reweight, double* r,
+                        qgx_stream_t stream);
+/* Workspace bytes of qgx_center_columns. */
+int64_t qgx_center_columns_workspace_bytes(int64_t ns, int64_t np);
+/* In-place O -> (O - mean_s O) * sqrt(r_s / ns) for a dense (ns x np) matrix, and
+ * omean = mean_s(O r). Generic form of the centring used by non-RBM models. */
+int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const double* r,
+                       double* omean, void* workspace, int64_t workspace_bytes,
+                       qgx_stream_t stream);
+
+/* ---- Gram matrices (quantax/optimizer/solver.py:139, 157) ---------------------------- */
+/* T = A A^T for A (rows x k, row stride lda floats), written as FP64 rows x rows
+ * (full symmetric matrix, row stride ldt). mode = QGX_GRAM_*. */
+int qgx_gram(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt,
+             int32_t mode, qgx_stream_t stream);
+/* S = A^T A (k x k) for the SR branch (Ns >= Np). */
+int qgx_gram_t(const float* A, int64_t rows, int64_t k, int64_t lda, double* S, int64_t lds,
+               qgx_stream_t stream);
+
+/* ---- FP64 solve (quantax/optimizer/solver.py:50-201) -------------------------------- */
+/* Workspace bytes of qgx_minsr_solve (Gram n x n, A n x np) or qgx_sr_solve (Gram
+ * np x np, pass n = np of the Gram and np = the number of samples). */
+int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* bytes);
+/* MinSR branch: given T = A A^T (n x n FP64, overwritten), b (n), A (n x np FP32):
+ *   SHIFT: (T + (rshift tr T + ashift) I) y = b by Cholesky, x = A^T y
+ *   PINV:  T = U diag(l) U^T, x = A^T U diag(l+) rho, rho = sum_without_noise(U^T o b)
+ * x (np doubles). info (device int, may be NULL) receives the cuSOLVER info. */
+int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t lda,
+                    const double* b, int32_t method, double rshift, double ashift,
+                    double rtol, double atol, double tol_snr, double* x, int32_t* info,
+                    void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+/* SR branch: given S = A^T A (np x np FP64, overwritten): x = S^-1 A^T b with the same
+ * two regularisations (lstsq_shift_eig / lstsq_pinv_eig). */
+int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda,
+                 const double* b, int32_t method, double rshift, double ashift,
+                 double rtol, double atol, double tol_snr, double* x, int32_t* info,
+                 void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+
+/* ---- parameter update (quantax/state/variational.py:558-579) ------------------------- */
+/* params <- params - step when every step entry is finite; otherwise params are left
+ * unchanged and *flag (device int) is set to 1 (else 0). */
+int qgx_apply_update(float* params, const double* step, int64_t np, int32_t* flag,
+                     qgx_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QGX_H_ */

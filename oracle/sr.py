@@ -1,0 +1,114 @@
+"""Stochastic reconfiguration / MinSR in FP64 (test infrastructure only).
+
+Restates:
+  * QNGD._Omat_to_Obar / get_Obar: Obar = (O - mean_s O) * sqrt(r / Ns)
+    (quantax/optimizer/sr.py:76-88);
+  * SR.get_Ebar: energy = Re mean(E r), VarE = mean(|E - Emean|^2 r),
+    Ebar = (E - mean E) * sqrt(r / Ns) (quantax/optimizer/sr.py:180-195);
+  * QNGD.solve: real-to-complex states stack [Re; Im] (quantax/optimizer/sr.py:90-113);
+  * the solvers of quantax/optimizer/solver.py:12-201: minnorm/lstsq shift (Cholesky),
+    minnorm/lstsq pinv (eigh with the soft inverse 1/(l (1 + ((rtol max|l| + atol)/|l|)^6)))
+    and the SNR truncation;
+  * Variational.update: params - step, skipped when non-finite
+    (quantax/state/variational.py:558-579).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+
+
+def obar(O, r=None):
+    ns = O.shape[0]
+    r = np.ones(ns) if r is None else np.asarray(r)
+    return (O - O.mean(axis=0, keepdims=True)) * np.sqrt(r / ns)[:, None]
+
+
+def ebar(E, r=None):
+    ns = E.shape[0]
+    r = np.ones(ns) if r is None else np.asarray(r)
+    emean = np.mean(E * r)
+    var = np.mean(np.abs(E - emean) ** 2 * r).real
+    eb = (E - np.mean(E)) * np.sqrt(r / ns)
+    return eb, float(np.real(emean)), float(var)
+
+
+def _rtol(dtype=np.float64):
+    return {np.dtype(np.float64): 1e-12, np.dtype(np.float32): 1e-6}[np.dtype(dtype)]
+
+
+def minnorm_shift(A, b, rshift=None, ashift=1e-4):
+    T = A @ A.conj().T
+    tr = np.trace(T).real
+    shift = (_rtol() if rshift is None else rshift) * tr + ashift
+    T = T + shift * np.eye(T.shape[0])
+    y = sla.solve(T, b, assume_a="pos")
+    return A.conj().T @ y
+
+
+def lstsq_shift(A, b, rshift=None, ashift=1e-4):
+    S = A.conj().T @ A
+    F = A.conj().T @ b
+    tr = np.trace(S).real
+    shift = (_rtol() if rshift is None else rshift) * tr + ashift
+    S = S + shift * np.eye(S.shape[0])
+    return sla.solve(S, F, assume_a="pos")
+
+
+def eigs_inv(vals, rtol=None, atol=0.0):
+    a = np.abs(vals)
+    rtol = _rtol() if rtol is None else rtol
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f = 1.0 + ((rtol * a.max() + atol) / a) ** 6
+        inv = 1.0 / (vals * f)
+    return np.where(a > 0.0, inv, 0.0)
+
+
+def sum_without_noise(inputs, tol_snr):
+    x = inputs.sum(axis=0)
+    if tol_snr <= 1e-6:
+        return x
+    xm = x / inputs.shape[0]
+    xv = np.sqrt(np.mean(np.abs(inputs - xm[None, :]) ** 2, axis=0) / inputs.shape[0])
+    snr = np.abs(xm) / xv
+    return x / (1.0 + (tol_snr / snr) ** 6)
+
+
+def minnorm_pinv(A, b, rtol=None, atol=0.0, tol_snr=0.0):
+    T = A @ A.conj().T
+    lam, U = np.linalg.eigh(T)
+    inv = eigs_inv(lam, rtol, atol)
+    rho = sum_without_noise(U.conj() * b[:, None], tol_snr)
+    return A.conj().T @ (U @ (inv * rho))
+
+
+def lstsq_pinv(A, b, rtol=None, atol=0.0, tol_snr=0.0):
+    S = A.conj().T @ A
+    lam, V = np.linalg.eigh(S)
+    inv = eigs_inv(lam, rtol, atol)
+    rho_sk = (A.conj() * b[:, None]) @ V.conj()
+    rho = sum_without_noise(rho_sk, tol_snr)
+    return V @ (inv * rho)
+
+
+def auto(A, b, kind="pinv", **kw):
+    if kind == "pinv":
+        return minnorm_pinv(A, b, **kw) if A.shape[0] < A.shape[1] else lstsq_pinv(A, b, **kw)
+    return minnorm_shift(A, b, **kw) if A.shape[0] < A.shape[1] else lstsq_shift(A, b, **kw)
+
+
+def solve(Obar, Ebar, solver, complex_out=False):
+    if complex_out:
+        A = np.concatenate([Obar.real, Obar.imag], axis=0)
+        b = np.concatenate([Ebar.real, Ebar.imag])
+    else:
+        A, b = np.real(Obar), np.real(Ebar)
+    return solver(A, b)
+
+
+def update(params, step, dtype=np.float32):
+    """params (stored in `dtype`) minus step cast to `dtype`, in `dtype` arithmetic."""
+    if not np.all(np.isfinite(step)):
+        return params, False
+    p = np.asarray(params, dtype=dtype)
+    return (p - np.real(step).astype(dtype)).astype(np.float64), True

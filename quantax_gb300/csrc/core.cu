@@ -1,0 +1,400 @@
+// Library plumbing, Philox known-answer entry, configuration init / packing, diagonal
+// operator terms, energy statistics, reweighting, column centring and the guarded
+// parameter update.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "qgx_colstats.cuh"
+#include "qgx_common.cuh"
+
+namespace qgx {
+
+static thread_local char g_last_error[256] = {0};
+
+void set_last_error(cudaError_t e) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_last_error(e);
+    return QGX_ERR_CUDA;
+  }
+  return QGX_OK;
+}
+
+int device_sm_count() {
+  int dev = 0, v = kNumSMs;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return v;
+}
+
+int device_max_smem_optin() {
+  int dev = 0, v = 48 * 1024;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
+// ---- Philox KAT ------------------------------------------------------------------------
+__global__ void philox_kernel(const uint32_t* __restrict__ ctr, const uint32_t* __restrict__ key,
+                              uint32_t* __restrict__ out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  u32x4 c{ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]};
+  u32x4 r = philox4x32_10(c, key[0], key[1]);
+  out[4 * i] = r.x;
+  out[4 * i + 1] = r.y;
+  out[4 * i + 2] = r.z;
+  out[4 * i + 3] = r.w;
+}
+
+// ---- configurations ---------------------------------------------------------------------
+// word w of chain c = word (w % 4) of draw(seed, c, w / 4, kTagInit); bits >= n cleared
+__global__ void init_uniform_kernel(uint32_t* __restrict__ spins, int64_t ns, int n, uint64_t seed) {
+  const int nw = words_for(n);
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= ns * nw) return;
+  const int64_t c = i / nw;
+  const int w = (int)(i % nw);
+  u32x4 r = draw(seed, (uint64_t)c, (uint64_t)(w >> 2), kTagInit);
+  uint32_t v = (w & 3) == 0 ? r.x : (w & 3) == 1 ? r.y : (w & 3) == 2 ? r.z : r.w;
+  const int rem = n - 32 * w;
+  if (rem < 32) v &= (1u << rem) - 1u;
+  spins[i] = v;
+}
+
+constexpr int kMaxInitWords = 32;  // n <= 1024 for the fixed-magnetisation init
+
+// sites 0..nup-1 up, then Fisher-Yates: for i = n-1..1, j = bounded(draw(c, i).x, i+1), swap
+__global__ void init_fixed_up_kernel(uint32_t* __restrict__ spins, int64_t ns, int n, int nup, uint64_t seed) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const int nw = words_for(n);
+  uint32_t w[kMaxInitWords];
+  for (int k = 0; k < nw; ++k) {
+    const int lo = 32 * k;
+    int cnt = nup - lo;
+    cnt = cnt < 0 ? 0 : (cnt > 32 ? 32 : cnt);
+    w[k] = cnt == 32 ? 0xFFFFFFFFu : ((1u << cnt) - 1u);
+  }
+  for (int i = n - 1; i > 0; --i) {
+    u32x4 r = draw(seed, (uint64_t)c, (uint64_t)i, kTagInitPerm);
+    const int j = (int)bounded(r.x, (uint32_t)(i + 1));
+    const uint32_t bi = (w[i >> 5] >> (i & 31)) & 1u;
+    const uint32_t bj = (w[j >> 5] >> (j & 31)) & 1u;
+    if (bi != bj) {
+      w[i >> 5] ^= 1u << (i & 31);
+      w[j >> 5] ^= 1u << (j & 31);
+    }
+  }
+  for (int k = 0; k < nw; ++k) spins[c * nw + k] = w[k];
+}
+
+__global__ void unpack_kernel(const uint32_t* __restrict__ spins, int8_t* __restrict__ out, int64_t ns, int n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= ns * n) return;
+  const int nw = words_for(n);
+  const int64_t c = i / n;
+  const int j = (int)(i % n);
+  out[i] = ((spins[c * nw + (j >> 5)] >> (j & 31)) & 1u) ? (int8_t)1 : (int8_t)-1;
+}
+
+__global__ void pack_kernel(const int8_t* __restrict__ in, uint32_t* __restrict__ spins, int64_t ns, int n) {
+  const int nw = words_for(n);
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= ns * nw) return;
+  const int64_t c = i / nw;
+  const int w = (int)(i % nw);
+  uint32_t v = 0;
+  for (int b = 0; b < 32 && 32 * w + b < n; ++b) v |= (in[c * n + 32 * w + b] > 0 ? 1u : 0u) << b;
+  spins[i] = v;
+}
+
+// ---- diagonal operator part -----------------------------------------------------------
+__device__ inline int spin_pm(const uint32_t* s, int i) { return ((s[i >> 5] >> (i & 31)) & 1u) ? 1 : -1; }
+
+__global__ void operator_diag_kernel(qgx_operator_t op, const uint32_t* __restrict__ spins, int64_t ns, int n,
+                                     double* __restrict__ out) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const uint32_t* s = spins + c * words_for(n);
+  double e = op.c0;
+  for (int k = 0; k < op.n_z; ++k) e += op.z_J[k] * spin_pm(s, op.z_i[k]);
+  for (int k = 0; k < op.n_zz; ++k) e += op.zz_J[k] * (spin_pm(s, op.zz_ij[2 * k]) * spin_pm(s, op.zz_ij[2 * k + 1]));
+  out[c] = e;
+}
+
+// ---- block reductions -------------------------------------------------------------------
+template <int NT>
+__device__ inline double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < NT / 32 ? sh[lane] : 0.0;
+    r = warp_sum(r);
+    if (lane == 0) sh[0] = r;
+  }
+  __syncthreads();
+  r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Compensated sum over a block: each thread holds a Neumaier (s, c) pair.
+template <int NT>
+__device__ inline double block_ksum(const KahanD& k, double* sh) {
+  // sum the high parts with error compensation tracked through the low parts
+  double hi = block_sum<NT>(k.s, sh);
+  double lo = block_sum<NT>(k.c, sh);
+  return hi + lo;
+}
+
+constexpr int kStatThreads = 1024;
+
+// Single-block energy statistics (quantax/optimizer/sr.py:180-195).
+__global__ void __launch_bounds__(kStatThreads) energy_stats_kernel(const double* __restrict__ er, const double* __restrict__ ei,
+                                                                   const double* __restrict__ r, int64_t ns,
+                                                                   double* __restrict__ stats, double* __restrict__ ebr,
+                                                                   double* __restrict__ ebi) {
+  __shared__ double sh[32];
+  KahanD swr, swi, sur, sui;
+  for (int64_t i = threadIdx.x; i < ns; i += kStatThreads) {
+    const double w = r ? r[i] : 1.0;
+    const double a = er[i];
+    const double b = ei ? ei[i] : 0.0;
+    swr.add(a * w);
+    swi.add(b * w);
+    sur.add(a);
+    sui.add(b);
+  }
+  const double inv = 1.0 / (double)ns;
+  const double emr = block_ksum<kStatThreads>(swr, sh) * inv;
+  const double emi = block_ksum<kStatThreads>(swi, sh) * inv;
+  const double mur = block_ksum<kStatThreads>(sur, sh) * inv;
+  const double mui = block_ksum<kStatThreads>(sui, sh) * inv;
+  KahanD sv;
+  for (int64_t i = threadIdx.x; i < ns; i += kStatThreads) {
+    const double w = r ? r[i] : 1.0;
+    const double a = er[i], b = ei ? ei[i] : 0.0;
+    const double da = a - emr, db = b - emi;
+    sv.add((da * da + db * db) * w);
+    const double f = sqrt(w * inv);
+    ebr[i] = (a - mur) * f;
+    if (ebi) ebi[i] = (b - mui) * f;
+  }
+  const double var = block_ksum<kStatThreads>(sv, sh) * inv;
+  if (threadIdx.x == 0) {
+    stats[0] = emr;
+    stats[1] = emi;
+    stats[2] = var;
+  }
+}
+
+// r_s = |psi_s|^(2-n) / mean = exp(x_s - xmax) / mean(exp(x - xmax)), x = (2-n) log|psi|
+__global__ void __launch_bounds__(kStatThreads) reweight_kernel(const float* __restrict__ lp, int64_t ns, float n,
+                                                               double* __restrict__ r) {
+  __shared__ double sh[32];
+  const double p = 2.0 - (double)n;
+  double mx = -INFINITY;
+  for (int64_t i = threadIdx.x; i < ns; i += kStatThreads) mx = fmax(mx, p * (double)lp[i]);
+  // block max
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = sh[threadIdx.x];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) sh[0] = v;
+  }
+  __syncthreads();
+  mx = sh[0];
+  __syncthreads();
+  KahanD s;
+  for (int64_t i = threadIdx.x; i < ns; i += kStatThreads) s.add(exp(p * (double)lp[i] - mx));
+  const double mean = block_ksum<kStatThreads>(s, sh) / (double)ns;
+  for (int64_t i = threadIdx.x; i < ns; i += kStatThreads) r[i] = exp(p * (double)lp[i] - mx) / mean;
+}
+
+// ---- column centring ------------------------------------------------------------------
+constexpr int kColThreads = 256;
+constexpr int kColRows = 128;  // rows per partial-sum chunk
+
+__global__ void col_partial_kernel(const float* __restrict__ O, int64_t ns, int64_t np, int64_t ldo,
+                                   const double* __restrict__ r, double* __restrict__ part_u,
+                                   double* __restrict__ part_w) {
+  const int64_t col = blockIdx.x * (int64_t)kColThreads + threadIdx.x;
+  const int64_t chunk = blockIdx.y;
+  if (col >= np) return;
+  const int64_t r0 = chunk * kColRows;
+  const int64_t r1 = min(ns, r0 + kColRows);
+  double su = 0.0, sw = 0.0;
+  for (int64_t s = r0; s < r1; ++s) {
+    const double v = (double)O[s * ldo + col];
+    su += v;
+    sw += v * (r ? r[s] : 1.0);
+  }
+  part_u[chunk * np + col] = su;
+  part_w[chunk * np + col] = sw;
+}
+
+__global__ void col_center_kernel(float* __restrict__ O, int64_t row0, int64_t ns, int64_t np, int64_t ldo,
+                                  const double* __restrict__ r, const double* __restrict__ mean_u) {
+  const int64_t s = row0 + blockIdx.y;
+  const double f = sqrt((r ? r[s] : 1.0) / (double)ns);
+  for (int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; col < np; col += (int64_t)gridDim.x * blockDim.x) {
+    O[s * ldo + col] = (float)(((double)O[s * ldo + col] - mean_u[col]) * f);
+  }
+}
+
+// ---- guarded update ---------------------------------------------------------------------
+__global__ void finite_check_kernel(const double* __restrict__ step, int64_t np, int32_t* __restrict__ flag) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(step[i]);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+__global__ void update_kernel(float* __restrict__ params, const double* __restrict__ step, int64_t np,
+                              const int32_t* __restrict__ flag) {
+  if (*flag) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x)
+    params[i] = params[i] - (float)step[i];  // f32(params) - f32(step), as variational.py:574-579
+}
+
+inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace qgx
+
+using namespace qgx;
+
+extern "C" {
+
+int qgx_abi_version(void) { return 1; }
+
+const char* qgx_status_string(int status) {
+  switch (status) {
+    case QGX_OK: return "ok";
+    case QGX_ERR_ARG: return "invalid argument";
+    case QGX_ERR_CUDA: return "CUDA error";
+    case QGX_ERR_TIMEOUT: return "device wait timed out";
+    case QGX_ERR_NONFINITE: return "non-finite value";
+    case QGX_ERR_UNSUPPORTED: return "unsupported configuration";
+    case QGX_ERR_SOLVER: return "cuSOLVER error";
+    default: return "unknown status";
+  }
+}
+
+const char* qgx_last_error(void) { return g_last_error; }
+
+int qgx_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int64_t n, qgx_stream_t stream) {
+  QGX_CHECK_ARG(n >= 0);
+  if (n == 0) return QGX_OK;
+  QGX_CHECK_ARG(ctr && key && out);
+  philox_kernel<<<blocks_for(n, 256), 256, 0, as_cuda(stream)>>>(ctr, key, out, n);
+  return launch_status();
+}
+
+int qgx_spins_init_uniform(uint32_t* spins, int64_t ns, int32_t n, uint64_t seed, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns >= 0 && n > 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(spins);
+  const int64_t tot = ns * words_for(n);
+  init_uniform_kernel<<<blocks_for(tot, 256), 256, 0, as_cuda(stream)>>>(spins, ns, n, seed);
+  return launch_status();
+}
+
+int qgx_spins_init_fixed_up(uint32_t* spins, int64_t ns, int32_t n, int32_t nup, uint64_t seed, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns >= 0 && n > 0 && n <= 32 * kMaxInitWords && nup >= 0 && nup <= n);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(spins);
+  init_fixed_up_kernel<<<blocks_for(ns, 128), 128, 0, as_cuda(stream)>>>(spins, ns, n, nup, seed);
+  return launch_status();
+}
+
+int qgx_spins_unpack(const uint32_t* spins, int8_t* out, int64_t ns, int32_t n, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns >= 0 && n > 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(spins && out);
+  unpack_kernel<<<blocks_for(ns * n, 256), 256, 0, as_cuda(stream)>>>(spins, out, ns, n);
+  return launch_status();
+}
+
+int qgx_spins_pack(const int8_t* in, uint32_t* spins, int64_t ns, int32_t n, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns >= 0 && n > 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(spins && in);
+  pack_kernel<<<blocks_for(ns * words_for(n), 256), 256, 0, as_cuda(stream)>>>(in, spins, ns, n);
+  return launch_status();
+}
+
+int qgx_operator_diag(const qgx_operator_t* op, const uint32_t* spins, int64_t ns, int32_t n, double* out,
+                      qgx_stream_t stream) {
+  QGX_CHECK_ARG(op && ns >= 0 && n > 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(spins && out);
+  operator_diag_kernel<<<blocks_for(ns, 128), 128, 0, as_cuda(stream)>>>(*op, spins, ns, n, out);
+  return launch_status();
+}
+
+int qgx_energy_stats(const double* E_re, const double* E_im, const double* r, int64_t ns, double* stats,
+                     double* ebar_re, double* ebar_im, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns > 0 && E_re && stats && ebar_re);
+  QGX_CHECK_ARG(!E_im || ebar_im);
+  energy_stats_kernel<<<1, kStatThreads, 0, as_cuda(stream)>>>(E_re, E_im, r, ns, stats, ebar_re, ebar_im);
+  return launch_status();
+}
+
+int qgx_reweight_factor(const float* log_psi, int64_t ns, float reweight, double* r, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns > 0 && log_psi && r);
+  reweight_kernel<<<1, kStatThreads, 0, as_cuda(stream)>>>(log_psi, ns, reweight, r);
+  return launch_status();
+}
+
+int64_t qgx_center_columns_workspace_bytes(int64_t ns, int64_t np) {
+  if (ns <= 0 || np <= 0) return 0;
+  const int64_t nchunk = (ns + kColRows - 1) / kColRows;
+  return (2 * nchunk * np + np) * (int64_t)sizeof(double);
+}
+
+int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const double* r, double* omean,
+                       void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns > 0 && np > 0 && ldo >= np && O);
+  QGX_CHECK_ARG(workspace && workspace_bytes >= qgx_center_columns_workspace_bytes(ns, np));
+  const int64_t nchunk = (ns + kColRows - 1) / kColRows;
+  QGX_CHECK_ARG(nchunk <= 65535);
+  double* part_u = static_cast<double*>(workspace);
+  double* part_w = part_u + nchunk * np;
+  double* mean_u = part_w + nchunk * np;
+  cudaStream_t st = as_cuda(stream);
+  dim3 g1(blocks_for(np, kColThreads), (unsigned)nchunk);
+  col_partial_kernel<<<g1, kColThreads, 0, st>>>(O, ns, np, ldo, r, part_u, part_w);
+  col_reduce_kernel<<<blocks_for(np, 256), 256, 0, st>>>(part_u, part_w, nchunk, np, ns, mean_u, omean, nullptr);
+  const unsigned gx = (unsigned)std::min<int64_t>(blocks_for(np, 256), 64);
+  for (int64_t r0 = 0; r0 < ns; r0 += 65535) {
+    const int64_t rows = std::min<int64_t>(65535, ns - r0);
+    col_center_kernel<<<dim3(gx, (unsigned)rows), 256, 0, st>>>(O, r0, ns, np, ldo, r, mean_u);
+  }
+  return launch_status();
+}
+
+int qgx_apply_update(float* params, const double* step, int64_t np, int32_t* flag, qgx_stream_t stream) {
+  QGX_CHECK_ARG(np >= 0 && params && step && flag);
+  cudaStream_t st = as_cuda(stream);
+  QGX_CHECK_CUDA(cudaMemsetAsync(flag, 0, sizeof(int32_t), st));
+  if (np == 0) return QGX_OK;
+  const unsigned nb = (unsigned)std::min<int64_t>(blocks_for(np, 256), 4 * device_sm_count());
+  finite_check_kernel<<<nb, 256, 0, st>>>(step, np, flag);
+  update_kernel<<<nb, 256, 0, st>>>(params, step, np, flag);
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// Shared device helpers of the qgx library: status plumbing, Philox4x32-10, bit-packed
+// spin access and warp reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/qgx.h"
+
+namespace qgx {
+
+// ---- status ---------------------------------------------------------------------------
+void set_last_error(cudaError_t e);
+int launch_status();  // QGX_OK or QGX_ERR_CUDA after a kernel launch
+
+#define QGX_CHECK_ARG(cond)            \
+  do {                                 \
+    if (!(cond)) return QGX_ERR_ARG;   \
+  } while (0)
+
+#define QGX_CHECK_CUDA(expr)                 \
+  do {                                       \
+    cudaError_t e_ = (expr);                 \
+    if (e_ != cudaSuccess) {                 \
+      ::qgx::set_last_error(e_);             \
+      return QGX_ERR_CUDA;                   \
+    }                                        \
+  } while (0)
+
+inline cudaStream_t as_cuda(qgx_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time where it matters)
+int device_sm_count();
+int device_max_smem_optin();
+
+// ---- Philox4x32-10 (Salmon et al., SC'11) -----------------------------------------------
+struct u32x4 {
+  uint32_t x, y, z, w;
+};
+
+__host__ __device__ inline uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ inline u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = mulhi32(0xD2511F53u, c.x);
+    const uint32_t lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = mulhi32(0xCD9E8D57u, c.z);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z;
+    c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Stream tags (counter word 3, bits 24..31).
+constexpr uint32_t kTagPropose = 1;
+constexpr uint32_t kTagInit = 2;
+constexpr uint32_t kTagInitPerm = 3;
+
+__host__ __device__ inline u32x4 draw(uint64_t seed, uint64_t chain, uint64_t step, uint32_t tag,
+                                      uint32_t substream = 0) {
+  u32x4 c{(uint32_t)chain, (uint32_t)step, (uint32_t)(step >> 32), (tag << 24) | (substream & 0xFFFFFFu)};
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// (w * n) >> 32: uniform word -> {0..n-1}
+__host__ __device__ inline uint32_t bounded(uint32_t w, uint32_t n) {
+  return (uint32_t)(((uint64_t)w * n) >> 32);
+}
+
+// (w >> 8) * 2^-24: uniform in [0, 1), exact in fp32
+__host__ __device__ inline float unit_float(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+
+// ---- packed spins ----------------------------------------------------------------------
+__host__ __device__ inline int words_for(int n) { return (n + 31) >> 5; }
+
+// ---- warp helpers ----------------------------------------------------------------------
+__device__ inline float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Neumaier-compensated double accumulator
+struct KahanD {
+  double s = 0.0, c = 0.0;
+  __device__ inline void add(double x) {
+    double t = s + x;
+    if (fabs(s) >= fabs(x))
+      c += (s - t) + x;
+    else
+      c += (x - t) + s;
+    s = t;
+  }
+  __device__ inline double value() const { return s + c; }
+};
+
+// log cosh(x) = |x| + log1p(exp(-2|x|)) - log 2, accurate for all finite x
+__device__ inline float logcoshf(float x) {
+  const float ax = fabsf(x);
+  return ax + log1pf(expf(-2.0f * ax)) - 0.69314718055994531f;
+}
+
+}  // namespace qgx

@@ -1,0 +1,325 @@
+// FP64 SR / MinSR solve (quantax/optimizer/solver.py:50-201): diagonal-shifted Cholesky
+// (cuSOLVER Xpotrf / Xpotrs) or the soft pseudo-inverse through an FP64 eigendecomposition
+// (cuSOLVER Xsyevd), followed by the projection x = A^T y over the FP32 Obar matrix.
+//
+// The Gram matrix is symmetric, so the row-major buffer written by qgx_gram is also its
+// own column-major image and is handed to cuSOLVER as is.
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "qgx_common.cuh"
+
+namespace qgx {
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_solver_mutex;
+cusolverDnHandle_t g_handle[kMaxDevices] = {};
+cusolverDnParams_t g_params[kMaxDevices] = {};
+thread_local std::vector<char> g_host_ws;
+
+int solver_for_current_device(cusolverDnHandle_t* h, cusolverDnParams_t* p) {
+  int dev = 0;
+  QGX_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return QGX_ERR_UNSUPPORTED;
+  if (!g_handle[dev]) {
+    if (cusolverDnCreate(&g_handle[dev]) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+    if (cusolverDnCreateParams(&g_params[dev]) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+  }
+  *h = g_handle[dev];
+  *p = g_params[dev];
+  return QGX_OK;
+}
+
+constexpr int kProjRows = 256;  // rows per partial sum of the projection x = A^T y
+
+inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
+
+// trace -> shift = rshift * tr + ashift -> added to the diagonal (single block)
+__global__ void shift_diag_kernel(double* __restrict__ T, int64_t n, int64_t ldt, double rshift, double ashift,
+                                  double* __restrict__ shift_out) {
+  __shared__ double sh[32];
+  KahanD k;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) k.add(T[i * ldt + i]);
+  double v = warp_sum(k.value());
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) sh[0] = v;
+  }
+  __syncthreads();
+  const double shift = rshift * sh[0] + ashift;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) T[i * ldt + i] += shift;
+  if (threadIdx.x == 0 && shift_out) *shift_out = shift;
+}
+
+// partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s]; FP32 products with y split
+// into hi + lo parts, FP64 across chunks
+__global__ void project_partial_kernel(const float* __restrict__ A, int64_t nrow, int64_t ncol, int64_t lda,
+                                       const double* __restrict__ y, double* __restrict__ part) {
+  const int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.y * kProjRows;
+  const int64_t r1 = min(nrow, r0 + kProjRows);
+  if (col >= ncol) return;
+  float hi = 0.0f, lo = 0.0f;
+#pragma unroll 8
+  for (int64_t s = r0; s < r1; ++s) {
+    const double ys = y[s];
+    const float yh = (float)ys;
+    const float yl = (float)(ys - (double)yh);
+    const float a = __ldg(A + s * lda + col);
+    hi = fmaf(a, yh, hi);
+    lo = fmaf(a, yl, lo);
+  }
+  part[blockIdx.y * ncol + col] = (double)hi + (double)lo;
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ part, int64_t nchunk, int64_t ncol,
+                                    double* __restrict__ x) {
+  const int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  KahanD k;
+  for (int64_t c = 0; c < nchunk; ++c) k.add(part[c * ncol + col]);
+  x[col] = k.value();
+}
+
+// soft inverse of the eigenvalues (solver.py:95-101), single block
+__global__ void eigs_inv_kernel(const double* __restrict__ w, int64_t n, double rtol, double atol,
+                                double* __restrict__ inv) {
+  __shared__ double sh[32];
+  double mx = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, fabs(w[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) sh[0] = v;
+  }
+  __syncthreads();
+  mx = sh[0];
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double a = fabs(w[i]);
+    double r = 0.0;
+    if (a > 0.0) {
+      const double q = (rtol * mx + atol) / a;
+      const double q2 = q * q;
+      r = 1.0 / (w[i] * (1.0 + q2 * q2 * q2));
+    }
+    inv[i] = r;
+  }
+}
+
+// v_j = inv_j * rho_j, rho_j = sum_without_noise(U[:, j] * b) (solver.py:114-125, 128-149).
+// U column-major (column j contiguous); one warp per column.
+__global__ void rho_kernel(const double* __restrict__ U, int64_t n, const double* __restrict__ b,
+                           const double* __restrict__ inv, double tol_snr, double* __restrict__ v) {
+  const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= n) return;
+  const double* col = U + j * n;
+  double s = 0.0;
+  for (int64_t t = lane; t < n; t += 32) s += col[t] * b[t];
+  s = warp_sum(s);
+  double rho = s;
+  if (tol_snr > 1e-6) {
+    const double xm = s / (double)n;
+    double q = 0.0;
+    for (int64_t t = lane; t < n; t += 32) {
+      const double d = col[t] * b[t] - xm;
+      q += d * d;
+    }
+    q = warp_sum(q);
+    const double xv = sqrt(q / (double)n / (double)n);
+    const double snr = fabs(xm) / xv;
+    const double r = tol_snr / snr;
+    const double r2 = r * r;
+    rho = s / (1.0 + r2 * r2 * r2);
+  }
+  if (lane == 0) v[j] = inv[j] * rho;
+}
+
+// y_t = sum_j U[t, j] v_j for column-major U: partials over column chunks
+__global__ void uv_partial_kernel(const double* __restrict__ U, int64_t n, const double* __restrict__ v,
+                                  double* __restrict__ part) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j0 = (int64_t)blockIdx.y * kProjRows;
+  const int64_t j1 = min(n, j0 + kProjRows);
+  if (t >= n) return;
+  double acc = 0.0;
+  for (int64_t j = j0; j < j1; ++j) acc += U[j * n + t] * v[j];
+  part[blockIdx.y * n + t] = acc;
+}
+
+struct SolveWs {
+  void* cus;
+  size_t cus_bytes;
+  double* y;      // n
+  double* w;      // n  eigenvalues
+  double* inv;    // n
+  double* v;      // n
+  double* f;      // n  right-hand side of the SR branch (A^T b)
+  double* part;   // nchunk * max(n, np)
+  double* shift;  // 1
+  int* info;      // 1
+};
+
+int query_cusolver_bytes(int64_t n, int method, size_t* dev_bytes, size_t* host_bytes) {
+  cusolverDnHandle_t h;
+  cusolverDnParams_t p;
+  int rc = solver_for_current_device(&h, &p);
+  if (rc != QGX_OK) return rc;
+  cusolverStatus_t s;
+  if (method == QGX_SOLVE_SHIFT) {
+    s = cusolverDnXpotrf_bufferSize(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, nullptr, n, CUDA_R_64F, dev_bytes,
+                                    host_bytes);
+  } else {
+    s = cusolverDnXsyevd_bufferSize(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, nullptr, n,
+                                    CUDA_R_64F, nullptr, CUDA_R_64F, dev_bytes, host_bytes);
+  }
+  return s == CUSOLVER_STATUS_SUCCESS ? QGX_OK : QGX_ERR_SOLVER;
+}
+
+int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t bytes, SolveWs* ws, int64_t* need) {
+  size_t cb = 0, hb = 0;
+  int rc = query_cusolver_bytes(n, method, &cb, &hb);
+  if (rc != QGX_OK) return rc;
+  const int64_t nchunk = (std::max(n, np) + kProjRows - 1) / kProjRows;
+  const int64_t wide = std::max(n, np);
+  int64_t off = 0;
+  auto take = [&](int64_t b) {
+    const int64_t o = off;
+    off += al256(b);
+    return o;
+  };
+  const int64_t o_cus = take((int64_t)cb);
+  const int64_t o_y = take(n * 8);
+  const int64_t o_w = take(n * 8);
+  const int64_t o_inv = take(n * 8);
+  const int64_t o_v = take(n * 8);
+  const int64_t o_f = take(n * 8);
+  const int64_t o_part = take(nchunk * wide * 8);
+  const int64_t o_shift = take(8);
+  const int64_t o_info = take(8);
+  *need = off;
+  if (!base) return QGX_OK;
+  if (bytes < off) return QGX_ERR_ARG;
+  char* b = static_cast<char*>(base);
+  ws->cus = b + o_cus;
+  ws->cus_bytes = cb;
+  ws->y = reinterpret_cast<double*>(b + o_y);
+  ws->w = reinterpret_cast<double*>(b + o_w);
+  ws->inv = reinterpret_cast<double*>(b + o_inv);
+  ws->v = reinterpret_cast<double*>(b + o_v);
+  ws->f = reinterpret_cast<double*>(b + o_f);
+  ws->part = reinterpret_cast<double*>(b + o_part);
+  ws->shift = reinterpret_cast<double*>(b + o_shift);
+  ws->info = reinterpret_cast<int*>(b + o_info);
+  if (hb > g_host_ws.size()) g_host_ws.resize(hb);
+  return QGX_OK;
+}
+
+// x (ncol) = A^T y for A (nrow x ncol, lda)
+int project(const float* A, int64_t nrow, int64_t ncol, int64_t lda, const double* y, double* part, double* x,
+            cudaStream_t st) {
+  const int64_t nchunk = (nrow + kProjRows - 1) / kProjRows;
+  if (nchunk > 65535) return QGX_ERR_UNSUPPORTED;
+  project_partial_kernel<<<dim3((unsigned)((ncol + 255) / 256), (unsigned)nchunk), 256, 0, st>>>(A, nrow, ncol, lda, y,
+                                                                                                  part);
+  sum_partials_kernel<<<(unsigned)((ncol + 255) / 256), 256, 0, st>>>(part, nchunk, ncol, x);
+  return launch_status();
+}
+
+// y = T^-1 b (SHIFT) or U diag(inv) rho (PINV), T n x n (overwritten)
+int solve_gram(double* T, int64_t n, const double* b, int method, double rshift, double ashift, double rtol, double atol,
+               double tol_snr, const SolveWs& ws, int32_t* info, cudaStream_t st) {
+  cusolverDnHandle_t h;
+  cusolverDnParams_t p;
+  int rc = solver_for_current_device(&h, &p);
+  if (rc != QGX_OK) return rc;
+  if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+  int* dinfo = info ? info : ws.info;
+  void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
+  if (method == QGX_SOLVE_SHIFT) {
+    shift_diag_kernel<<<1, 1024, 0, st>>>(T, n, n, rshift, ashift, ws.shift);
+    if ((rc = launch_status()) != QGX_OK) return rc;
+    if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus, ws.cus_bytes, hws,
+                         g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
+      return QGX_ERR_SOLVER;
+    QGX_CHECK_CUDA(cudaMemcpyAsync(ws.y, b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, dinfo) !=
+        CUSOLVER_STATUS_SUCCESS)
+      return QGX_ERR_SOLVER;
+    return QGX_OK;
+  }
+  if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.w,
+                       CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
+    return QGX_ERR_SOLVER;
+  eigs_inv_kernel<<<1, 1024, 0, st>>>(ws.w, n, rtol, atol, ws.inv);
+  rho_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(T, n, b, ws.inv, tol_snr, ws.v);
+  const int64_t nchunk = (n + kProjRows - 1) / kProjRows;
+  uv_partial_kernel<<<dim3((unsigned)((n + 255) / 256), (unsigned)nchunk), 256, 0, st>>>(T, n, ws.v, ws.part);
+  sum_partials_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ws.part, nchunk, n, ws.y);
+  return launch_status();
+}
+
+}  // namespace
+}  // namespace qgx
+
+using namespace qgx;
+
+extern "C" {
+
+int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* bytes) {
+  QGX_CHECK_ARG(n > 0 && np > 0 && bytes && (method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV));
+  std::lock_guard<std::mutex> lock(g_solver_mutex);
+  SolveWs ws;
+  return workspace_layout(n, np, method, nullptr, 0, &ws, bytes);
+}
+
+int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t lda, const double* b, int32_t method,
+                    double rshift, double ashift, double rtol, double atol, double tol_snr, double* x, int32_t* info,
+                    void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(n > 0 && np > 0 && lda >= np && T && A && b && x && workspace);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  std::lock_guard<std::mutex> lock(g_solver_mutex);
+  SolveWs ws;
+  int64_t need = 0;
+  int rc = workspace_layout(n, np, method, workspace, workspace_bytes, &ws, &need);
+  if (rc != QGX_OK) return rc;
+  cudaStream_t st = as_cuda(stream);
+  if ((rc = solve_gram(T, n, b, method, rshift, ashift, rtol, atol, tol_snr, ws, info, st)) != QGX_OK) return rc;
+  return project(A, n, np, lda, ws.y, ws.part, x, st);
+}
+
+int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, const double* b, int32_t method,
+                 double rshift, double ashift, double rtol, double atol, double tol_snr, double* x, int32_t* info,
+                 void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(n > 0 && np > 0 && lda >= np && S && A && b && x && workspace);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  // the per-sample SNR truncation of lstsq_pinv_eig needs the full (ns x np) rho matrix
+  if (method == QGX_SOLVE_PINV && tol_snr > 1e-6) return QGX_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_solver_mutex);
+  SolveWs ws;
+  int64_t need = 0;
+  int rc = workspace_layout(np, n, method, workspace, workspace_bytes, &ws, &need);
+  if (rc != QGX_OK) return rc;
+  cudaStream_t st = as_cuda(stream);
+  // F = A^T b into ws.f, then S x = F
+  if ((rc = project(A, n, np, lda, b, ws.part, ws.f, st)) != QGX_OK) return rc;
+  if ((rc = solve_gram(S, np, ws.f, method, rshift, ashift, rtol, atol, 0.0, ws, info, st)) != QGX_OK) return rc;
+  QGX_CHECK_CUDA(cudaMemcpyAsync(x, ws.y, np * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  return QGX_OK;
+}
+
+}  // extern "C"

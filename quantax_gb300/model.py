@@ -1,0 +1,127 @@
+"""Variational models and their device kernels.
+
+RBM_Dense mirrors quantax/model/shallow_nets.py:35-126: psi(s) = prod_i cosh(W s + b)_i,
+optionally times exp(a.s) (a visible bias, absent in the reference). Parameters are
+flattened in the reference's ravel order: W (M x N, row-major), b (M), then a (N).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .global_defs import get_sites, get_subkeys
+
+
+def _truncated_normal(rng, shape, std):
+    """Normal(0, std^2) truncated at +-2 std, rescaled to unit variance like JAX's
+    variance_scaling("truncated_normal") (quantax/nn/initializers.py:29-57)."""
+    out = rng.standard_normal(shape)
+    bad = np.abs(out) > 2.0
+    while bad.any():
+        out[bad] = rng.standard_normal(int(bad.sum()))
+        bad = np.abs(out) > 2.0
+    return out * std / 0.87962566103423978
+
+
+def _cosh_scale(features: int, n_sites: int, rng) -> float:
+    """Grid search of quantax/model/shallow_nets.py:17-32 for cosh: the scale in [0, 1)
+    whose output std over 1000 normal inputs is closest to 0.1 sqrt(N)."""
+    x = rng.standard_normal((1000, features))
+    target = 0.1 * np.sqrt(n_sites)
+    best, arg = np.inf, 0.0
+    for scale in np.arange(0, 1, 0.01):
+        out = np.sum(np.log(np.abs(np.cosh(x * scale))), axis=1)
+        err = (np.std(out) - target) ** 2
+        if err < best:
+            best, arg = err, scale
+    return float(arg)
+
+
+class RBM_Dense:
+    """Restricted Boltzmann machine with one dense layer, psi = prod cosh(W s + b)."""
+
+    kind = "rbm"
+    holomorphic = False
+
+    def __init__(self, features: int, use_bias: bool = True, dtype=np.float32, visible_bias: bool = False,
+                 init_std: Optional[float] = None, seed: Optional[int] = None):
+        if np.dtype(dtype) != np.float32:
+            raise NotImplementedError("RBM_Dense runs with float32 parameters")
+        sites = get_sites()
+        self.N = sites.Nmodes
+        self.M = int(features)
+        self.use_bias = use_bias
+        self.visible_bias = visible_bias
+        rng = np.random.default_rng(get_subkeys() if seed is None else seed)
+        if init_std is not None:
+            W = rng.normal(0.0, init_std, (self.M, self.N))
+            b = rng.normal(0.0, init_std, self.M) if use_bias else np.zeros(self.M)
+            a = rng.normal(0.0, init_std, self.N) if visible_bias else None
+        else:
+            W = _truncated_normal(rng, (self.M, self.N), 1.0 / np.sqrt(self.N))
+            W *= _cosh_scale(self.M, self.N, rng)
+            b = np.zeros(self.M)
+            a = np.zeros(self.N) if visible_bias else None
+        parts = [W.ravel(), b] + ([a] if a is not None else [])
+        self.init_params = np.concatenate(parts).astype(np.float32)
+
+    @property
+    def nparams(self) -> int:
+        return self.M * self.N + self.M + (self.N if self.visible_bias else 0)
+
+    @classmethod
+    def from_arrays(cls, W, b, a=None):
+        """Model with explicit parameters (W (M, N), b (M), optional a (N))."""
+        obj = cls.__new__(cls)
+        W = np.asarray(W, np.float32)
+        obj.M, obj.N = W.shape
+        obj.use_bias = True
+        obj.visible_bias = a is not None
+        parts = [W.ravel(), np.asarray(b, np.float32)] + ([np.asarray(a, np.float32)] if a is not None else [])
+        obj.init_params = np.concatenate(parts).astype(np.float32)
+        return obj
+
+    # ---- device side ------------------------------------------------------------------------
+    def table_floats(self) -> int:
+        return int(_lib.lib().qgx_rbm_table_floats(self.N, self.M))
+
+    def split(self, params: torch.Tensor):
+        M, N = self.M, self.N
+        W = params[:M * N]
+        b = params[M * N:M * N + M]
+        a = params[M * N + M:] if self.visible_bias else None
+        return W, b, a
+
+    def prepare(self, params: torch.Tensor, table: torch.Tensor) -> None:
+        W, b, a = self.split(params)
+        _lib.call("qgx_rbm_prepare", _lib.ptr(W), _lib.ptr(b), _lib.ptr(a), self.N, self.M, _lib.ptr(table),
+                  _lib.stream_ptr())
+
+    def log_psi(self, table, packed, out):
+        _lib.call("qgx_rbm_log_psi", _lib.ptr(table), self.N, self.M, _lib.ptr(packed), packed.shape[0],
+                  _lib.ptr(out), _lib.stream_ptr())
+
+    def sweep(self, table, packed, log_psi, accepts, nsteps, seed, step0, reweight, proposal, nbr, z, hop):
+        _lib.call("qgx_rbm_sweep", _lib.ptr(table), self.N, self.M, _lib.ptr(packed), _lib.ptr(log_psi),
+                  _lib.ptr(accepts), packed.shape[0], int(nsteps), int(seed), int(step0), float(reweight),
+                  int(proposal), _lib.ptr(nbr), int(z), int(hop), _lib.stream_ptr())
+
+    def eloc(self, table, compiled_op, packed, out):
+        _lib.call("qgx_rbm_eloc", _lib.ptr(table), self.N, self.M, C.byref(compiled_op.struct), _lib.ptr(packed),
+                  packed.shape[0], _lib.ptr(out), _lib.stream_ptr())
+
+    def jacobian(self, table, packed, out):
+        _lib.call("qgx_rbm_jacobian", _lib.ptr(table), self.N, self.M, int(self.visible_bias), _lib.ptr(packed),
+                  packed.shape[0], _lib.ptr(out), out.stride(0), _lib.stream_ptr())
+
+    def obar_workspace_bytes(self, ns: int) -> int:
+        return int(_lib.lib().qgx_rbm_obar_workspace_bytes(self.N, self.M, ns))
+
+    def obar(self, table, packed, r, out, omean, workspace):
+        _lib.call("qgx_rbm_obar", _lib.ptr(table), self.N, self.M, int(self.visible_bias), _lib.ptr(packed),
+                  _lib.ptr(r), packed.shape[0], _lib.ptr(out), out.stride(0), _lib.ptr(omean), _lib.ptr(workspace),
+                  workspace.numel(), _lib.stream_ptr())

@@ -1,0 +1,195 @@
+"""SR / MinSR optimiser (quantax/optimizer/sr.py:17-195) and its solvers
+(quantax/optimizer/solver.py:12-201).
+
+A solver here is a description (regularisation kind, branch and tolerances) that the
+device path executes: Gram matrix on the GPU (FP32 SIMT or tensor cores), FP64 Cholesky
+or FP64 eigendecomposition through cuSOLVER, projection back to parameter space.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Optional
+
+import torch
+
+from . import _lib
+from .state import VS_TYPE
+
+_GRAM_MODES = {"fp32": _lib.GRAM_FP32, "tf32": _lib.GRAM_TF32, "bf16": _lib.GRAM_BF16, "3xtf32": _lib.GRAM_3XTF32}
+
+
+@dataclass(frozen=True)
+class Solver:
+    kind: str                 # "shift" (Cholesky) or "pinv" (eigh)
+    branch: str = "auto"      # "auto", "minnorm" (T = A A^T) or "lstsq" (S = A^T A)
+    rshift: Optional[float] = None
+    ashift: float = 1e-4
+    rtol: Optional[float] = None
+    atol: float = 0.0
+    tol_snr: float = 0.0
+
+    def use_minnorm(self, ns: int, np_: int) -> bool:
+        if self.branch == "auto":
+            return ns < np_
+        return self.branch == "minnorm"
+
+
+def auto_pinv_eig(rtol: Optional[float] = None, atol: float = 0.0, tol_snr: float = 0.0) -> Solver:
+    """solver.py:167-201"""
+    return Solver("pinv", "auto", rtol=rtol, atol=atol, tol_snr=tol_snr)
+
+
+def minnorm_pinv_eig(rtol: Optional[float] = None, atol: float = 0.0, tol_snr: float = 0.0) -> Solver:
+    """solver.py:128-149"""
+    return Solver("pinv", "minnorm", rtol=rtol, atol=atol, tol_snr=tol_snr)
+
+
+def lstsq_pinv_eig(rtol: Optional[float] = None, atol: float = 0.0, tol_snr: float = 0.0) -> Solver:
+    """solver.py:152-164"""
+    return Solver("pinv", "lstsq", rtol=rtol, atol=atol, tol_snr=tol_snr)
+
+
+def auto_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
+    """solver.py:80-91"""
+    return Solver("shift", "auto", rshift=rshift, ashift=ashift)
+
+
+def minnorm_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
+    """solver.py:50-62"""
+    return Solver("shift", "minnorm", rshift=rshift, ashift=ashift)
+
+
+def lstsq_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
+    """solver.py:65-77"""
+    return Solver("shift", "lstsq", rshift=rshift, ashift=ashift)
+
+
+_F64_RTOL = 1e-12  # solver.py:12-21 for the float64 default dtype
+
+
+class QNGD:
+    """Quantum natural gradient descent: solve Obar theta_dot = Ebar (sr.py:17-128)."""
+
+    def __init__(self, state, imag_time: bool = True, solver: Optional[Solver] = None, gram: str = "fp32"):
+        if not imag_time:
+            raise NotImplementedError("real-time evolution is not implemented in quantax_gb300")
+        self._state = state
+        self._imag_time = imag_time
+        self._solver = auto_pinv_eig() if solver is None else solver
+        if gram not in _GRAM_MODES:
+            raise ValueError(f"gram must be one of {sorted(_GRAM_MODES)}")
+        self._gram = _GRAM_MODES[gram]
+        self._Omean = None
+        self._buf = {}
+        self.marks = None  # optional list: solve() appends ("gram", event) after the Gram build
+
+    @property
+    def state(self):
+        return self._state
+
+    @property
+    def vs_type(self):
+        return self._state.vs_type
+
+    def _buffer(self, name, shape, dtype):
+        b = self._buf.get(name)
+        if b is None or tuple(b.shape) != tuple(shape) or b.dtype != dtype:
+            b = torch.empty(shape, dtype=dtype, device=self._state.params.device)
+            self._buf[name] = b
+        return b
+
+    def get_Ebar(self, samples):
+        raise NotImplementedError
+
+    def get_Obar(self, samples) -> torch.Tensor:
+        """Obar = (O - <O>) sqrt(r / Ns) (sr.py:79-88)."""
+        out = self._buffer("obar", (samples.nsamples, self._state.nparams), torch.float32)
+        obar, self._Omean = self._state.obar(samples, out)
+        return obar
+
+    def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
+        """step = solver(Obar, Ebar) in FP64 (sr.py:90-113)."""
+        if self.vs_type != VS_TYPE.real_or_holomorphic:
+            raise NotImplementedError("complex-output states are solved by the stacked real path")
+        A = Obar
+        b = Ebar.to(torch.float64).contiguous()
+        ns, np_ = A.shape
+        sv = self._solver
+        method = _lib.SOLVE_SHIFT if sv.kind == "shift" else _lib.SOLVE_PINV
+        rshift = _F64_RTOL if sv.rshift is None else sv.rshift
+        rtol = _F64_RTOL if sv.rtol is None else sv.rtol
+        x = torch.empty(np_, dtype=torch.float64, device=A.device)
+        info = self._buffer("info", (1,), torch.int32)
+        st = _lib.stream_ptr()
+        L = _lib.lib()
+        import ctypes as C
+        nbytes = C.c_int64(0)
+        if sv.use_minnorm(ns, np_):
+            T = self._buffer("gram", (ns, ns), torch.float64)
+            _lib.call("qgx_gram", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(T), ns, self._gram, st)
+            self._mark("gram")
+            _lib.call("qgx_solve_workspace_bytes", ns, np_, method, C.byref(nbytes))
+            ws = self._state.workspace("solve", nbytes.value)
+            _lib.call("qgx_minsr_solve", _lib.ptr(T), ns, _lib.ptr(A), np_, A.stride(0), _lib.ptr(b), method, rshift,
+                      sv.ashift, rtol, sv.atol, sv.tol_snr, _lib.ptr(x), _lib.ptr(info), _lib.ptr(ws), ws.numel(), st)
+        else:
+            S = self._buffer("gram", (np_, np_), torch.float64)
+            _lib.call("qgx_gram_t", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(S), np_, st)
+            self._mark("gram")
+            _lib.call("qgx_solve_workspace_bytes", np_, ns, method, C.byref(nbytes))
+            ws = self._state.workspace("solve", nbytes.value)
+            _lib.call("qgx_sr_solve", _lib.ptr(S), np_, _lib.ptr(A), ns, A.stride(0), _lib.ptr(b), method, rshift,
+                      sv.ashift, rtol, sv.atol, sv.tol_snr, _lib.ptr(x), _lib.ptr(info), _lib.ptr(ws), ws.numel(), st)
+        return x
+
+    def _mark(self, name: str) -> None:
+        if self.marks is not None:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            self.marks.append((name, ev))
+
+    def get_step(self, samples) -> torch.Tensor:
+        Ebar = self.get_Ebar(samples)
+        Obar = self.get_Obar(samples)
+        return self.solve(Obar, Ebar)
+
+
+class SR(QNGD):
+    """Stochastic reconfiguration; MinSR when Ns < Np (sr.py:131-195)."""
+
+    def __init__(self, state, hamiltonian, imag_time: bool = True, solver: Optional[Solver] = None,
+                 gram: str = "fp32"):
+        super().__init__(state, imag_time, solver, gram)
+        self._hamiltonian = hamiltonian
+        self._stats = None
+
+    @property
+    def hamiltonian(self):
+        return self._hamiltonian
+
+    @property
+    def energy(self) -> Optional[float]:
+        return None if self._stats is None else float(self._stats[0])
+
+    @property
+    def VarE(self) -> Optional[float]:
+        return None if self._stats is None else float(self._stats[2])
+
+    @property
+    def stats(self) -> Optional[torch.Tensor]:
+        """Device tensor [Re energy, Im energy, VarE] of the last step (no sync)."""
+        return self._stats
+
+    def get_Ebar(self, samples) -> torch.Tensor:
+        """Ebar = (E - <E>) sqrt(r / Ns); energy and VarE kept on the device (sr.py:180-195)."""
+        E = self._hamiltonian.Oloc(self._state, samples)
+        ns = samples.nsamples
+        stats = self._buffer("stats", (3,), torch.float64)
+        ebar = torch.empty(ns, dtype=torch.float64, device=E.device)
+        _lib.call("qgx_energy_stats", _lib.ptr(E), None, _lib.ptr(samples.reweight_factor), ns, _lib.ptr(stats),
+                  _lib.ptr(ebar), None, _lib.stream_ptr())
+        self._stats = stats
+        return ebar
+
+
+MinSR = SR

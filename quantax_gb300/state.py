@@ -1,0 +1,194 @@
+"""Variational state: device-resident parameters and the model kernels behind the
+reference's State protocol (quantax/state/variational.py:97-587).
+"""
+from __future__ import annotations
+
+import warnings
+from enum import Enum
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .global_defs import device, get_sites, is_default_cpl
+
+
+class VS_TYPE(Enum):
+    """quantax/state/variational.py:40-94"""
+    real_or_holomorphic = 0
+    non_holomorphic = 1
+    real_to_complex = 2
+
+
+def _words(n: int) -> int:
+    return (n + 31) // 32
+
+
+def pack_spins(spins, n: Optional[int] = None) -> torch.Tensor:
+    """+-1 configurations (numpy or torch, (ns, N)) -> packed int32 words on the device."""
+    dev = device()
+    s = torch.as_tensor(np.asarray(spins) if not isinstance(spins, torch.Tensor) else spins)
+    s = s.reshape(-1, s.shape[-1] if n is None else n).to(device=dev, dtype=torch.int8).contiguous()
+    ns, n = s.shape
+    out = torch.empty((ns, _words(n)), dtype=torch.int32, device=dev)
+    _lib.call("qgx_spins_pack", _lib.ptr(s), _lib.ptr(out), ns, n, _lib.stream_ptr())
+    return out
+
+
+def unpack_spins(packed: torch.Tensor, n: int) -> torch.Tensor:
+    out = torch.empty((packed.shape[0], n), dtype=torch.int8, device=packed.device)
+    _lib.call("qgx_spins_unpack", _lib.ptr(packed), _lib.ptr(out), packed.shape[0], n, _lib.stream_ptr())
+    return out
+
+
+class Variational:
+    """Variational state wrapping a model with device kernels."""
+
+    def __init__(self, model, param_file=None, symm=None, max_parallel=None, use_ref: bool = True):
+        if symm is not None:
+            raise NotImplementedError("symmetry projection is not implemented in quantax_gb300")
+        self._model = model
+        self._dev = device()
+        params = model.init_params
+        if param_file is not None:
+            params = np.load(param_file).astype(np.float32).reshape(-1)
+            if params.size != model.nparams:
+                raise ValueError(f"{param_file} holds {params.size} parameters, the model has {model.nparams}")
+        self._params = torch.as_tensor(params, dtype=torch.float32, device=self._dev).contiguous()
+        self._table = torch.empty(max(model.table_floats(), 4), dtype=torch.float32, device=self._dev)
+        self._flag = torch.zeros(1, dtype=torch.int32, device=self._dev)
+        self._flag_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self._flag_event = None
+        self._use_ref = use_ref
+        is_cpl = is_default_cpl() and getattr(model, "complex_output", False)
+        self._vs_type = VS_TYPE.real_to_complex if is_cpl else VS_TYPE.real_or_holomorphic
+        self._ws = {}
+        self._refresh()
+
+    # ---- properties ----------------------------------------------------------------------
+    @property
+    def model(self):
+        return self._model
+
+    @property
+    def nparams(self) -> int:
+        return self._model.nparams
+
+    @property
+    def Nsites(self) -> int:
+        return get_sites().Nsites
+
+    @property
+    def Nmodes(self) -> int:
+        return get_sites().Nmodes
+
+    @property
+    def vs_type(self) -> VS_TYPE:
+        return self._vs_type
+
+    @property
+    def use_ref(self) -> bool:
+        return self._use_ref
+
+    @property
+    def params(self) -> torch.Tensor:
+        """Flat float32 parameters on the device (reference ravel order)."""
+        return self._params
+
+    @property
+    def table(self) -> torch.Tensor:
+        return self._table
+
+    def _refresh(self) -> None:
+        self._model.prepare(self._params, self._table)
+
+    def workspace(self, name: str, nbytes: int) -> torch.Tensor:
+        """Cached uint8 device buffer of at least nbytes (256-byte aligned by the allocator)."""
+        buf = self._ws.get(name)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=self._dev)
+            self._ws[name] = buf
+        return buf
+
+    # ---- forward ------------------------------------------------------------------------
+    def log_psi_packed(self, packed: torch.Tensor) -> torch.Tensor:
+        out = torch.empty(packed.shape[0], dtype=torch.float32, device=self._dev)
+        self._model.log_psi(self._table, packed, out)
+        return out
+
+    def log_psi(self, s) -> torch.Tensor:
+        return self.log_psi_packed(pack_spins(s, self.Nmodes))
+
+    def __call__(self, s) -> torch.Tensor:
+        """psi(s) as float64 (variational.py:325-347); use log_psi for large systems."""
+        return torch.exp(self.log_psi(s).double())
+
+    def init_internal(self, s):
+        return None
+
+    # ---- local energies and log-derivatives ---------------------------------------------
+    def local_energy(self, op, samples) -> torch.Tensor:
+        out = torch.empty(samples.nsamples, dtype=torch.float64, device=self._dev)
+        self._model.eloc(self._table, op.compiled(), samples.packed, out)
+        return out
+
+    def jacobian(self, s) -> torch.Tensor:
+        """O_sk = d log psi(s) / d theta_k, (ns, nparams) float32 (variational.py:497-511)."""
+        packed = s if isinstance(s, torch.Tensor) and s.dtype == torch.int32 else pack_spins(s, self.Nmodes)
+        out = torch.empty((packed.shape[0], self.nparams), dtype=torch.float32, device=self._dev)
+        self._model.jacobian(self._table, packed, out)
+        return out
+
+    def obar(self, samples, out: Optional[torch.Tensor] = None):
+        """Centred and scaled Obar and the weighted mean Omean (sr.py:76-88)."""
+        ns = samples.nsamples
+        if out is None:
+            out = torch.empty((ns, self.nparams), dtype=torch.float32, device=self._dev)
+        omean = torch.empty(self.nparams, dtype=torch.float64, device=self._dev)
+        ws = self.workspace("obar", self._model.obar_workspace_bytes(ns))
+        self._model.obar(self._table, samples.packed, samples.reweight_factor, out, omean, ws)
+        return out, omean
+
+    # ---- parameter update ------------------------------------------------------------------
+    def _check_last_update(self) -> None:
+        if self._flag_event is not None and self._flag_event.query():
+            if int(self._flag_host[0]) != 0:
+                warnings.warn("Got invalid update step. The update is interrupted.")
+            self._flag_event = None
+
+    def update(self, step: torch.Tensor) -> None:
+        """theta <- theta - step, skipped when step has a non-finite entry
+        (variational.py:558-579). The skip is reported by a warning at the next update."""
+        self._check_last_update()
+        if step.is_complex():
+            step = step.real
+        step = step.to(device=self._dev, dtype=torch.float64).contiguous()
+        if step.numel() != self.nparams:
+            raise ValueError(f"step has {step.numel()} entries, the state has {self.nparams} parameters")
+        _lib.call("qgx_apply_update", _lib.ptr(self._params), _lib.ptr(step), self.nparams, _lib.ptr(self._flag),
+                  _lib.stream_ptr())
+        self._flag_host.copy_(self._flag, non_blocking=True)
+        self._flag_event = torch.cuda.Event()
+        self._flag_event.record()
+        self._refresh()
+
+    def last_update_skipped(self) -> bool:
+        """Synchronises and tells whether the last update was skipped (non-finite step)."""
+        torch.cuda.current_stream().synchronize()
+        self._flag_event = None
+        return int(self._flag_host[0]) != 0
+
+    def get_params_flatten(self) -> torch.Tensor:
+        return self._params.clone()
+
+    def set_params(self, params) -> None:
+        p = torch.as_tensor(params, dtype=torch.float32).reshape(-1)
+        if p.numel() != self.nparams:
+            raise ValueError("wrong number of parameters")
+        self._params.copy_(p.to(self._dev))
+        self._refresh()
+
+    def save(self, file) -> None:
+        np.save(file, self._params.cpu().numpy())

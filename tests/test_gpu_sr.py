@@ -1,0 +1,175 @@
+"""GPU parity of the SR / MinSR pieces and of the whole VMC loop against the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import metropolis, operators as oops, rbm, sr as osr
+
+pytestmark = pytest.mark.gpu
+
+
+def lib():
+    from quantax_gb300 import _lib
+    return _lib
+
+
+def gram(A, mode=0):
+    L = lib()
+    At = torch.as_tensor(A, dtype=torch.float32).cuda().contiguous()
+    n = At.shape[0]
+    T = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    L.call("qgx_gram", L.ptr(At), n, At.shape[1], At.shape[1], L.ptr(T), n, mode, L.stream_ptr())
+    return T.cpu().numpy()
+
+
+@pytest.mark.parametrize("shape", [(64, 144), (300, 1000), (129, 17), (1, 5), (257, 4100)])
+def test_gram_fp32(cuda, shape):
+    A = np.random.default_rng(shape[0]).normal(size=shape).astype(np.float32)
+    T = gram(A)
+    ref = A.astype(np.float64) @ A.astype(np.float64).T
+    # FP32 accumulation over k terms: error ~ sqrt(k) eps |a||b|
+    tol = 4 * np.sqrt(shape[1]) * 6e-8 * np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+    assert (np.abs(T - ref) <= tol + 1e-30).all()
+    assert np.array_equal(T, T.T)
+
+
+def test_gram_transposed(cuda):
+    L = lib()
+    A = np.random.default_rng(3).normal(size=(500, 130)).astype(np.float32)
+    At = torch.as_tensor(A).cuda()
+    S = torch.empty((130, 130), dtype=torch.float64, device="cuda")
+    L.call("qgx_gram_t", L.ptr(At), 500, 130, 130, L.ptr(S), 130, L.stream_ptr())
+    ref = A.astype(np.float64).T @ A.astype(np.float64)
+    np.testing.assert_allclose(S.cpu().numpy(), ref, rtol=1e-5, atol=1e-4)
+
+
+def solve_minsr(A, b, method, **kw):
+    L = lib()
+    At = torch.as_tensor(A, dtype=torch.float32).cuda()
+    bt = torch.as_tensor(b, dtype=torch.float64).cuda()
+    n, np_ = A.shape
+    T = torch.as_tensor(A.astype(np.float32).astype(np.float64) @ A.astype(np.float32).astype(np.float64).T).cuda()
+    nb = C.c_int64(0)
+    L.call("qgx_solve_workspace_bytes", n, np_, method, C.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    x = torch.empty(np_, dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L.call("qgx_minsr_solve", L.ptr(T), n, L.ptr(At), np_, np_, L.ptr(bt), method, kw.get("rshift", 1e-12),
+           kw.get("ashift", 1e-4), kw.get("rtol", 1e-12), kw.get("atol", 0.0), kw.get("tol_snr", 0.0), L.ptr(x),
+           L.ptr(info), L.ptr(ws), ws.numel(), L.stream_ptr())
+    assert int(info.item()) == 0
+    return x.cpu().numpy()
+
+
+@pytest.mark.parametrize("n,np_", [(64, 144), (200, 1000)])
+def test_minsr_shift_solve(cuda, n, np_):
+    rng = np.random.default_rng(n)
+    A = rng.normal(size=(n, np_)).astype(np.float32) / np.sqrt(np_)
+    b = rng.normal(size=n)
+    x = solve_minsr(A, b, 0, ashift=1e-4)
+    ref = osr.minnorm_shift(A.astype(np.float64), b, ashift=1e-4)
+    np.testing.assert_allclose(x, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("tol_snr", [0.0, 0.5])
+def test_minsr_pinv_solve(cuda, tol_snr):
+    rng = np.random.default_rng(7)
+    A = rng.normal(size=(120, 400)).astype(np.float32) / 20
+    b = rng.normal(size=120)
+    x = solve_minsr(A, b, 1, rtol=1e-12, tol_snr=tol_snr)
+    ref = osr.minnorm_pinv(A.astype(np.float64), b, rtol=1e-12, tol_snr=tol_snr)
+    np.testing.assert_allclose(x, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_sr_lstsq_solve(cuda, method):
+    L = lib()
+    rng = np.random.default_rng(9)
+    A = rng.normal(size=(400, 60)).astype(np.float32) / 20
+    b = rng.normal(size=400)
+    At = torch.as_tensor(A).cuda()
+    bt = torch.as_tensor(b).cuda()
+    S = torch.empty((60, 60), dtype=torch.float64, device="cuda")
+    L.call("qgx_gram_t", L.ptr(At), 400, 60, 60, L.ptr(S), 60, L.stream_ptr())
+    nb = C.c_int64(0)
+    L.call("qgx_solve_workspace_bytes", 60, 400, method, C.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    x = torch.empty(60, dtype=torch.float64, device="cuda")
+    L.call("qgx_sr_solve", L.ptr(S), 60, L.ptr(At), 400, 60, L.ptr(bt), method, 1e-12, 1e-4, 1e-12, 0.0, 0.0,
+           L.ptr(x), None, L.ptr(ws), ws.numel(), L.stream_ptr())
+    A64 = A.astype(np.float64)
+    ref = osr.lstsq_shift(A64, b, ashift=1e-4) if method == 0 else osr.lstsq_pinv(A64, b, rtol=1e-12)
+    np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
+
+
+def test_energy_stats(cuda):
+    L = lib()
+    rng = np.random.default_rng(2)
+    E = rng.normal(-10, 1, 1000)
+    r = rng.uniform(0.5, 1.5, 1000)
+    r /= r.mean()
+    Et, rt = torch.as_tensor(E).cuda(), torch.as_tensor(r).cuda()
+    stats = torch.empty(3, dtype=torch.float64, device="cuda")
+    eb = torch.empty(1000, dtype=torch.float64, device="cuda")
+    L.call("qgx_energy_stats", L.ptr(Et), None, L.ptr(rt), 1000, L.ptr(stats), L.ptr(eb), None, L.stream_ptr())
+    want_eb, em, var = osr.ebar(E, r)
+    s = stats.cpu().numpy()
+    assert abs(s[0] - em) < 1e-12 and abs(s[2] - var) < 1e-12 and s[1] == 0.0
+    np.testing.assert_allclose(eb.cpu().numpy(), want_eb, rtol=1e-12, atol=1e-14)
+
+
+def test_update_skips_non_finite(cuda):
+    L = lib()
+    p = torch.ones(1000, dtype=torch.float32, device="cuda")
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    step = torch.full((1000,), 0.25, dtype=torch.float64, device="cuda")
+    L.call("qgx_apply_update", L.ptr(p), L.ptr(step), 1000, L.ptr(flag), L.stream_ptr())
+    assert int(flag.item()) == 0 and torch.all(p == 0.75)
+    step[123] = float("nan")
+    L.call("qgx_apply_update", L.ptr(p), L.ptr(step), 1000, L.ptr(flag), L.stream_ptr())
+    assert int(flag.item()) == 1 and torch.all(p == 0.75)
+
+
+def test_vmc_loop_matches_oracle_and_ed(cuda):
+    """Config 1 through the public API: chain L=8 TFIM h=1, RBM M=16 with visible bias,
+    64 chains, 16 proposals per sweep, SR with diagonal shift 1e-4, lr 1e-2."""
+    import quantax_gb300 as qtx
+    qtx.set_random_seed(0)
+    qtx.sites.Chain(8)
+    H = qtx.operator.Ising(h=1.0)
+    W, b, a = rbm.init_normal(8, 16, 0.01, seed=0, visible_bias=True)
+    state = qtx.state.Variational(qtx.model.RBM_Dense.from_arrays(W, b, a))
+    sampler = qtx.sampler.LocalFlip(state, 64, thermal_steps=0, sweep_steps=16)
+    opt = qtx.optimizer.SR(state, H, solver=qtx.optimizer.auto_shift_eig(ashift=1e-4))
+    # the oracle runs the same Philox stream from the same initial configurations
+    s = sampler.sweep(0).spins.cpu().numpy()
+    assert (s == metropolis.init_uniform(64, 8, qtx.global_defs._splitmix64(0 * 0x100000001B3 + 2))).all()
+    seed = sampler._seed
+    net = rbm.RBM(W, b, a)
+    ops = oops.chain_tfim(8)
+    step0 = 0
+    s, _, _ = metropolis.sweep(net.log_psi, s, 160, seed, step0)
+    sampler.sweep(160)
+    step0 += 160
+    energies, ref_energies = [], []
+    for it in range(100):
+        samples = sampler.sweep()
+        step = opt.get_step(samples)
+        state.update(step * 1e-2)
+        energies.append(opt.energy)
+        if it < 10:
+            s, _, st = metropolis.sweep(net.log_psi, s, 16, seed, step0)
+            step0 += 16
+            assert (samples.spins.cpu().numpy() == s).all(), f"samples diverged at step {it}"
+            E = oops.local_energy(s, ops, net.log_psi).real
+            eb, em, _ = osr.ebar(E)
+            x = osr.solve(osr.obar(net.jacobian(s)), eb, lambda A, b: osr.auto(A, b, "shift", ashift=1e-4))
+            p, _ = osr.update(net.params(), 1e-2 * x)
+            net.set_params(p)
+            ref_energies.append(em)
+            np.testing.assert_allclose(state.params.cpu().numpy(), p, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(energies[:10], ref_energies, rtol=1e-6)
+    e_ed = -10.2516617909660
+    assert abs(np.mean(energies[-10:]) - e_ed) / abs(e_ed) < 0.02

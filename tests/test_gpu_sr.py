@@ -134,7 +134,13 @@ def test_update_skips_non_finite(cuda):
 
 def test_vmc_loop_matches_oracle_and_ed(cuda):
     """Config 1 through the public API: chain L=8 TFIM h=1, RBM M=16 with visible bias,
-    64 chains, 16 proposals per sweep, SR with diagonal shift 1e-4, lr 1e-2."""
+    64 chains, 16 proposals per sweep, SR with diagonal shift 1e-4, lr 1e-2.
+
+    Every step is checked on identical inputs: the oracle takes the device's parameters,
+    runs the same Philox stream from the same configurations (bit-exact samples), and
+    computes E_loc, Obar and the SR update in FP64. Stated FP32 tolerances: energy 1e-6
+    relative, SR update 1e-3 in relative 2-norm (FP32 Obar / E_loc errors of ~1e-7 are
+    amplified by the conditioning of T + 1e-4 I)."""
     import quantax_gb300 as qtx
     qtx.set_random_seed(0)
     qtx.sites.Chain(8)
@@ -143,7 +149,6 @@ def test_vmc_loop_matches_oracle_and_ed(cuda):
     state = qtx.state.Variational(qtx.model.RBM_Dense.from_arrays(W, b, a))
     sampler = qtx.sampler.LocalFlip(state, 64, thermal_steps=0, sweep_steps=16)
     opt = qtx.optimizer.SR(state, H, solver=qtx.optimizer.auto_shift_eig(ashift=1e-4))
-    # the oracle runs the same Philox stream from the same initial configurations
     s = sampler.sweep(0).spins.cpu().numpy()
     assert (s == metropolis.init_uniform(64, 8, qtx.global_defs._splitmix64(0 * 0x100000001B3 + 2))).all()
     seed = sampler._seed
@@ -153,23 +158,24 @@ def test_vmc_loop_matches_oracle_and_ed(cuda):
     s, _, _ = metropolis.sweep(net.log_psi, s, 160, seed, step0)
     sampler.sweep(160)
     step0 += 160
-    energies, ref_energies = [], []
+    energies, errs = [], []
     for it in range(100):
+        if it < 10:
+            net.set_params(state.params.cpu().numpy().astype(np.float64))
         samples = sampler.sweep()
         step = opt.get_step(samples)
-        state.update(step * 1e-2)
         energies.append(opt.energy)
         if it < 10:
             s, _, st = metropolis.sweep(net.log_psi, s, 16, seed, step0)
             step0 += 16
             assert (samples.spins.cpu().numpy() == s).all(), f"samples diverged at step {it}"
             E = oops.local_energy(s, ops, net.log_psi).real
-            eb, em, _ = osr.ebar(E)
+            eb, em, var = osr.ebar(E)
             x = osr.solve(osr.obar(net.jacobian(s)), eb, lambda A, b: osr.auto(A, b, "shift", ashift=1e-4))
-            p, _ = osr.update(net.params(), 1e-2 * x)
-            net.set_params(p)
-            ref_energies.append(em)
-            np.testing.assert_allclose(state.params.cpu().numpy(), p, rtol=1e-5, atol=1e-7)
-    np.testing.assert_allclose(energies[:10], ref_energies, rtol=1e-6)
+            assert abs(opt.energy - em) <= 1e-6 * abs(em)
+            assert abs(opt.VarE - var) <= 1e-4 * var + 1e-9
+            errs.append(np.linalg.norm(step.cpu().numpy() - x) / np.linalg.norm(x))
+        state.update(step * 1e-2)
+    assert max(errs) < 1e-3, errs
     e_ed = -10.2516617909660
     assert abs(np.mean(energies[-10:]) - e_ed) / abs(e_ed) < 0.02

@@ -143,6 +143,26 @@ int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias,
                  const uint32_t* spins, const double* r, int64_t ns, float* Obar, int64_t ldo,
                  double* omean, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
 
+/* qgx_rbm_obar for callers that cannot allocate device memory. No counterpart in the
+ * reference. Some callers are not allowed to call cudaMalloc at all: a JAX/XLA FFI
+ * custom-call handler runs inside the framework's executor, whose device memory belongs
+ * to the framework's allocator, and a serving loop that reserved its HBM budget at start-up
+ * must not allocate while jobs are running. This entry point takes the same inputs and
+ * outputs as qgx_rbm_obar but keeps its scratch (tanh buffer, column partial sums, column
+ * means) in one static device array of QGX_RBM_OBAR_STATIC_SCRATCH_BYTES bytes inside
+ * the library; every GPU that loads the library holds that array until the process exits.
+ * Requests needing more scratch (qgx_rbm_obar_workspace_bytes(n, m, ns) larger than the
+ * array) return QGX_ERR_ARG and nothing is enqueued; qgx_last_error() then says why.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture. All calls
+ * share the array and it keeps the last call's contents (every region is fully written
+ * before it is read, so nothing needs clearing): calls that overlap on the GPU, on
+ * different streams of one device, race on it and must be serialised by the caller. */
+#define QGX_RBM_OBAR_STATIC_SCRATCH_BYTES (32LL << 20)
+int qgx_rbm_obar_noalloc(const float* table, int32_t n, int32_t m, int32_t has_vbias,
+                         const uint32_t* spins, const double* r, int64_t ns, float* Obar,
+                         int64_t ldo, double* omean, qgx_stream_t stream);
+
 /* ---- statistics and centring (quantax/optimizer/sr.py:76-88, 180-195) ----------------- */
 /* energy = Re mean(E r), VarE = mean(|E - energy|^2 r) with compensated FP64 sums;
  * ebar = (E - mean E) sqrt(r / ns). E_im / ebar_im may be NULL for real E.

@@ -67,6 +67,7 @@ SIGNATURES = {
     "qgx_rbm_jacobian": (C.c_int, [vp, i32, i32, i32, vp, i64, vp, i64, vp]),
     "qgx_rbm_obar_workspace_bytes": (i64, [i32, i32, i64]),
     "qgx_rbm_obar": (C.c_int, [vp, i32, i32, i32, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
+    "qgx_rbm_obar_noalloc": (C.c_int, [vp, i32, i32, i32, vp, vp, i64, vp, i64, vp, vp]),
     "qgx_energy_stats": (C.c_int, [vp, vp, vp, i64, vp, vp, vp, vp]),
     "qgx_reweight_factor": (C.c_int, [vp, i64, f32, vp, vp]),
     "qgx_center_columns_workspace_bytes": (i64, [i64, i64]),
@@ -92,7 +93,7 @@ class QgxError(RuntimeError):
 KERNELS_PER_CALL = {
     "qgx_philox4x32_10": 1, "qgx_spins_init_uniform": 1, "qgx_spins_init_fixed_up": 1, "qgx_spins_unpack": 1,
     "qgx_spins_pack": 1, "qgx_operator_diag": 1, "qgx_rbm_prepare": 1, "qgx_rbm_log_psi": 1, "qgx_rbm_sweep": 1,
-    "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
+    "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
     "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_apply_update": 2,
 }
 launch_count = 0

@@ -17,6 +17,8 @@ void set_last_error(cudaError_t e) {
   std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
+void set_last_message(const char* msg) { std::snprintf(g_last_error, sizeof(g_last_error), "%s", msg); }
+
 int launch_status() {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

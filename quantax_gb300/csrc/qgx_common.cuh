@@ -11,6 +11,7 @@ namespace qgx {
 
 // ---- status ---------------------------------------------------------------------------
 void set_last_error(cudaError_t e);
+void set_last_message(const char* msg);
 int launch_status();  // QGX_OK or QGX_ERR_CUDA after a kernel launch
 
 #define QGX_CHECK_ARG(cond)            \

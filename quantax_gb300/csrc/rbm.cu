@@ -14,6 +14,8 @@
 // row is read with one 16-byte shared-memory load per lane and j. theta and t stay in
 // registers for the whole sweep; only the packed spins and log|psi| touch HBM.
 #include <algorithm>
+#include <cstdio>
+#include <mutex>
 
 #include "qgx_colstats.cuh"
 #include "qgx_common.cuh"
@@ -816,6 +818,51 @@ int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias, co
 #define CALL(JT) launch_jacobian<JT>(table, n, m, mp, has_vbias, spins, ns, Obar, ldo, true, mean_f, r, st)
   QGX_DISPATCH_JT(mp, CALL)
 #undef CALL
+}
+
+// ---- no-allocation variant of qgx_rbm_obar -----------------------------------------------
+// Scratch for callers that cannot allocate: one static device array per GPU that loads the
+// library. Host code must not use the symbol's name as an address: the device address is
+// looked up once per device with cudaGetSymbolAddress (with that device current) and cached.
+static __device__ __align__(256) unsigned char g_obar_scratch[QGX_RBM_OBAR_STATIC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxScratchDevices = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_ptr[kMaxScratchDevices] = {};
+
+int scratch_for_current_device(void** out) {
+  int dev = 0;
+  QGX_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxScratchDevices) return QGX_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    QGX_CHECK_CUDA(cudaGetSymbolAddress(&p, g_obar_scratch));
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return QGX_OK;
+}
+}  // namespace
+
+int qgx_rbm_obar_noalloc(const float* table, int32_t n, int32_t m, int32_t has_vbias, const uint32_t* spins,
+                         const double* r, int64_t ns, float* Obar, int64_t ldo, double* omean, qgx_stream_t stream) {
+  QGX_CHECK_ARG(n > 0 && m > 0 && ns > 0);
+  const int64_t need = qgx_rbm_obar_workspace_bytes(n, m, ns);
+  if (need > QGX_RBM_OBAR_STATIC_SCRATCH_BYTES) {
+    char msg[200];
+    std::snprintf(msg, sizeof(msg),
+                  "qgx_rbm_obar_noalloc: n=%d m=%d ns=%lld needs %lld bytes of scratch, the static array holds %lld",
+                  n, m, (long long)ns, (long long)need, (long long)QGX_RBM_OBAR_STATIC_SCRATCH_BYTES);
+    set_last_message(msg);
+    return QGX_ERR_ARG;
+  }
+  void* scratch = nullptr;
+  const int rc = scratch_for_current_device(&scratch);
+  if (rc != QGX_OK) return rc;
+  return qgx_rbm_obar(table, n, m, has_vbias, spins, r, ns, Obar, ldo, omean, scratch,
+                      QGX_RBM_OBAR_STATIC_SCRATCH_BYTES, stream);
 }
 
 }  // extern "C"

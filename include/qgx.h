@@ -186,6 +186,16 @@ int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const doub
  * (full symmetric matrix, row stride ldt). mode = QGX_GRAM_*. */
 int qgx_gram(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt,
              int32_t mode, qgx_stream_t stream);
+/* T = A A^T on the tcgen05 tensor cores: A is FP32 read as TF32 (a_dtype 0) or bf16
+ * (a_dtype 1), FP32 accumulation in TMEM, T written as FP64 (full symmetric matrix).
+ * Needs k > 0, a 16-byte aligned A and lda * element size a multiple of 16 bytes (else
+ * QGX_ERR_UNSUPPORTED). status (device int, may be NULL) is set to QGX_ERR_TIMEOUT if a
+ * bounded pipeline wait expired, else 0. */
+int qgx_gram_tc(const void* A, int32_t a_dtype, int64_t rows, int64_t k, int64_t lda, double* T,
+                int64_t ldt, int32_t* status, qgx_stream_t stream);
+/* bf16 copy of an FP32 matrix (round to nearest even), the operand of the bf16 Gram. */
+int qgx_f32_to_bf16(const float* in, int64_t rows, int64_t k, int64_t ldi, uint16_t* out,
+                    int64_t ldo, qgx_stream_t stream);
 /* S = A^T A (k x k) for the SR branch (Ns >= Np). */
 int qgx_gram_t(const float* A, int64_t rows, int64_t k, int64_t lda, double* S, int64_t lds,
                qgx_stream_t stream);

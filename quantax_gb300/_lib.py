@@ -74,6 +74,8 @@ SIGNATURES = {
     "qgx_center_columns": (C.c_int, [vp, i64, i64, i64, vp, vp, vp, i64, vp]),
     "qgx_gram": (C.c_int, [vp, i64, i64, i64, vp, i64, i32, vp]),
     "qgx_gram_t": (C.c_int, [vp, i64, i64, i64, vp, i64, vp]),
+    "qgx_gram_tc": (C.c_int, [vp, i32, i64, i64, i64, vp, i64, vp, vp]),
+    "qgx_f32_to_bf16": (C.c_int, [vp, i64, i64, i64, vp, i64, vp]),
     "qgx_solve_workspace_bytes": (C.c_int, [i64, i64, i32, C.POINTER(i64)]),
     "qgx_minsr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_sr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
@@ -94,7 +96,7 @@ KERNELS_PER_CALL = {
     "qgx_philox4x32_10": 1, "qgx_spins_init_uniform": 1, "qgx_spins_init_fixed_up": 1, "qgx_spins_unpack": 1,
     "qgx_spins_pack": 1, "qgx_operator_diag": 1, "qgx_rbm_prepare": 1, "qgx_rbm_log_psi": 1, "qgx_rbm_sweep": 1,
     "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
-    "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_apply_update": 2,
+    "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_apply_update": 2,
 }
 launch_count = 0
 

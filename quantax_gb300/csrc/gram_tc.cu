@@ -1,8 +1,349 @@
-// Tensor-core Gram paths (tcgen05). Placeholder until the tcgen05 kernel lands.
+// Tensor-core Gram matrix T = A A^T on sm_103a with tcgen05 (quantax/optimizer/solver.py:139).
+//
+// One CTA computes one 128 x 128 tile of T on or below the diagonal:
+//   warp 1 / lane 0  TMA producer: 128 x 128-byte K-major tiles of the row block and of the
+//                    column block, 128B-swizzled, into a ring of kStages shared-memory stages;
+//   warp 2 / lane 0  MMA issuer: tcgen05.mma M=128 N=128 (K = 8 for tf32, 16 for bf16; four
+//                    per 128-byte k-block), accumulator in 128 TMEM columns, tcgen05.commit
+//                    frees a stage when its MMAs are done;
+//   all 4 warps      epilogue: tcgen05.ld of the accumulator (warp w owns TMEM lanes
+//                    32w..32w+31, i.e. tile rows), FP64 stores of the tile and its mirror,
+//                    both coalesced (the direct tile goes through a shared-memory transpose).
+// Every mbarrier wait is bounded by a wall-clock limit; a wait that runs out records
+// QGX_ERR_TIMEOUT in the optional status word, the CTA releases its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
 #include "qgx_common.cuh"
 
 namespace qgx {
-int gram_tc(const float*, int64_t, int64_t, int64_t, double*, int64_t, int, cudaStream_t) {
+namespace {
+
+constexpr int kTile = 128;          // rows / columns of a T tile
+constexpr int kRowBytes = 128;      // bytes of one operand row per k-block (one swizzle atom)
+constexpr int kStageBytes = 2 * kTile * kRowBytes;  // A block + B block
+constexpr int kStages = 3;
+constexpr int kThreads = 128;
+constexpr uint32_t kTmemCols = 128;
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
+
+__device__ inline uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ inline uint64_t global_timer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ inline void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ inline void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ inline bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false when the phase did not complete within kWaitLimitNs
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_timer() - t0 > kWaitLimitNs) return false;
+  }
+  return true;
+}
+
+__device__ inline void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ inline void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ inline void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand tile, 128-byte rows, 128B swizzle: 8-row core groups 1024 bytes apart
+__device__ inline uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: 8 rows x 128 bytes
+  d |= (uint64_t)1 << 46;                   // descriptor version of tcgen05
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: FP32 accumulator, K-major A and B, M = N = 128
+template <int KIND>
+constexpr uint32_t instr_desc() {
+  // operand format: tf32 = 2 (kind::tf32), bf16 = 1 (kind::f16)
+  return (1u << 4) | ((KIND == 0 ? 2u : 1u) << 7) | ((KIND == 0 ? 2u : 1u) << 10) | ((uint32_t)(kTile >> 3) << 17) |
+         ((uint32_t)(kTile >> 4) << 24);
+}
+
+template <int KIND>
+__device__ inline void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  if (KIND == 0) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(instr_desc<KIND>()), "r"(accumulate));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(instr_desc<KIND>()), "r"(accumulate));
+  }
+}
+
+__device__ inline void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ inline void tmem_ld_32cols(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ inline void record_status(int32_t* status, int code) {
+  if (status) atomicExch(status, code);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 1)
+    gram_tc_kernel(const __grid_constant__ CUtensorMap tmap, int64_t n, int64_t nkb, double* __restrict__ T,
+                   int64_t ldt, int32_t* __restrict__ status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* done = empty + kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* fail = reinterpret_cast<int*>(tmem_slot + 1);
+
+  // lower-triangular tile index -> (bi, bj), bi >= bj
+  const int64_t tile = blockIdx.x;
+  int64_t bi = (int64_t)((sqrt(8.0 * (double)tile + 1.0) - 1.0) * 0.5);
+  while ((bi + 1) * (bi + 2) / 2 <= tile) ++bi;
+  while (bi * (bi + 1) / 2 > tile) --bi;
+  const int64_t bj = tile - bi * (bi + 1) / 2;
+  const int row0 = (int)(bi * kTile), col0 = (int)(bj * kTile);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  constexpr int kElems = KIND == 0 ? 32 : 64;  // elements per 128-byte k-block
+
+  if (warp == 1 && lane == 0) {
+    for (int64_t kb = 0; kb < nkb; ++kb) {
+      const int s = (int)(kb % kStages);
+      const uint32_t ph = (uint32_t)((kb / kStages) & 1);
+      if (!mbar_wait(&empty[s], ph ^ 1u)) {
+        *fail = 1;
+        break;
+      }
+      uint8_t* a = smem + s * kStageBytes;
+      uint8_t* b = a + kTile * kRowBytes;
+      mbar_expect_tx(&full[s], kStageBytes);
+      tma_load_2d(a, &tmap, &full[s], (int)(kb * kElems), row0);
+      tma_load_2d(b, &tmap, &full[s], (int)(kb * kElems), col0);
+    }
+  } else if (warp == 2 && lane == 0) {
+    for (int64_t kb = 0; kb < nkb; ++kb) {
+      const int s = (int)(kb % kStages);
+      const uint32_t ph = (uint32_t)((kb / kStages) & 1);
+      if (!mbar_wait(&full[s], ph)) {
+        *fail = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint64_t da = smem_desc_sw128(smem_u32(smem + s * kStageBytes));
+      const uint64_t db = smem_desc_sw128(smem_u32(smem + s * kStageBytes + kTile * kRowBytes));
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)  // 32 bytes of K per instruction
+        mma<KIND>(tmem, da + 2 * kk, db + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
+      mma_commit(&empty[s]);
+    }
+    mma_commit(done);
+  }
+
+  // epilogue
+  if (!mbar_wait(done, 0)) *fail = 1;
+  __syncthreads();
+  if (*fail) {
+    if (threadIdx.x == 0) record_status(status, QGX_ERR_TIMEOUT);
+  } else {
+    tc_fence_after();
+    float* tr = reinterpret_cast<float*>(smem) + warp * 32 * 33;  // stage memory is free now
+    const int r_local = 32 * warp + lane;
+    for (int c = 0; c < kTile / 32; ++c) {
+      float v[32];
+      tmem_ld_32cols(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * c), v);
+      // mirror: T[col][row], consecutive lanes -> consecutive rows of T's column
+      const int64_t r = row0 + r_local;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int64_t cc = col0 + 32 * c + j;
+        if (r < n && cc < n) T[cc * ldt + r] = (double)v[j];
+      }
+      if (bi != bj) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) tr[lane * 33 + j] = v[j];
+        __syncwarp();
+        const int64_t cc = col0 + 32 * c + lane;
+        for (int j = 0; j < 32; ++j) {
+          const int64_t rr = row0 + 32 * warp + j;
+          if (rr < n && cc < n) T[rr * ldt + cc] = (double)tr[j * 33 + lane];
+        }
+        __syncwarp();
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static std::once_flag once;
+  static EncodeTiled fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+constexpr size_t kSmemBytes = 1024 + kStages * kStageBytes + 256;
+
+template <int KIND>
+int launch_gram_tc(const void* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt, int32_t* status,
+                   cudaStream_t st) {
+  const int esize = KIND == 0 ? 4 : 2;
+  const int elems = KIND == 0 ? 32 : 64;
+  // TMA: 16-byte aligned base and row stride
+  if ((reinterpret_cast<uintptr_t>(A) & 15) || ((lda * esize) & 15)) return QGX_ERR_UNSUPPORTED;
+  if (rows > 0x7fffffffLL || k > 0x7fffffffLL) return QGX_ERR_UNSUPPORTED;
+  EncodeTiled enc = encode_fn();
+  if (!enc) return QGX_ERR_UNSUPPORTED;
+  CUtensorMap map;
+  const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)(lda * esize)};
+  const cuuint32_t box[2] = {(cuuint32_t)elems, (cuuint32_t)kTile};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult cr = enc(&map, KIND == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                    const_cast<void*>(A), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return QGX_ERR_UNSUPPORTED;
+  const int64_t nb = (rows + kTile - 1) / kTile;
+  const int64_t tiles = nb * (nb + 1) / 2;
+  const int64_t nkb = (k + elems - 1) / elems;
+  auto kern = gram_tc_kernel<KIND>;
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+  if (status) QGX_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), st));
+  kern<<<(unsigned)tiles, kThreads, kSmemBytes, st>>>(map, rows, nkb, T, ldt, status);
+  return launch_status();
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ in, int64_t rows, int64_t k, int64_t ldi,
+                               __nv_bfloat16* __restrict__ out, int64_t ldo) {
+  const int64_t r = blockIdx.y;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < k; c += (int64_t)gridDim.x * blockDim.x)
+    out[r * ldo + c] = __float2bfloat16_rn(in[r * ldi + c]);
+}
+
+}  // namespace
+
+int gram_tc(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt, int mode, cudaStream_t st) {
+  if (mode == QGX_GRAM_TF32 && k > 0) return launch_gram_tc<0>(A, rows, k, lda, T, ldt, nullptr, st);
   return QGX_ERR_UNSUPPORTED;
 }
+
 }  // namespace qgx
+
+using namespace qgx;
+
+extern "C" {
+
+int qgx_gram_tc(const void* A, int32_t a_dtype, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt,
+                int32_t* status, qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows >= 0 && k > 0 && lda >= k && ldt >= rows && (a_dtype == 0 || a_dtype == 1));
+  if (rows == 0) return QGX_OK;
+  QGX_CHECK_ARG(A && T);
+  if (a_dtype == 0) return launch_gram_tc<0>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
+  return launch_gram_tc<1>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
+}
+
+int qgx_f32_to_bf16(const float* in, int64_t rows, int64_t k, int64_t ldi, uint16_t* out, int64_t ldo,
+                    qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows >= 0 && k >= 0 && ldi >= k && ldo >= k);
+  if (rows == 0 || k == 0) return QGX_OK;
+  QGX_CHECK_ARG(in && out && rows <= 2147483647LL);
+  const unsigned gx = (unsigned)std::min<int64_t>((k + 255) / 256, 64);
+  to_bf16_kernel<<<dim3(gx, (unsigned)std::min<int64_t>(rows, 65535)), 256, 0, as_cuda(stream)>>>(
+      in, std::min<int64_t>(rows, 65535), k, ldi, reinterpret_cast<__nv_bfloat16*>(out), ldo);
+  for (int64_t r0 = 65535; r0 < rows; r0 += 65535) {
+    const int64_t rr = std::min<int64_t>(65535, rows - r0);
+    to_bf16_kernel<<<dim3(gx, (unsigned)rr), 256, 0, as_cuda(stream)>>>(
+        in + r0 * ldi, rr, k, ldi, reinterpret_cast<__nv_bfloat16*>(out) + r0 * ldo, ldo);
+  }
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+"""tcgen05 Gram matrix (TF32 and BF16 operands, FP32 accumulation) against FP64."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def tc_gram(A, dtype):
+    from quantax_gb300 import _lib as L
+    At = torch.as_tensor(A, dtype=torch.float32).cuda().contiguous()
+    rows, k = At.shape
+    src = At
+    if dtype == 1:
+        src = torch.empty((rows, k), dtype=torch.bfloat16, device="cuda")
+        L.call("qgx_f32_to_bf16", L.ptr(At), rows, k, k, L.ptr(src), k, L.stream_ptr())
+        assert torch.equal(src, At.to(torch.bfloat16))
+    T = torch.full((rows, rows), float("nan"), dtype=torch.float64, device="cuda")
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    L.call("qgx_gram_tc", L.ptr(src), dtype, rows, k, k, L.ptr(T), rows, L.ptr(status), L.stream_ptr())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    return T.cpu().numpy()
+
+
+# bound |T - A A^T| <= c ||a_r|| ||a_c||: TF32 keeps 10 mantissa bits, bf16 keeps 7
+TOL = {0: 2.5e-3, 1: 1.0e-2}
+
+
+@pytest.mark.parametrize("dtype", [0, 1])
+@pytest.mark.parametrize("shape", [(128, 64), (300, 1000), (129, 40), (1024, 4160)])
+def test_tc_gram(cuda, dtype, shape):
+    A = np.random.default_rng(shape[0] + shape[1]).normal(size=shape).astype(np.float32)
+    T = tc_gram(A, dtype)
+    A64 = A.astype(np.float64)
+    ref = A64 @ A64.T
+    d = np.sqrt(np.diag(ref))
+    assert np.isfinite(T).all()
+    err = np.abs(T - ref) / np.outer(d, d)
+    assert err.max() < TOL[dtype], err.max()
+    # the mirror of every off-diagonal tile is the same accumulator element
+    np.testing.assert_allclose(T, T.T, rtol=0, atol=TOL[dtype] * np.outer(d, d).max())
+
+
+def test_tc_gram_through_qgx_gram_mode(cuda):
+    from quantax_gb300 import _lib as L
+    A = np.random.default_rng(0).normal(size=(256, 512)).astype(np.float32)
+    At = torch.as_tensor(A).cuda()
+    T = torch.empty((256, 256), dtype=torch.float64, device="cuda")
+    L.call("qgx_gram", L.ptr(At), 256, 512, 512, L.ptr(T), 256, L.GRAM_TF32, L.stream_ptr())
+    ref = A.astype(np.float64) @ A.astype(np.float64).T
+    d = np.sqrt(np.diag(ref))
+    assert (np.abs(T.cpu().numpy() - ref) / np.outer(d, d)).max() < TOL[0]
+
+
+def test_tc_gram_rejects_unaligned_stride(cuda):
+    from quantax_gb300 import _lib as L
+    A = torch.zeros((64, 30), dtype=torch.float32, device="cuda")
+    T = torch.empty((64, 64), dtype=torch.float64, device="cuda")
+    rc = L.lib().qgx_gram_tc(L.ptr(A), 0, 64, 30, 30, L.ptr(T), 64, None, L.stream_ptr())
+    assert rc == L.QGX_ERR_UNSUPPORTED

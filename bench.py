@@ -281,12 +281,17 @@ def main():
     if rank == 0:
         hbm, bf16, src = peaks()
         ns, npar = 8192, state.nparams
-        gram_flop = 2.0 * ns * ns * npar
+        syrk_flop = float(ns) * (ns + 1) * npar  # lower triangle of T = Obar Obar^T, 2 flops per MAC
         t_gram = phases.get("gram", float("nan")) / 1000.0
-        achieved = gram_flop / t_gram / 1e12
-        roof = {"kernel": "qgx_gram (T = Obar Obar^T)", "bound": "tensor", "achieved": achieved, "peak": bf16,
-                "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": f"bf16 dense, {src}",
-                "traffic": None, "algorithmic": f"2*Ns^2*Np = {gram_flop:.3e} FLOP per launch"}
+        achieved = syrk_flop / t_gram / 1e12
+        # tensor-core modes run at the bf16 rate (bf16) or half of it (tf32, split tf32 x3 MMAs)
+        rate = {"bf16": 1.0, "tf32": 0.5, "3xtf32": 0.5 / 3.0, "fp32": None}[args.gram]
+        roof = {"kernel": f"qgx_gram {args.gram} (T = Obar Obar^T)", "bound": "tensor", "achieved": achieved,
+                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": f"bf16 dense, {src}",
+                "mode_peak": None if rate is None else bf16 * rate,
+                "frac_of_mode_peak": None if rate is None else achieved / (bf16 * rate),
+                "traffic": None, "algorithmic": f"Ns(Ns+1)Np = {syrk_flop:.3e} FLOP per launch (symmetric rank-k)",
+                "note": "fp32 runs on the FP32 SIMT pipes; the FP64 cuSOLVER factorisation dominates the step"}
         lat_sorted = sorted(lat)
         p = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(round(q * (len(lat_sorted) - 1))))]
         line = {

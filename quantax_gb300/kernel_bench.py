@@ -1,0 +1,106 @@
+"""Time one qgx kernel on synthetic data (the command line behind the profiles).
+
+    python -m quantax_gb300.kernel_bench gram --mode tf32 --rows 2048 --k 16640 --reps 3
+    python -m quantax_gb300.kernel_bench sweep --ns 8192 --n 64 --m 256 --steps 64
+    python -m quantax_gb300.kernel_bench eloc --ns 8192 --n 64 --m 256
+    python -m quantax_gb300.kernel_bench obar --ns 8192 --n 64 --m 256
+
+Prints one JSON line with the mean device time per launch (CUDA events, after warm-up).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+import torch
+
+from . import _build, _lib as L
+
+
+def _events(fn, reps, warmup=2):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _rbm(n, m, ns, seed=0):
+    rng = np.random.default_rng(seed)
+    W = torch.as_tensor(rng.normal(0, 0.01, (m, n)).astype(np.float32)).cuda()
+    b = torch.as_tensor(rng.normal(0, 0.01, m).astype(np.float32)).cuda()
+    table = torch.empty(L.lib().qgx_rbm_table_floats(n, m), dtype=torch.float32, device="cuda")
+    L.call("qgx_rbm_prepare", L.ptr(W), L.ptr(b), None, n, m, L.ptr(table), L.stream_ptr())
+    spins = torch.empty((ns, (n + 31) // 32), dtype=torch.int32, device="cuda")
+    L.call("qgx_spins_init_uniform", L.ptr(spins), ns, n, 5, L.stream_ptr())
+    return table, spins
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("kernel", choices=["gram", "sweep", "eloc", "obar"])
+    ap.add_argument("--mode", default="tf32", choices=["fp32", "tf32", "bf16", "3xtf32"])
+    ap.add_argument("--rows", type=int, default=2048)
+    ap.add_argument("--k", type=int, default=16640)
+    ap.add_argument("--ns", type=int, default=8192)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--m", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args()
+    _build.build()
+    st = L.stream_ptr()
+    out = {"kernel": a.kernel}
+    if a.kernel == "gram":
+        A = torch.randn((a.rows, a.k), dtype=torch.float32, device="cuda") * 1e-2
+        T = torch.empty((a.rows, a.rows), dtype=torch.float64, device="cuda")
+        if a.mode == "bf16":
+            Ab = torch.empty((a.rows, a.k), dtype=torch.bfloat16, device="cuda")
+            L.call("qgx_f32_to_bf16", L.ptr(A), a.rows, a.k, a.k, L.ptr(Ab), a.k, st)
+            fn = lambda: L.call("qgx_gram_tc", L.ptr(Ab), 1, a.rows, a.k, a.k, L.ptr(T), a.rows, None, st)
+        else:
+            mode = {"fp32": L.GRAM_FP32, "tf32": L.GRAM_TF32, "3xtf32": L.GRAM_3XTF32}[a.mode]
+            fn = lambda: L.call("qgx_gram", L.ptr(A), a.rows, a.k, a.k, L.ptr(T), a.rows, mode, st)
+        ms = _events(fn, a.reps)
+        syrk = float(a.rows) * (a.rows + 1) * a.k
+        out.update(mode=a.mode, rows=a.rows, k=a.k, ms=ms, syrk_tflops=syrk / ms / 1e9,
+                   gemm_equiv_tflops=2.0 * a.rows * a.rows * a.k / ms / 1e9)
+    else:
+        table, spins = _rbm(a.n, a.m, a.ns)
+        if a.kernel == "sweep":
+            lp = torch.empty(a.ns, dtype=torch.float32, device="cuda")
+            fn = lambda: L.call("qgx_rbm_sweep", L.ptr(table), a.n, a.m, L.ptr(spins), L.ptr(lp), None, a.ns,
+                                a.steps, 7, 0, 2.0, L.PROPOSAL_LOCAL_FLIP, None, 0, 1, st)
+            ms = _events(fn, a.reps)
+            out.update(ns=a.ns, n=a.n, m=a.m, steps=a.steps, ms=ms,
+                       proposals_per_s=a.ns * a.steps / ms * 1e3)
+        elif a.kernel == "eloc":
+            import quantax_gb300 as qtx
+            qtx.sites.Chain(a.n)
+            op = qtx.operator.Ising(h=1.0).compiled()
+            import ctypes as C
+            E = torch.empty(a.ns, dtype=torch.float64, device="cuda")
+            fn = lambda: L.call("qgx_rbm_eloc", L.ptr(table), a.n, a.m, C.byref(op.struct), L.ptr(spins), a.ns,
+                                L.ptr(E), st)
+            ms = _events(fn, a.reps)
+            out.update(ns=a.ns, n=a.n, m=a.m, ms=ms, samples_per_s=a.ns / ms * 1e3)
+        else:
+            np_ = a.m * a.n + a.m
+            O = torch.empty((a.ns, np_), dtype=torch.float32, device="cuda")
+            om = torch.empty(np_, dtype=torch.float64, device="cuda")
+            ws = torch.empty(L.lib().qgx_rbm_obar_workspace_bytes(a.n, a.m, a.ns), dtype=torch.uint8, device="cuda")
+            fn = lambda: L.call("qgx_rbm_obar", L.ptr(table), a.n, a.m, 0, L.ptr(spins), None, a.ns, L.ptr(O), np_,
+                                L.ptr(om), L.ptr(ws), ws.numel(), st)
+            ms = _events(fn, a.reps)
+            out.update(ns=a.ns, np=np_, ms=ms, obar_write_gbs=a.ns * np_ * 4 / ms / 1e6)
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

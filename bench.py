@@ -146,41 +146,44 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--gram", default="fp32", choices=["fp32", "tf32", "bf16", "3xtf32"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    args = ap.parse_args()
+WORKLOAD_RESCONV = dict(workload="j1j2_square10_resconv8x16_minsr16384", lattice="Square(10) PBC, Sz=0",
+                        hamiltonian="Heisenberg(J=[1, 0.5], n_neighbor=[1, 2], msr=True)",
+                        model="ResConv(8 blocks, 16 channels, complex output)", nparams=34944,
+                        sampler="SpinExchange", chains=16384, proposals_per_sweep=200, thermal_proposals=200,
+                        solver="minnorm_shift_eig(ashift=1e-4) on the stacked [Re; Im] 32768 x 34944 matrix",
+                        l2="Obar (4.6 GB) and T (8.6 GB) exceed the 129 MB L2 every step")
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        run_reference(args, rank)
-        return
 
+def build_workload(qtx, rank, gram, solve, workload="rbm"):
+    import numpy as np
+    qtx.set_random_seed(1234 + rank)
+    solver = qtx.optimizer.minnorm_shift_eig(ashift=1e-4, precision=solve)
+    if workload == "resconv":
+        qtx.set_default_dtype(np.complex128)
+        qtx.sites.Square(10, Nparticles=(50, 50))
+        H = qtx.operator.Heisenberg(J=[1.0, 0.5], n_neighbor=[1, 2], msr=True)
+        state = qtx.state.Variational(qtx.model.ResConv(8, 16, out_dtype=np.complex64))
+        sampler = qtx.sampler.SpinExchange(state, 16384, thermal_steps=200, sweep_steps=200)
+    else:
+        qtx.set_default_dtype(np.float64)
+        qtx.sites.Chain(64)
+        H = qtx.operator.Ising(h=1.0, J=1.0)
+        state = qtx.state.Variational(qtx.model.RBM_Dense(256, init_std=0.01))
+        sampler = qtx.sampler.LocalFlip(state, 8192, thermal_steps=640, sweep_steps=64)
+    opt = qtx.optimizer.SR(state, H, solver=solver, gram=gram)
+    return state, sampler, opt
+
+
+def run_form(args, rank, world, gram, solve, e2e=True, clocks=None):
+    """Warm-up + timed SR steps of one form; returns timings, phases, energies, e2e."""
     import torch
     import torch.distributed as dist
-
-    torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
     import quantax_gb300 as qtx
-    from quantax_gb300 import _build, _lib
+    from quantax_gb300 import _lib
 
-    _build.build()
-    qtx.set_random_seed(1234 + rank)
-    qtx.sites.Chain(64)
-    H = qtx.operator.Ising(h=1.0, J=1.0)
-    state = qtx.state.Variational(qtx.model.RBM_Dense(256, init_std=0.01))
-    sampler = qtx.sampler.LocalFlip(state, 8192, thermal_steps=640, sweep_steps=64)
-    opt = qtx.optimizer.SR(state, H, solver=qtx.optimizer.minnorm_shift_eig(ashift=1e-4), gram=args.gram)
+    state, sampler, opt = build_workload(qtx, rank, gram, solve, args.workload)
     lr = 1e-2
+    energies = []
 
     def sr_step(ev=None):
         def mark(name):
@@ -200,13 +203,13 @@ def main():
         mark("solve")
         state.update(step * lr)
         mark("update")
+        return opt.stats
 
+    stats = []
     for _ in range(args.warmup):
-        sr_step()
+        stats.append(sr_step().clone())
     torch.cuda.synchronize()
-
-    clocks = Clocks(local)
-    if rank == 0:
+    if clocks is not None:
         clocks.start()
     if world > 1:
         dist.barrier()
@@ -214,11 +217,10 @@ def main():
     launches0 = _lib.launch_count
     start = torch.cuda.Event(enable_timing=True)
     start.record()
-    step_events = []
-    phase_events = []
+    step_events, phase_events = [], []
     for _ in range(args.steps):
         ev = []
-        sr_step(ev)
+        stats.append(sr_step(ev).clone())
         phase_events.append(ev)
         step_events.append(ev[-1][1])
     end = torch.cuda.Event(enable_timing=True)
@@ -226,15 +228,13 @@ def main():
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    clk = clocks.stop() if rank == 0 else None
+    clk = clocks.stop() if clocks is not None else None
     launches = _lib.launch_count - launches0
     elapsed = start.elapsed_time(end) / 1000.0
     if world > 1:
         t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
-
-    # per-step latency and per-phase device time
     lat, prev = [], start
     for e in step_events:
         lat.append(prev.elapsed_time(e))
@@ -248,64 +248,123 @@ def main():
     phases = {k: v / args.steps for k, v in phases.items()}
     if "gram" in phases:
         phases["cusolver_and_projection"] = phases.pop("solve")
-    energy = opt.energy
+    energies = [float(x[0]) for x in stats]
+    out = dict(elapsed=elapsed, lat=lat, phases=phases, energies=energies, launches=launches, clocks=clk,
+               nparams=state.nparams)
 
-    # end to end through the public API with host buffers: parameters in from pinned host
-    # memory, energy statistics and updated parameters back every step
-    host_params = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
-    host_params.copy_(state.params.cpu())
-    host_out = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
-    host_stats = torch.empty(3, dtype=torch.float64).pin_memory()
-    torch.cuda.synchronize()
+    if e2e:
+        # end to end through the public API with host buffers: parameters in from pinned host
+        # memory, energy statistics and updated parameters back every step
+        host_params = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
+        host_params.copy_(state.params.cpu())
+        host_out = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
+        host_stats = torch.empty(3, dtype=torch.float64).pin_memory()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            state.params.copy_(host_params, non_blocking=True)
+            state._refresh()
+            sr_step()
+            host_stats.copy_(opt.stats, non_blocking=True)
+            host_out.copy_(state.params, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            host_params.copy_(host_out)
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_s = e0.elapsed_time(e1) / 1000.0
+        if world > 1:
+            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        out["e2e_s"] = e2e_s
+    return out
+
+
+def percentile(lat, q):
+    s = sorted(lat)
+    return s[min(len(s) - 1, int(round(q * (len(s) - 1))))]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--gram", default="fp32", choices=["fp32", "tf32", "bf16", "3xtf32"])
+    ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
+    ap.add_argument("--workload", default="rbm", choices=["rbm", "resconv"],
+                    help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv)")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
     if world > 1:
-        dist.barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        state.params.copy_(host_params, non_blocking=True)
-        state._refresh()
-        sr_step()
-        host_stats.copy_(opt.stats, non_blocking=True)
-        host_out.copy_(state.params, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        host_params.copy_(host_out)
-    e1.record()
-    torch.cuda.synchronize()
-    e2e_s = e0.elapsed_time(e1) / 1000.0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from quantax_gb300 import _build
+    _build.build()
+
+    plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)
+    forms = {}
+    if not args.no_forms:
+        # precision form: tcgen05 TF32 Gram + FP32 Cholesky with FP64 refinement, same seed
+        prec = run_form(args, rank, world, "tf32", "mixed", e2e=False)
+        de = [abs(a - b) / abs(b) for a, b in zip(prec["energies"], plain["energies"])]
+        forms["precision_tf32_gram_mixed_solve"] = {
+            "value": world * args.steps / prec["elapsed"], "unit": UNIT,
+            "ms_per_step": 1000.0 * prec["elapsed"] / args.steps,
+            "p50_step_ms": percentile(prec["lat"], 0.5), "p99_step_ms": percentile(prec["lat"], 0.99),
+            "phases_ms": {k: round(v, 4) for k, v in prec["phases"].items()},
+            "speedup_vs_plain": plain["elapsed"] / prec["elapsed"],
+            "energy_rel_diff_vs_plain_max": max(de), "energy_rel_diff_vs_plain_last": de[-1]}
 
     if rank == 0:
         hbm, bf16, src = peaks()
-        ns, npar = 8192, state.nparams
+        npar = plain["nparams"]
+        ns = 8192 if args.workload == "rbm" else 2 * 16384  # rows of the Gram matrix
+        phases = plain["phases"]
         syrk_flop = float(ns) * (ns + 1) * npar  # lower triangle of T = Obar Obar^T, 2 flops per MAC
         t_gram = phases.get("gram", float("nan")) / 1000.0
         achieved = syrk_flop / t_gram / 1e12
-        # tensor-core modes run at the bf16 rate (bf16) or half of it (tf32, split tf32 x3 MMAs)
         rate = {"bf16": 1.0, "tf32": 0.5, "3xtf32": 0.5 / 3.0, "fp32": None}[args.gram]
         roof = {"kernel": f"qgx_gram {args.gram} (T = Obar Obar^T)", "bound": "tensor", "achieved": achieved,
                 "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": f"bf16 dense, {src}",
                 "mode_peak": None if rate is None else bf16 * rate,
                 "frac_of_mode_peak": None if rate is None else achieved / (bf16 * rate),
                 "traffic": None, "algorithmic": f"Ns(Ns+1)Np = {syrk_flop:.3e} FLOP per launch (symmetric rank-k)",
-                "note": "fp32 runs on the FP32 SIMT pipes; the FP64 cuSOLVER factorisation dominates the step"}
-        lat_sorted = sorted(lat)
-        p = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(round(q * (len(lat_sorted) - 1))))]
+                "note": ("fp32 runs on the FP32 SIMT pipes (its roofline is the FP32 FMA rate); the FP64 cuSOLVER "
+                         "factorisation dominates the plain step")}
+        elapsed = plain["elapsed"]
         line = {
             "metric": METRIC, "value": world * args.steps / elapsed, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 solve)",
-            "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas x{world}", gram=args.gram),
-            "samples_per_s": world * args.steps * ns / elapsed, "p50_step_ms": p(0.5), "p99_step_ms": p(0.99),
-            "phases_ms": {k: round(v, 4) for k, v in phases.items()}, "energy": energy,
-            "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": npar * 4,
+            "data": "synthetic",
+            "config": dict(WORKLOAD if args.workload == "rbm" else WORKLOAD_RESCONV, parallelism=f"replicas x{world}",
+                           gram=args.gram, solve=args.solve),
+            "samples_per_s": world * args.steps * (8192 if args.workload == "rbm" else 16384) / elapsed, "p50_step_ms": percentile(plain["lat"], 0.5),
+            "p99_step_ms": percentile(plain["lat"], 0.99),
+            "phases_ms": {k: round(v, 4) for k, v in phases.items()}, "energy": plain["energies"][-1],
+            "e2e": {"value": world * args.steps / plain["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": npar * 4,
                     "d2h_bytes_per_step": npar * 4 + 24},
-            "gpu_launches": launches, "roofline": roof, "clocks": clk,
+            "gpu_launches": plain["launches"], "roofline": roof, "clocks": plain["clocks"], "forms": forms,
         }
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and args.workload == "rbm":
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line), flush=True)
     if world > 1:

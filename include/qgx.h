@@ -42,6 +42,10 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
 
 #define QGX_SOLVE_SHIFT 0  /* diagonal-shifted Cholesky (minnorm_shift_eig) */
 #define QGX_SOLVE_PINV 1   /* soft pseudo-inverse via eigh (minnorm_pinv_eig) */
+/* diagonal-shifted system solved with an FP32 Cholesky factor and FP64 iterative
+ * refinement against the FP64 matrix (residuals in FP64); info = -1 when the refined
+ * residual stays above 1e-12 relative (the caller then falls back to QGX_SOLVE_SHIFT) */
+#define QGX_SOLVE_SHIFT_MIXED 2
 
 #define QGX_GRAM_FP32 0    /* FP32 SIMT FMA, FP32 accumulation */
 #define QGX_GRAM_TF32 1    /* tcgen05 kind::tf32, FP32 accumulation in TMEM */
@@ -163,6 +167,52 @@ int qgx_rbm_obar_noalloc(const float* table, int32_t n, int32_t m, int32_t has_v
                          const uint32_t* spins, const double* r, int64_t ns, float* Obar,
                          int64_t ldo, double* omean, qgx_stream_t stream);
 
+/* ---- ResConv (quantax/model/conv_nets.py:26-183) ----------------------------------- */
+/* Parameters in the reference's ravel order: per block conv1.weight (C, Cin, 3, 3),
+ * conv1.bias (C), conv2.weight (C, C, 3, 3), conv2.bias (C, absent in the last block);
+ * Cin = 1 in block 0. Supported: L x L periodic lattices with L*L <= 256, C in {4,8,12,16}. */
+int64_t qgx_resconv_nparams(int32_t nblocks, int32_t channels);
+int64_t qgx_resconv_table_floats(int32_t nblocks, int32_t channels);
+/* Reorder the parameters into the kernels' table; re-run after every parameter update. */
+int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, float* table,
+                        qgx_stream_t stream);
+/* log psi(s) as (re, im) float pairs (2*ns floats); im = 0 for real output
+ * (Variational.__call__, quantax/state/variational.py:325-347). */
+int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                        int32_t complex_out, const uint32_t* spins, int64_t ns, float* log_psi,
+                        qgx_stream_t stream);
+int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns);
+/* nsteps SpinExchange proposals per chain (common_samplers.py:58-162, metropolis.py:246-322):
+ * each step proposes for every chain, evaluates the proposals with one batched forward and
+ * accepts in log space on the shared Philox stream. log_psi: (re, im) pairs, in/out
+ * (recomputed at the start). */
+int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                      int32_t complex_out, uint32_t* spins, float* log_psi, int32_t* accepts,
+                      int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0, float reweight,
+                      const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
+                      int64_t workspace_bytes, qgx_stream_t stream);
+/* max_conn = n_f1 + n_f2 of the operator. */
+int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn);
+/* Complex local energies over the compacted connected configurations (Operator.Oloc,
+ * quantax/operator/operator.py:510-562, with the nonzero compaction of :144-165);
+ * eloc_im may be NULL for real output. */
+int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                     int32_t complex_out, const qgx_operator_t* op, const uint32_t* spins, int64_t ns,
+                     double* eloc_re, double* eloc_im, void* workspace, int64_t workspace_bytes,
+                     qgx_stream_t stream);
+
+/* Workspace bytes of qgx_resconv_jacobian (per-CTA activation scratch). */
+int64_t qgx_resconv_jacobian_workspace_bytes(int32_t L, int32_t nblocks, int32_t channels);
+/* Per-sample log-derivatives by a hand-written backward pass: O_re = d Re log psi / d params,
+ * O_im = d Im log psi / d params (complex output; may be NULL for real output), row stride
+ * ldo floats, parameter order as qgx_resconv_prepare (Variational.jacobian,
+ * quantax/state/variational.py:424-511, VS_TYPE real_to_complex :40-94). Passing
+ * O_im = O_re + ns * ldo writes the stacked [Re; Im] matrix of QNGD.solve (sr.py:99-105). */
+int qgx_resconv_jacobian(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                         int32_t complex_out, const uint32_t* spins, int64_t ns, float* O_re,
+                         float* O_im, int64_t ldo, void* workspace, int64_t workspace_bytes,
+                         qgx_stream_t stream);
+
 /* ---- statistics and centring (quantax/optimizer/sr.py:76-88, 180-195) ----------------- */
 /* energy = Re mean(E r), VarE = mean(|E - energy|^2 r) with compensated FP64 sums;
  * ebar = (E - mean E) sqrt(r / ns). E_im / ebar_im may be NULL for real E.
@@ -186,8 +236,10 @@ int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const doub
  * (full symmetric matrix, row stride ldt). mode = QGX_GRAM_*. */
 int qgx_gram(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt,
              int32_t mode, qgx_stream_t stream);
-/* T = A A^T on the tcgen05 tensor cores: A is FP32 read as TF32 (a_dtype 0) or bf16
- * (a_dtype 1), FP32 accumulation in TMEM, T written as FP64 (full symmetric matrix).
+/* T = A A^T on the tcgen05 tensor cores: A is FP32 read as TF32 (a_dtype 0), bf16
+ * (a_dtype 1) or FP32 split in-kernel into TF32 hi + lo parts with T = hi hi^T + hi lo^T +
+ * lo hi^T (a_dtype 2, FP32-class accuracy); FP32 accumulation in TMEM, T written as FP64
+ * (full symmetric matrix).
  * Needs k > 0, a 16-byte aligned A and lda * element size a multiple of 16 bytes (else
  * QGX_ERR_UNSUPPORTED). status (device int, may be NULL) is set to QGX_ERR_TIMEOUT if a
  * bounded pipeline wait expired, else 0. */
@@ -207,7 +259,9 @@ int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* by
 /* MinSR branch: given T = A A^T (n x n FP64, overwritten), b (n), A (n x np FP32):
  *   SHIFT: (T + (rshift tr T + ashift) I) y = b by Cholesky, x = A^T y
  *   PINV:  T = U diag(l) U^T, x = A^T U diag(l+) rho, rho = sum_without_noise(U^T o b)
- * x (np doubles). info (device int, may be NULL) receives the cuSOLVER info. */
+ *   SHIFT_MIXED: as SHIFT, factor in FP32, refined in FP64 (see QGX_SOLVE_SHIFT_MIXED)
+ * x (np doubles). info (device int, may be NULL) receives the cuSOLVER info (-1: the
+ * mixed-precision refinement did not converge). */
 int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t lda,
                     const double* b, int32_t method, double rshift, double ashift,
                     double rtol, double atol, double tol_snr, double* x, int32_t* info,

@@ -24,6 +24,7 @@ PROPOSAL_LOCAL_FLIP = 0
 PROPOSAL_SPIN_EXCHANGE = 1
 SOLVE_SHIFT = 0
 SOLVE_PINV = 1
+SOLVE_SHIFT_MIXED = 2
 GRAM_FP32 = 0
 GRAM_TF32 = 1
 GRAM_BF16 = 2
@@ -68,6 +69,17 @@ SIGNATURES = {
     "qgx_rbm_obar_workspace_bytes": (i64, [i32, i32, i64]),
     "qgx_rbm_obar": (C.c_int, [vp, i32, i32, i32, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "qgx_rbm_obar_noalloc": (C.c_int, [vp, i32, i32, i32, vp, vp, i64, vp, i64, vp, vp]),
+    "qgx_resconv_nparams": (i64, [i32, i32]),
+    "qgx_resconv_table_floats": (i64, [i32, i32]),
+    "qgx_resconv_prepare": (C.c_int, [vp, i32, i32, vp, vp]),
+    "qgx_resconv_log_psi": (C.c_int, [vp, i32, i32, i32, i32, vp, i64, vp, vp]),
+    "qgx_resconv_sweep_workspace_bytes": (i64, [i32, i64]),
+    "qgx_resconv_sweep": (C.c_int, [vp, i32, i32, i32, i32, vp, vp, vp, i64, i32, u64, u64, f32, vp, i32, i32, vp,
+                                    i64, vp]),
+    "qgx_resconv_eloc_workspace_bytes": (i64, [i32, i64, i32]),
+    "qgx_resconv_eloc": (C.c_int, [vp, i32, i32, i32, i32, C.POINTER(Operator), vp, i64, vp, vp, vp, i64, vp]),
+    "qgx_resconv_jacobian_workspace_bytes": (i64, [i32, i32, i32]),
+    "qgx_resconv_jacobian": (C.c_int, [vp, i32, i32, i32, i32, vp, i64, vp, vp, i64, vp, i64, vp]),
     "qgx_energy_stats": (C.c_int, [vp, vp, vp, i64, vp, vp, vp, vp]),
     "qgx_reweight_factor": (C.c_int, [vp, i64, f32, vp, vp]),
     "qgx_center_columns_workspace_bytes": (i64, [i64, i64]),
@@ -95,7 +107,9 @@ class QgxError(RuntimeError):
 KERNELS_PER_CALL = {
     "qgx_philox4x32_10": 1, "qgx_spins_init_uniform": 1, "qgx_spins_init_fixed_up": 1, "qgx_spins_unpack": 1,
     "qgx_spins_pack": 1, "qgx_operator_diag": 1, "qgx_rbm_prepare": 1, "qgx_rbm_log_psi": 1, "qgx_rbm_sweep": 1,
-    "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
+    "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_resconv_prepare": 1,
+    "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6,
+    "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
     "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_apply_update": 2,
 }
 launch_count = 0
@@ -103,7 +117,9 @@ launch_count = 0
 
 def _kernels(name, args):
     if name == "qgx_minsr_solve":
-        return 3 if args[6] == SOLVE_SHIFT else 6
+        return {SOLVE_SHIFT: 3, SOLVE_PINV: 6, SOLVE_SHIFT_MIXED: 36}[args[6]]
+    if name == "qgx_resconv_sweep":
+        return 1 + 3 * int(args[9])
     if name == "qgx_sr_solve":
         return 3 if args[6] == SOLVE_SHIFT else 6
     return KERNELS_PER_CALL.get(name, 0)

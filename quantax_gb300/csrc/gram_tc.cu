@@ -24,9 +24,15 @@ namespace {
 
 constexpr int kTile = 128;          // rows / columns of a T tile
 constexpr int kRowBytes = 128;      // bytes of one operand row per k-block (one swizzle atom)
-constexpr int kStageBytes = 2 * kTile * kRowBytes;  // A block + B block
-constexpr int kStages = 3;
-constexpr int kThreads = 128;
+constexpr int kBlockBytes = kTile * kRowBytes;  // one operand block of a stage
+// KIND 0: tf32, 1: bf16, 2: split tf32 (hi*hi + hi*lo + lo*hi, FP32-class accuracy)
+template <int KIND>
+struct GramCfg {
+  static constexpr int kStageBytes = (KIND == 2 ? 4 : 2) * kBlockBytes;  // A, B (+ A lo, B lo)
+  static constexpr int kStages = KIND == 2 ? 3 : 3;
+  static constexpr int kThreads = KIND == 2 ? 256 : 128;  // KIND 2: warps 4..7 split the operands
+  static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 256;
+};
 constexpr uint32_t kTmemCols = 128;
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
 
@@ -94,13 +100,13 @@ __device__ inline uint64_t smem_desc_sw128(uint32_t saddr) {
 template <int KIND>
 constexpr uint32_t instr_desc() {
   // operand format: tf32 = 2 (kind::tf32), bf16 = 1 (kind::f16)
-  return (1u << 4) | ((KIND == 0 ? 2u : 1u) << 7) | ((KIND == 0 ? 2u : 1u) << 10) | ((uint32_t)(kTile >> 3) << 17) |
+  return (1u << 4) | ((KIND == 1 ? 1u : 2u) << 7) | ((KIND == 1 ? 1u : 2u) << 10) | ((uint32_t)(kTile >> 3) << 17) |
          ((uint32_t)(kTile >> 4) << 24);
 }
 
 template <int KIND>
 __device__ inline void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
-  if (KIND == 0) {
+  if (KIND != 1) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
@@ -138,14 +144,18 @@ __device__ inline void record_status(int32_t* status, int code) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
     gram_tc_kernel(const __grid_constant__ CUtensorMap tmap, int64_t n, int64_t nkb, double* __restrict__ T,
                    int64_t ldt, int32_t* __restrict__ status) {
+  using Cfg = GramCfg<KIND>;
+  constexpr int kStages = Cfg::kStages;
+  constexpr int kStageBytes = Cfg::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
   uint64_t* empty = full + kStages;
-  uint64_t* done = empty + kStages;
+  uint64_t* split = empty + kStages;  // KIND 2: operands split into hi / lo
+  uint64_t* done = split + kStages;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   int* fail = reinterpret_cast<int*>(tmem_slot + 1);
 
@@ -162,6 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+      mbar_init(&split[s], 128);
     }
     mbar_init(done, 1);
     *fail = 0;
@@ -178,7 +189,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  constexpr int kElems = KIND == 0 ? 32 : 64;  // elements per 128-byte k-block
+  constexpr int kElems = KIND == 1 ? 64 : 32;  // elements per 128-byte k-block
 
   if (warp == 1 && lane == 0) {
     for (int64_t kb = 0; kb < nkb; ++kb) {
@@ -189,8 +200,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       uint8_t* a = smem + s * kStageBytes;
-      uint8_t* b = a + kTile * kRowBytes;
-      mbar_expect_tx(&full[s], kStageBytes);
+      uint8_t* b = a + kBlockBytes;
+      mbar_expect_tx(&full[s], 2 * kBlockBytes);
       tma_load_2d(a, &tmap, &full[s], (int)(kb * kElems), row0);
       tma_load_2d(b, &tmap, &full[s], (int)(kb * kElems), col0);
     }
@@ -198,33 +209,72 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int64_t kb = 0; kb < nkb; ++kb) {
       const int s = (int)(kb % kStages);
       const uint32_t ph = (uint32_t)((kb / kStages) & 1);
-      if (!mbar_wait(&full[s], ph)) {
+      if (!mbar_wait(KIND == 2 ? &split[s] : &full[s], ph)) {
         *fail = 1;
         break;
       }
       tc_fence_after();
-      const uint64_t da = smem_desc_sw128(smem_u32(smem + s * kStageBytes));
-      const uint64_t db = smem_desc_sw128(smem_u32(smem + s * kStageBytes + kTile * kRowBytes));
+      const uint32_t base = smem_u32(smem + s * kStageBytes);
+      const uint64_t da = smem_desc_sw128(base);
+      const uint64_t db = smem_desc_sw128(base + kBlockBytes);
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk)  // 32 bytes of K per instruction
         mma<KIND>(tmem, da + 2 * kk, db + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
+      if (KIND == 2) {
+        const uint64_t la = smem_desc_sw128(base + 2 * kBlockBytes);
+        const uint64_t lb = smem_desc_sw128(base + 3 * kBlockBytes);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          mma<KIND>(tmem, da + 2 * kk, lb + 2 * kk, 1u);
+          mma<KIND>(tmem, la + 2 * kk, db + 2 * kk, 1u);
+        }
+      }
       mma_commit(&empty[s]);
     }
     mma_commit(done);
+  } else if (KIND == 2 && warp >= 4) {
+    // split x = hi + lo: hi keeps the 10 explicit mantissa bits the tensor core reads
+    // (written in place), lo = x - hi exactly (second buffer, same swizzled layout)
+    const int t = threadIdx.x - 128;
+    for (int64_t kb = 0; kb < nkb; ++kb) {
+      const int s = (int)(kb % kStages);
+      const uint32_t ph = (uint32_t)((kb / kStages) & 1);
+      if (!mbar_wait(&full[s], ph)) {
+        *fail = 1;
+        break;
+      }
+      float4* x = reinterpret_cast<float4*>(smem + s * kStageBytes);
+      float4* lo = reinterpret_cast<float4*>(smem + s * kStageBytes + 2 * kBlockBytes);
+#pragma unroll 4
+      for (int e = t; e < 2 * kBlockBytes / 16; e += 128) {
+        float4 v = x[e];
+        float4 h;
+        h.x = __uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u);
+        h.y = __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u);
+        h.z = __uint_as_float(__float_as_uint(v.z) & 0xFFFFE000u);
+        h.w = __uint_as_float(__float_as_uint(v.w) & 0xFFFFE000u);
+        x[e] = h;
+        lo[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&split[s])) : "memory");
+    }
   }
 
-  // epilogue
+  // epilogue: warps 0..3 (KIND 0/1) or 4..7 (KIND 2) read TMEM lanes 32 (warp % 4) ...
   if (!mbar_wait(done, 0)) *fail = 1;
   __syncthreads();
+  const bool epi = KIND == 2 ? warp >= 4 : true;
   if (*fail) {
     if (threadIdx.x == 0) record_status(status, QGX_ERR_TIMEOUT);
-  } else {
+  } else if (epi) {
     tc_fence_after();
-    float* tr = reinterpret_cast<float*>(smem) + warp * 32 * 33;  // stage memory is free now
-    const int r_local = 32 * warp + lane;
+    const int q = warp & 3;
+    float* tr = reinterpret_cast<float*>(smem) + q * 32 * 33;  // stage memory is free now
+    const int r_local = 32 * q + lane;
     for (int c = 0; c < kTile / 32; ++c) {
       float v[32];
-      tmem_ld_32cols(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * c), v);
+      tmem_ld_32cols(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * c), v);
       // mirror: T[col][row], consecutive lanes -> consecutive rows of T's column
       const int64_t r = row0 + r_local;
 #pragma unroll
@@ -238,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         const int64_t cc = col0 + 32 * c + lane;
         for (int j = 0; j < 32; ++j) {
-          const int64_t rr = row0 + 32 * warp + j;
+          const int64_t rr = row0 + 32 * q + j;
           if (rr < n && cc < n) T[rr * ldt + cc] = (double)tr[j * 33 + lane];
         }
         __syncwarp();
@@ -270,13 +320,11 @@ EncodeTiled encode_fn() {
   return fn;
 }
 
-constexpr size_t kSmemBytes = 1024 + kStages * kStageBytes + 256;
-
 template <int KIND>
 int launch_gram_tc(const void* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt, int32_t* status,
                    cudaStream_t st) {
-  const int esize = KIND == 0 ? 4 : 2;
-  const int elems = KIND == 0 ? 32 : 64;
+  const int esize = KIND == 1 ? 2 : 4;
+  const int elems = KIND == 1 ? 64 : 32;
   // TMA: 16-byte aligned base and row stride
   if ((reinterpret_cast<uintptr_t>(A) & 15) || ((lda * esize) & 15)) return QGX_ERR_UNSUPPORTED;
   if (rows > 0x7fffffffLL || k > 0x7fffffffLL) return QGX_ERR_UNSUPPORTED;
@@ -287,7 +335,7 @@ int launch_gram_tc(const void* A, int64_t rows, int64_t k, int64_t lda, double* 
   const cuuint64_t strides[1] = {(cuuint64_t)(lda * esize)};
   const cuuint32_t box[2] = {(cuuint32_t)elems, (cuuint32_t)kTile};
   const cuuint32_t estr[2] = {1, 1};
-  CUresult cr = enc(&map, KIND == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+  CUresult cr = enc(&map, KIND == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                     const_cast<void*>(A), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) return QGX_ERR_UNSUPPORTED;
@@ -295,9 +343,10 @@ int launch_gram_tc(const void* A, int64_t rows, int64_t k, int64_t lda, double* 
   const int64_t tiles = nb * (nb + 1) / 2;
   const int64_t nkb = (k + elems - 1) / elems;
   auto kern = gram_tc_kernel<KIND>;
-  QGX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+  constexpr size_t smem = GramCfg<KIND>::kSmem;
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (status) QGX_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), st));
-  kern<<<(unsigned)tiles, kThreads, kSmemBytes, st>>>(map, rows, nkb, T, ldt, status);
+  kern<<<(unsigned)tiles, GramCfg<KIND>::kThreads, smem, st>>>(map, rows, nkb, T, ldt, status);
   return launch_status();
 }
 
@@ -312,6 +361,7 @@ __global__ void to_bf16_kernel(const float* __restrict__ in, int64_t rows, int64
 
 int gram_tc(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt, int mode, cudaStream_t st) {
   if (mode == QGX_GRAM_TF32 && k > 0) return launch_gram_tc<0>(A, rows, k, lda, T, ldt, nullptr, st);
+  if (mode == QGX_GRAM_3XTF32 && k > 0) return launch_gram_tc<2>(A, rows, k, lda, T, ldt, nullptr, st);
   return QGX_ERR_UNSUPPORTED;
 }
 
@@ -323,10 +373,11 @@ extern "C" {
 
 int qgx_gram_tc(const void* A, int32_t a_dtype, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt,
                 int32_t* status, qgx_stream_t stream) {
-  QGX_CHECK_ARG(rows >= 0 && k > 0 && lda >= k && ldt >= rows && (a_dtype == 0 || a_dtype == 1));
+  QGX_CHECK_ARG(rows >= 0 && k > 0 && lda >= k && ldt >= rows && a_dtype >= 0 && a_dtype <= 2);
   if (rows == 0) return QGX_OK;
   QGX_CHECK_ARG(A && T);
   if (a_dtype == 0) return launch_gram_tc<0>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
+  if (a_dtype == 2) return launch_gram_tc<2>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
   return launch_gram_tc<1>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
 }
 

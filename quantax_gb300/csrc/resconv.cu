@@ -1,0 +1,826 @@
+// ResConv kernels (quantax/model/conv_nets.py:26-183): batched forward over packed
+// configurations, the SpinExchange Metropolis step (propose / accept) and local energies
+// over compacted connected configurations.
+//
+// Network: x0 = s repeated over C channels (block 0's residual is repeated over the
+// channels, conv_nets.py:88-91); per block b:
+//   P = x / sqrt(b+1) (/ sqrt 2 in block 0, else gelu), Q = gelu(conv1(P) + b1),
+//   x += conv2(Q) (+ b2 except in the last block);
+// final z = x / sqrt(B+1), complex output z_c + i z_{c+C/2} (pair_cpl), and
+// log psi = logsumexp(z) - log(C' N) (exp_by_scale + ConvSymmetrize over translations).
+// Convolutions: 3x3, circular, cross-correlation. gelu: tanh approximation.
+//
+// Work layout: one CTA holds S samples' activations (three C x N buffers per sample) and
+// the current layer's weights in shared memory; a thread computes all C output channels of
+// one (sample, site) pair, so every weight load is a warp-wide broadcast.
+#include <algorithm>
+#include <cstdio>
+
+#include "qgx_common.cuh"
+
+namespace qgx {
+namespace {
+
+constexpr int kFwdThreads = 256;
+constexpr int kMaxSitesConv = 256;  // L <= 16
+
+struct ConvNet {
+  int L, N, B, C;
+  bool cplx;
+};
+
+// per-layer table: W'[i][tap][o] (cin x 9 x C) then bias[o] (C)
+__host__ __device__ inline int layer_cin(int l, int C) { return l == 0 ? 1 : C; }
+__host__ __device__ inline int64_t layer_floats(int l, int C) { return (int64_t)layer_cin(l, C) * 9 * C + C; }
+__host__ __device__ inline int64_t layer_offset(int l, int C) {
+  int64_t off = 0;
+  for (int k = 0; k < l; ++k) off += layer_floats(k, C);
+  return off;
+}
+inline int64_t table_floats_rc(int B, int C) { return layer_offset(2 * B, C); }
+__host__ __device__ inline int64_t nparams_rc(int B, int C) {
+  // reference ravel order: per block conv1.weight, conv1.bias, conv2.weight, conv2.bias (not in the last block)
+  int64_t n = 0;
+  for (int b = 0; b < B; ++b) {
+    n += (int64_t)C * layer_cin(2 * b, C) * 9 + C;
+    n += (int64_t)C * C * 9 + (b == B - 1 ? 0 : C);
+  }
+  return n;
+}
+
+// params (reference order) -> table
+__global__ void rc_prepare_kernel(const float* __restrict__ params, int B, int C, float* __restrict__ table) {
+  int64_t pofs = 0;
+  for (int l = 0; l < 2 * B; ++l) {
+    const int cin = layer_cin(l, C);
+    const bool has_bias = !(l == 2 * B - 1);
+    const int64_t toff = layer_offset(l, C);
+    const int64_t nw = (int64_t)C * cin * 9;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nw; e += (int64_t)gridDim.x * blockDim.x) {
+      // params weight layout (o, i, ky, kx) -> table (i, tap, o)
+      const int o = (int)(e / (cin * 9));
+      const int rem = (int)(e % (cin * 9));
+      const int i = rem / 9, tap = rem % 9;
+      table[toff + ((int64_t)i * 9 + tap) * C + o] = params[pofs + e];
+    }
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < C; o += gridDim.x * blockDim.x)
+      table[toff + (int64_t)cin * 9 * C + o] = has_bias ? params[pofs + nw + o] : 0.0f;
+    pofs += nw + (has_bias ? C : 0);
+  }
+}
+
+__device__ inline float gelu_tanh(float x) {
+  const float k0 = 0.7978845608028654f;  // sqrt(2 / pi)
+  return 0.5f * x * (1.0f + tanhf(k0 * fmaf(0.044715f * x, x * x, x)));
+}
+
+__device__ inline void stage_floats(float* dst, const float* src, int64_t n) {
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) dst[e] = __ldg(src + e);
+}
+
+// out[a][o][r] = act(sum_{i,tap} W[i][tap][o] in[a][i][nbr(r,tap)] + bias[o]); mode 0: gelu and store,
+// mode 1: accumulate into out (residual add)
+template <int C>
+__device__ inline void conv_layer(const float* __restrict__ in, int cin, float* __restrict__ out,
+                                  const float* __restrict__ w, const int16_t* __restrict__ nbr, int N, int S,
+                                  int mode) {
+  const float* bias = w + cin * 9 * C;
+  for (int it = threadIdx.x; it < S * N; it += blockDim.x) {
+    const int a = it / N, r = it - a * N;
+    int nb[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) nb[t] = nbr[r * 9 + t];
+    float acc[C];
+#pragma unroll
+    for (int o = 0; o < C; ++o) acc[o] = bias[o];
+    const float* ina = in + (int64_t)a * C * N;
+    for (int i = 0; i < cin; ++i) {
+      const float* ini = ina + i * N;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const float v = ini[nb[t]];
+        const float4* wp = reinterpret_cast<const float4*>(w + (i * 9 + t) * C);
+#pragma unroll
+        for (int o4 = 0; o4 < C / 4; ++o4) {
+          const float4 ww = wp[o4];
+          acc[4 * o4] = fmaf(v, ww.x, acc[4 * o4]);
+          acc[4 * o4 + 1] = fmaf(v, ww.y, acc[4 * o4 + 1]);
+          acc[4 * o4 + 2] = fmaf(v, ww.z, acc[4 * o4 + 2]);
+          acc[4 * o4 + 3] = fmaf(v, ww.w, acc[4 * o4 + 3]);
+        }
+      }
+    }
+    float* oa = out + (int64_t)a * C * N + r;
+    if (mode == 0) {
+#pragma unroll
+      for (int o = 0; o < C; ++o) oa[o * N] = gelu_tanh(acc[o]);
+    } else {
+#pragma unroll
+      for (int o = 0; o < C; ++o) oa[o * N] += acc[o];
+    }
+  }
+}
+
+__device__ inline void build_nbr(int16_t* nbr, int L) {
+  const int N = L * L;
+  for (int e = threadIdx.x; e < N * 9; e += blockDim.x) {
+    const int r = e / 9, t = e % 9;
+    const int y = r / L, x = r % L;
+    const int dy = t / 3 - 1, dx = t % 3 - 1;
+    nbr[e] = (int16_t)(((y + dy + L) % L) * L + (x + dx + L) % L);
+  }
+}
+
+// Forward of ncfg packed configurations (nw words each). n_live (device, may be NULL)
+// caps the count at run time. out: (re, im) of log psi per configuration.
+template <int C>
+__global__ void __launch_bounds__(kFwdThreads)
+    rc_forward_kernel(const float* __restrict__ table, ConvNet net, const uint32_t* __restrict__ cfg, int64_t ncfg,
+                      const int64_t* __restrict__ n_live, float2* __restrict__ out, int S) {
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int N = net.N, nw = words_for(N);
+  float* X = sm;
+  float* P = X + (int64_t)S * C * N;
+  float* Q = P + (int64_t)S * C * N;
+  float* Wl = Q + (int64_t)S * C * N;
+  int16_t* nbr = reinterpret_cast<int16_t*>(Wl + C * 9 * C + C);
+  build_nbr(nbr, net.L);
+  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t base = (int64_t)blockIdx.x * S; base < total; base += (int64_t)gridDim.x * S) {
+    const int s_here = (int)(total - base < S ? total - base : S);
+    __syncthreads();
+    for (int e = threadIdx.x; e < S * N; e += blockDim.x) {
+      const int a = e / N, r = e % N;
+      float v = 0.0f;
+      if (a < s_here) v = ((cfg[(base + a) * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
+      for (int c = 0; c < C; ++c) X[((int64_t)a * C + c) * N + r] = v;
+    }
+    for (int b = 0; b < net.B; ++b) {
+      const float scale = rsqrtf((float)(b + 1)) * (b == 0 ? 0.70710678118654752f : 1.0f);
+      const int cin = b == 0 ? 1 : C;
+      __syncthreads();
+      for (int e = threadIdx.x; e < S * cin * N; e += blockDim.x) {
+        const int a = e / (cin * N), rem = e % (cin * N);
+        const float v = X[(int64_t)a * C * N + rem] * scale;
+        P[(int64_t)a * C * N + rem] = b == 0 ? v : gelu_tanh(v);
+      }
+      stage_floats(Wl, table + layer_offset(2 * b, C), layer_floats(2 * b, C));
+      __syncthreads();
+      conv_layer<C>(P, cin, Q, Wl, nbr, N, S, 0);
+      __syncthreads();
+      stage_floats(Wl, table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
+      __syncthreads();
+      conv_layer<C>(Q, C, X, Wl, nbr, N, S, 1);
+    }
+    __syncthreads();
+    // log sum exp over (channel, site) per sample, one warp per sample
+    const float fs = rsqrtf((float)(net.B + 1));
+    const int cp = net.cplx ? C / 2 : C;
+    for (int a = warp; a < s_here; a += kFwdThreads / 32) {
+      const float* xa = X + (int64_t)a * C * N;
+      float m = -INFINITY;
+      for (int e = lane; e < cp * N; e += 32) m = fmaxf(m, xa[e] * fs);
+      m = warp_max(m);
+      float sr = 0.0f, si = 0.0f;
+      for (int e = lane; e < cp * N; e += 32) {
+        const float re = xa[e] * fs - m;
+        const float im = net.cplx ? xa[cp * N + e] * fs : 0.0f;
+        const float ex = expf(re);
+        float sn, cs;
+        sincosf(im, &sn, &cs);
+        sr = fmaf(ex, cs, sr);
+        si = fmaf(ex, sn, si);
+      }
+      sr = warp_sum(sr);
+      si = warp_sum(si);
+      if (lane == 0) {
+        const float lr = m + 0.5f * logf(sr * sr + si * si) - logf((float)(cp * N));
+        out[base + a] = make_float2(lr, atan2f(si, sr));
+      }
+    }
+  }
+}
+
+// ---- SpinExchange step ----------------------------------------------------------------
+// proposal of chain c at draw t: site i uniform among the hopping spins, j uniform in the
+// padded neighbour row of i (-1: no move); writes the swapped configuration and changed flag
+__global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* __restrict__ prop,
+                                  int8_t* __restrict__ changed, int64_t ns, int n, uint64_t seed, uint64_t step,
+                                  const int32_t* __restrict__ nbr, int z, int hop) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const int nw = words_for(n);
+  uint32_t w[8];
+  int total = 0;
+  for (int k = 0; k < nw; ++k) {
+    w[k] = spins[c * nw + k];
+    const uint32_t valid = (32 * k + 32 <= n) ? 0xffffffffu : ((1u << (n - 32 * k)) - 1u);
+    total += __popc((hop > 0 ? w[k] : ~w[k]) & valid);
+  }
+  const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
+  int8_t ch = 0;
+  if (total > 0) {
+    int pick = (int)bounded(r.x, (uint32_t)total);
+    int i = -1;
+    for (int k = 0; k < nw && i < 0; ++k) {
+      const uint32_t valid = (32 * k + 32 <= n) ? 0xffffffffu : ((1u << (n - 32 * k)) - 1u);
+      uint32_t m = (hop > 0 ? w[k] : ~w[k]) & valid;
+      const int cnt = __popc(m);
+      if (pick < cnt) {
+        for (int q = 0; q < pick; ++q) m &= m - 1u;
+        i = 32 * k + __ffs(m) - 1;
+      } else {
+        pick -= cnt;
+      }
+    }
+    int j = nbr[(int64_t)i * z + (int)bounded(r.z, (uint32_t)z)];
+    if (j < 0) j = i;
+    const uint32_t bi = (w[i >> 5] >> (i & 31)) & 1u, bj = (w[j >> 5] >> (j & 31)) & 1u;
+    if (bi != bj) {
+      w[i >> 5] ^= 1u << (i & 31);
+      w[j >> 5] ^= 1u << (j & 31);
+      ch = 1;
+    }
+  }
+  for (int k = 0; k < nw; ++k) prop[c * nw + k] = w[k];
+  changed[c] = ch;
+}
+
+__global__ void rc_accept_kernel(uint32_t* __restrict__ spins, float2* __restrict__ lp,
+                                 const uint32_t* __restrict__ prop, const float2* __restrict__ lp_prop,
+                                 const int8_t* __restrict__ changed, int32_t* __restrict__ accepts, int64_t ns, int n,
+                                 uint64_t seed, uint64_t step, float reweight) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
+  const float rhs = log1pf(-unit_float(r.y));
+  if (changed[c] && reweight * (lp_prop[c].x - lp[c].x) > rhs) {
+    const int nw = words_for(n);
+    for (int k = 0; k < nw; ++k) spins[c * nw + k] = prop[c * nw + k];
+    lp[c] = lp_prop[c];
+    if (accepts) accepts[c] += 1;
+  }
+}
+
+// ---- local energies ----------------------------------------------------------------------
+__device__ inline int bit_at(const uint32_t* s, int k) { return (int)((s[k >> 5] >> (k & 31)) & 1u); }
+
+// number of connected configurations with a non-zero element per sample
+__global__ void rc_conn_count_kernel(qgx_operator_t op, const uint32_t* __restrict__ spins, int64_t ns, int n,
+                                     int64_t* __restrict__ counts) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const uint32_t* s = spins + c * words_for(n);
+  int64_t k = 0;
+  for (int t = 0; t < op.n_f1; ++t) k += op.f1_J[2 * t + bit_at(s, op.f1_i[t])] != 0.0;
+  for (int t = 0; t < op.n_f2; ++t)
+    k += op.f2_J[4 * t + 2 * bit_at(s, op.f2_ij[2 * t]) + bit_at(s, op.f2_ij[2 * t + 1])] != 0.0;
+  counts[c] = k;
+}
+
+// exclusive prefix sum of counts into offsets[0..ns], single block
+__global__ void rc_scan_kernel(const int64_t* __restrict__ counts, int64_t ns, int64_t* __restrict__ offsets) {
+  __shared__ int64_t part[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (ns + blockDim.x - 1) / blockDim.x;
+  const int64_t lo = min(ns, t * per), hi = min(ns, lo + per);
+  int64_t s = 0;
+  for (int64_t i = lo; i < hi; ++i) s += counts[i];
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int64_t acc = 0;
+    for (int k = 0; k < (int)blockDim.x; ++k) {
+      const int64_t v = part[k];
+      part[k] = acc;
+      acc += v;
+    }
+    offsets[ns] = acc;
+  }
+  __syncthreads();
+  int64_t acc = part[t];
+  for (int64_t i = lo; i < hi; ++i) {
+    offsets[i] = acc;
+    acc += counts[i];
+  }
+}
+
+__global__ void rc_conn_write_kernel(qgx_operator_t op, const uint32_t* __restrict__ spins, int64_t ns, int n,
+                                     const int64_t* __restrict__ offsets, uint32_t* __restrict__ conn,
+                                     double* __restrict__ elem) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const int nw = words_for(n);
+  const uint32_t* s = spins + c * nw;
+  int64_t k = offsets[c];
+  for (int t = 0; t < op.n_f1; ++t) {
+    const int i = op.f1_i[t];
+    const double e = op.f1_J[2 * t + bit_at(s, i)];
+    if (e == 0.0) continue;
+    for (int q = 0; q < nw; ++q) conn[k * nw + q] = s[q] ^ ((q == (i >> 5)) ? (1u << (i & 31)) : 0u);
+    elem[k++] = e;
+  }
+  for (int t = 0; t < op.n_f2; ++t) {
+    const int i = op.f2_ij[2 * t], j = op.f2_ij[2 * t + 1];
+    const double e = op.f2_J[4 * t + 2 * bit_at(s, i) + bit_at(s, j)];
+    if (e == 0.0) continue;
+    for (int q = 0; q < nw; ++q) {
+      uint32_t v = s[q];
+      if (q == (i >> 5)) v ^= 1u << (i & 31);
+      if (q == (j >> 5)) v ^= 1u << (j & 31);
+      conn[k * nw + q] = v;
+    }
+    elem[k++] = e;
+  }
+}
+
+// E_loc(s) = diag(s) + sum_k elem_k exp(log psi(s'_k) - log psi(s)), complex
+__global__ void rc_eloc_reduce_kernel(qgx_operator_t op, const uint32_t* __restrict__ spins, int64_t ns, int n,
+                                      const float2* __restrict__ lp, const int64_t* __restrict__ offsets,
+                                      const double* __restrict__ elem, const float2* __restrict__ lp_conn,
+                                      double* __restrict__ er, double* __restrict__ ei) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ns) return;
+  const uint32_t* s = spins + c * words_for(n);
+  double d = op.c0;
+  for (int t = 0; t < op.n_z; ++t) d += op.z_J[t] * (bit_at(s, op.z_i[t]) ? 1.0 : -1.0);
+  for (int t = 0; t < op.n_zz; ++t)
+    d += op.zz_J[t] * ((bit_at(s, op.zz_ij[2 * t]) == bit_at(s, op.zz_ij[2 * t + 1])) ? 1.0 : -1.0);
+  double re = d, im = 0.0;
+  const float2 l0 = lp[c];
+  for (int64_t k = offsets[c]; k < offsets[c + 1]; ++k) {
+    const float2 l = lp_conn[k];
+    const double m = exp((double)l.x - (double)l0.x);
+    const double ph = (double)l.y - (double)l0.y;
+    re += elem[k] * m * cos(ph);
+    im += elem[k] * m * sin(ph);
+  }
+  er[c] = re;
+  if (ei) ei[c] = im;
+}
+
+// ---- per-sample log-derivatives (Variational.jacobian, quantax/state/variational.py:424-511) ----
+__device__ inline float gelu_tanh_grad(float x) {
+  const float k0 = 0.7978845608028654f;
+  const float u = k0 * fmaf(0.044715f * x, x * x, x);
+  const float t = tanhf(u);
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * k0 * fmaf(3.0f * 0.044715f, x * x, 1.0f);
+}
+
+constexpr int kJacThreads = 256;
+
+// dW[o][i][t] += sum_r g[k][o][r] in[i][nbr(r,t)] and db[o] = sum_r g[k][o][r] for both
+// cotangents k, written to the O rows at the layer's parameter offset (reference layout
+// (o, i, ky, kx) then bias). Thread = (cotangent, 4 output channels, input channel, half of
+// the sites); the two halves are summed with a lane shuffle.
+template <int C>
+__device__ inline void weight_grads(const float* __restrict__ g /*[2][C][N]*/, const float* __restrict__ in /*[cin][N]*/,
+                                    int cin, const int16_t* __restrict__ nbr, int N, bool has_bias,
+                                    float* __restrict__ o_re, float* __restrict__ o_im) {
+  constexpr int G = C / 4;
+  const int items = 2 * G * cin * 2;  // cotangent x o-group x input channel x half
+  // every lane of a warp runs the same iterations (blockDim is a multiple of 32), so the
+  // full-warp shuffles below always see all 32 lanes; lanes past `items` add zeros
+  for (int base = 0; base < items; base += blockDim.x) {
+    const int it = base + threadIdx.x;
+    const bool active = it < items;
+    const int half = it & 1;
+    const int rest = active ? it >> 1 : 0;
+    const int i = rest % cin;
+    const int og = (rest / cin) % G;
+    const int k = rest / (cin * G);
+    float acc[4][9];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int t = 0; t < 9; ++t) acc[q][t] = 0.0f;
+    float bacc[4] = {0.f, 0.f, 0.f, 0.f};
+    const float* gk = g + (int64_t)k * C * N + (4 * og) * N;
+    const float* ini = in + (int64_t)i * N;
+    const int r0 = half ? N / 2 : 0, r1 = !active ? 0 : (half ? N : N / 2);
+    for (int r = r0; r < r1; ++r) {
+      float gv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) gv[q] = gk[q * N + r];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const float v = ini[nbr[r * 9 + t]];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q][t] = fmaf(gv[q], v, acc[q][t]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) bacc[q] += gv[q];
+    }
+    // the two halves sit in adjacent lanes (items are laid out half-fastest)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+      for (int t = 0; t < 9; ++t) acc[q][t] += __shfl_xor_sync(0xffffffffu, acc[q][t], 1);
+      bacc[q] += __shfl_xor_sync(0xffffffffu, bacc[q], 1);
+    }
+    if (active && half == 0) {
+      float* row = k == 0 ? o_re : o_im;
+      if (row) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int o = 4 * og + q;
+#pragma unroll
+          for (int t = 0; t < 9; ++t) row[((int64_t)o * cin + i) * 9 + t] = acc[q][t];
+          if (has_bias && i == 0) row[(int64_t)C * cin * 9 + o] = bacc[q];
+        }
+      }
+    }
+  }
+}
+
+// gin[k][i][r] = sum_{t,o} W[o][i][t] g[k][o][nbr(r, 8 - t)] (transposed convolution), WT = W as [t][o][i]
+template <int C>
+__device__ inline void input_grads(const float* __restrict__ g, const float* __restrict__ WT, int cin,
+                                   const int16_t* __restrict__ nbr, int N, float* __restrict__ gin) {
+  for (int it = threadIdx.x; it < 2 * N; it += blockDim.x) {
+    const int k = it / N, r = it - k * N;
+    float acc[C];
+#pragma unroll
+    for (int i = 0; i < C; ++i) acc[i] = 0.0f;
+    const float* gk = g + (int64_t)k * C * N;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int rn = nbr[r * 9 + (8 - t)];
+      for (int o = 0; o < C; ++o) {
+        const float v = gk[o * N + rn];
+        const float4* wp = reinterpret_cast<const float4*>(WT + (t * C + o) * C);
+#pragma unroll
+        for (int i4 = 0; i4 < C / 4; ++i4) {
+          const float4 w = wp[i4];
+          acc[4 * i4] = fmaf(v, w.x, acc[4 * i4]);
+          acc[4 * i4 + 1] = fmaf(v, w.y, acc[4 * i4 + 1]);
+          acc[4 * i4 + 2] = fmaf(v, w.z, acc[4 * i4 + 2]);
+          acc[4 * i4 + 3] = fmaf(v, w.w, acc[4 * i4 + 3]);
+        }
+      }
+    }
+    for (int i = 0; i < cin; ++i) gin[((int64_t)k * C + i) * N + r] = acc[i];
+  }
+}
+
+// stage layer l's table slice into W and its transpose WT[t][o][i]
+template <int C>
+__device__ inline void stage_layer(const float* table, int l, float* W, float* WT) {
+  const int cin = layer_cin(l, C);
+  const float* src = table + layer_offset(l, C);
+  const int nf = cin * 9 * C + C;
+  for (int e = threadIdx.x; e < nf; e += blockDim.x) W[e] = __ldg(src + e);
+  for (int e = threadIdx.x; e < 9 * C * C; e += blockDim.x) {
+    const int t = e / (C * C), o = (e / C) % C, i = e % C;
+    WT[e] = i < cin ? __ldg(src + (i * 9 + t) * C + o) : 0.0f;
+  }
+}
+
+template <int C>
+__global__ void __launch_bounds__(kJacThreads)
+    rc_jacobian_kernel(const float* __restrict__ table, ConvNet net, const uint32_t* __restrict__ spins, int64_t ns,
+                       float* __restrict__ o_re, float* __restrict__ o_im, int64_t ldo, float* __restrict__ scratch) {
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int N = net.N, B = net.B, nw = words_for(N);
+  const int CN = C * N;
+  float* X = sm;                 // [C][N] block input / running activation
+  float* P = X + CN;             // [C][N] pre(X_b)
+  float* Qa = P + CN;            // [C][N] conv1 pre-activation A, then gelu(A)
+  float* G = Qa + CN;            // [2][C][N] cotangent of X
+  float* GA = G + 2 * CN;        // [2][C][N] cotangent of A
+  float* GP = GA + 2 * CN;       // [2][C][N] cotangent of P
+  float* W = GP + 2 * CN;        // layer table slice (C*9*C + C)
+  float* WT = W + C * 9 * C + C; // [9][C][C]
+  int16_t* nbr = reinterpret_cast<int16_t*>(WT + 9 * C * C);
+  __shared__ float red[2][kJacThreads / 32];
+  build_nbr(nbr, net.L);
+  float* mine = scratch + (int64_t)blockIdx.x * B * 2 * CN;  // X_b and A_b of every block
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float fs = rsqrtf((float)(B + 1));
+  const int cp = net.cplx ? C / 2 : C;
+  for (int64_t smp = blockIdx.x; smp < ns; smp += gridDim.x) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < N; e += blockDim.x) {
+      const float v = ((spins[smp * nw + (e >> 5)] >> (e & 31)) & 1u) ? 1.0f : -1.0f;
+      for (int c = 0; c < C; ++c) X[c * N + e] = v;
+    }
+    // ---- forward, saving X_b and A_b
+    for (int b = 0; b < B; ++b) {
+      const float scale = rsqrtf((float)(b + 1)) * (b == 0 ? 0.70710678118654752f : 1.0f);
+      const int cin = b == 0 ? 1 : C;
+      __syncthreads();
+      float* xs = mine + (int64_t)b * 2 * CN;
+      for (int e = threadIdx.x; e < CN; e += blockDim.x) {
+        xs[e] = X[e];
+        const float v = X[e] * scale;
+        if (e < cin * N) P[e] = b == 0 ? v : gelu_tanh(v);
+      }
+      stage_layer<C>(table, 2 * b, W, WT);
+      __syncthreads();
+      // A = conv1(P) + b1 (pre-activation kept: conv_layer mode 1 on a zeroed buffer)
+      for (int e = threadIdx.x; e < CN; e += blockDim.x) Qa[e] = 0.0f;
+      __syncthreads();
+      conv_layer<C>(P, cin, Qa, W, nbr, N, 1, 1);
+      __syncthreads();
+      for (int e = threadIdx.x; e < CN; e += blockDim.x) {
+        xs[CN + e] = Qa[e];
+        Qa[e] = gelu_tanh(Qa[e]);
+      }
+      stage_layer<C>(table, 2 * b + 1, W, WT);
+      __syncthreads();
+      conv_layer<C>(Qa, C, X, W, nbr, N, 1, 1);
+    }
+    __syncthreads();
+    // ---- output cotangents: w = exp(z - logsumexp z)
+    float m = -INFINITY;
+    for (int e = threadIdx.x; e < cp * N; e += blockDim.x) m = fmaxf(m, X[e] * fs);
+    m = warp_max(m);
+    if (lane == 0) red[0][warp] = m;
+    __syncthreads();
+    m = red[0][0];
+    for (int w = 1; w < kJacThreads / 32; ++w) m = fmaxf(m, red[0][w]);
+    __syncthreads();
+    float sr = 0.0f, si = 0.0f;
+    for (int e = threadIdx.x; e < cp * N; e += blockDim.x) {
+      const float ex = expf(X[e] * fs - m);
+      float sn = 0.0f, cs = 1.0f;
+      if (net.cplx) sincosf(X[cp * N + e] * fs, &sn, &cs);
+      sr = fmaf(ex, cs, sr);
+      si = fmaf(ex, sn, si);
+    }
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) {
+      red[0][warp] = sr;
+      red[1][warp] = si;
+    }
+    __syncthreads();
+    sr = 0.0f;
+    si = 0.0f;
+    for (int w = 0; w < kJacThreads / 32; ++w) {
+      sr += red[0][w];
+      si += red[1][w];
+    }
+    // 1 / (sr + i si)
+    const float den = sr * sr + si * si;
+    const float ir = sr / den, ii = -si / den;
+    for (int e = threadIdx.x; e < cp * N; e += blockDim.x) {
+      const float ex = expf(X[e] * fs - m);
+      float sn = 0.0f, cs = 1.0f;
+      if (net.cplx) sincosf(X[cp * N + e] * fs, &sn, &cs);
+      const float ar = ex * cs, ai = ex * sn;
+      const float wr = ar * ir - ai * ii, wi = ar * ii + ai * ir;  // w = exp(z) / sum
+      if (net.cplx) {
+        G[e] = wr * fs;               // d Re / d y_c
+        G[cp * N + e] = -wi * fs;     // d Re / d y_{c+C/2}
+        G[CN + e] = wi * fs;          // d Im / d y_c
+        G[CN + cp * N + e] = wr * fs; // d Im / d y_{c+C/2}
+      } else {
+        G[e] = wr * fs;
+        G[CN + e] = 0.0f;
+      }
+    }
+    // ---- backward
+    float* row_re = o_re + smp * ldo;
+    float* row_im = o_im ? o_im + smp * ldo : nullptr;
+    int64_t poff = nparams_rc(B, C);
+    for (int b = B - 1; b >= 0; --b) {
+      const int cin = b == 0 ? 1 : C;
+      const bool last = b == B - 1;
+      const int64_t n2 = (int64_t)C * C * 9 + (last ? 0 : C);
+      const int64_t n1 = (int64_t)C * cin * 9 + C;
+      poff -= n1 + n2;
+      const float scale = rsqrtf((float)(b + 1)) * (b == 0 ? 0.70710678118654752f : 1.0f);
+      const float* xs = mine + (int64_t)b * 2 * CN;
+      __syncthreads();
+      for (int e = threadIdx.x; e < CN; e += blockDim.x) {
+        const float a = xs[CN + e];
+        Qa[e] = gelu_tanh(a);
+        const float v = xs[e] * scale;
+        if (e < cin * N) P[e] = b == 0 ? v : gelu_tanh(v);
+      }
+      stage_layer<C>(table, 2 * b + 1, W, WT);
+      __syncthreads();
+      // conv2: grads of W2, b2 and of Q (into GA)
+      weight_grads<C>(G, Qa, C, nbr, N, !last, row_re + poff + n1, row_im ? row_im + poff + n1 : nullptr);
+      input_grads<C>(G, WT, C, nbr, N, GA);
+      __syncthreads();
+      for (int e = threadIdx.x; e < 2 * CN; e += blockDim.x) GA[e] *= gelu_tanh_grad(xs[CN + (e % CN)]);
+      stage_layer<C>(table, 2 * b, W, WT);
+      __syncthreads();
+      weight_grads<C>(GA, P, cin, nbr, N, true, row_re + poff, row_im ? row_im + poff : nullptr);
+      if (b > 0) {
+        input_grads<C>(GA, WT, cin, nbr, N, GP);
+        __syncthreads();
+        for (int e = threadIdx.x; e < 2 * CN; e += blockDim.x) {
+          const int ee = e % CN;
+          G[e] += GP[e] * gelu_tanh_grad(xs[ee] * scale) * scale;
+        }
+      }
+    }
+  }
+}
+
+template <int C>
+int launch_jacobian_c(const float* table, const ConvNet& net, const uint32_t* spins, int64_t ns, float* o_re,
+                      float* o_im, int64_t ldo, float* scratch, int64_t scratch_floats, cudaStream_t st) {
+  const int CN = C * net.N;
+  const int64_t sf = 3LL * CN + 6LL * CN + C * 9 * C + C + 9 * C * C;
+  const int smem = (int)(sf * 4 + net.N * 9 * 2 + 16);
+  auto k = rc_jacobian_kernel<C>;
+  if (smem > 48 * 1024) QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int per_sm = 0;
+  QGX_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kJacThreads, smem));
+  if (per_sm < 1) return QGX_ERR_UNSUPPORTED;
+  const int64_t per_cta = (int64_t)net.B * 2 * CN;
+  int64_t grid = std::min<int64_t>((int64_t)device_sm_count() * per_sm, ns);
+  grid = std::min<int64_t>(grid, scratch_floats / per_cta);
+  if (grid < 1) return QGX_ERR_ARG;
+  k<<<(unsigned)grid, kJacThreads, smem, st>>>(table, net, spins, ns, o_re, o_im, ldo, scratch);
+  return launch_status();
+}
+
+int rc_smem_bytes(const ConvNet& net, int S) {
+  const int64_t f = 3LL * S * net.C * net.N + (int64_t)net.C * 9 * net.C + net.C;
+  return (int)(f * 4 + (int64_t)net.N * 9 * 2 + 16);
+}
+
+template <int C>
+int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
+                     float2* out, cudaStream_t st) {
+  const int S = 4;
+  const int smem = rc_smem_bytes(net, S);
+  auto k = rc_forward_kernel<C>;
+  if (smem > 48 * 1024) QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int per_sm = 0;
+  QGX_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kFwdThreads, smem));
+  if (per_sm < 1) return QGX_ERR_UNSUPPORTED;
+  const int64_t want = (ncfg + S - 1) / S;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)device_sm_count() * per_sm, want));
+  k<<<grid, kFwdThreads, smem, st>>>(table, net, cfg, ncfg, n_live, out, S);
+  return launch_status();
+}
+
+int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
+                   float2* out, cudaStream_t st) {
+  switch (net.C) {
+    case 4: return launch_forward_c<4>(table, net, cfg, ncfg, n_live, out, st);
+    case 8: return launch_forward_c<8>(table, net, cfg, ncfg, n_live, out, st);
+    case 12: return launch_forward_c<12>(table, net, cfg, ncfg, n_live, out, st);
+    case 16: return launch_forward_c<16>(table, net, cfg, ncfg, n_live, out, st);
+    default: return QGX_ERR_UNSUPPORTED;
+  }
+}
+
+bool valid_net(int L, int B, int C, int cplx) {
+  return L >= 3 && L * L <= kMaxSitesConv && B >= 1 && B <= 64 && (C == 4 || C == 8 || C == 12 || C == 16) &&
+         (!cplx || C % 2 == 0);
+}
+
+inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
+
+}  // namespace
+}  // namespace qgx
+
+using namespace qgx;
+
+extern "C" {
+
+int64_t qgx_resconv_nparams(int32_t nblocks, int32_t channels) {
+  if (nblocks < 1 || channels < 1) return 0;
+  return nparams_rc(nblocks, channels);
+}
+
+int64_t qgx_resconv_table_floats(int32_t nblocks, int32_t channels) {
+  if (nblocks < 1 || channels < 1) return 0;
+  return table_floats_rc(nblocks, channels);
+}
+
+int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, float* table, qgx_stream_t stream) {
+  QGX_CHECK_ARG(params && table && nblocks >= 1 && (channels == 4 || channels == 8 || channels == 12 || channels == 16));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(table) & 15) == 0);
+  rc_prepare_kernel<<<16, 256, 0, as_cuda(stream)>>>(params, nblocks, channels, table);
+  return launch_status();
+}
+
+int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                        const uint32_t* spins, int64_t ns, float* log_psi, qgx_stream_t stream) {
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi);
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  return launch_forward(table, net, spins, ns, nullptr, reinterpret_cast<float2*>(log_psi), as_cuda(stream));
+}
+
+int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns) {
+  if (L < 1 || ns < 1) return 0;
+  const int nw = words_for(L * L);
+  return al256(ns * nw * 4) + al256(ns * 8) + al256(ns);
+}
+
+int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                      uint32_t* spins, float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed,
+                      uint64_t step0, float reweight, const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
+                      int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && ns >= 0 && nsteps >= 0);
+  QGX_CHECK_ARG(nbr && z > 0 && (hop == 1 || hop == -1));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_workspace_bytes(L, ns));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  cudaStream_t st = as_cuda(stream);
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  const int nw = words_for(net.N);
+  char* ws = static_cast<char*>(workspace);
+  uint32_t* prop = reinterpret_cast<uint32_t*>(ws);
+  float2* lp_prop = reinterpret_cast<float2*>(ws + al256(ns * nw * 4));
+  int8_t* changed = reinterpret_cast<int8_t*>(ws + al256(ns * nw * 4) + al256(ns * 8));
+  float2* lp = reinterpret_cast<float2*>(log_psi);
+  int rc = launch_forward(table, net, spins, ns, nullptr, lp, st);
+  if (rc != QGX_OK) return rc;
+  if (accepts) QGX_CHECK_CUDA(cudaMemsetAsync(accepts, 0, ns * sizeof(int32_t), st));
+  const unsigned g = (unsigned)((ns + 127) / 128);
+  for (int t = 0; t < nsteps; ++t) {
+    rc_propose_kernel<<<g, 128, 0, st>>>(spins, prop, changed, ns, net.N, seed, step0 + t, nbr, z, hop);
+    if ((rc = launch_forward(table, net, prop, ns, nullptr, lp_prop, st)) != QGX_OK) return rc;
+    rc_accept_kernel<<<g, 128, 0, st>>>(spins, lp, prop, lp_prop, changed, accepts, ns, net.N, seed, step0 + t,
+                                        reweight);
+  }
+  return launch_status();
+}
+
+int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn) {
+  if (L < 1 || ns < 1 || max_conn < 0) return 0;
+  const int nw = words_for(L * L);
+  const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
+  return al256(ns * 8) + al256((ns + 1) * 8) + al256(nc * nw * 4) + al256(nc * 8) + al256(nc * 8) + al256(ns * 8);
+}
+
+int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                     const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im,
+                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(op && valid_net(L, nblocks, channels, complex_out) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && eloc_re && workspace);
+  const int max_conn = op->n_f1 + op->n_f2;
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_workspace_bytes(L, ns, max_conn));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  cudaStream_t st = as_cuda(stream);
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  const int nw = words_for(net.N);
+  const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
+  char* ws = static_cast<char*>(workspace);
+  int64_t off = 0;
+  auto take = [&](int64_t b) {
+    char* p = ws + off;
+    off += al256(b);
+    return p;
+  };
+  int64_t* counts = reinterpret_cast<int64_t*>(take(ns * 8));
+  int64_t* offsets = reinterpret_cast<int64_t*>(take((ns + 1) * 8));
+  uint32_t* conn = reinterpret_cast<uint32_t*>(take(nc * nw * 4));
+  double* elem = reinterpret_cast<double*>(take(nc * 8));
+  float2* lp_conn = reinterpret_cast<float2*>(take(nc * 8));
+  float2* lp = reinterpret_cast<float2*>(take(ns * 8));
+  const unsigned g = (unsigned)((ns + 127) / 128);
+  rc_conn_count_kernel<<<g, 128, 0, st>>>(*op, spins, ns, net.N, counts);
+  rc_scan_kernel<<<1, 1024, 0, st>>>(counts, ns, offsets);
+  rc_conn_write_kernel<<<g, 128, 0, st>>>(*op, spins, ns, net.N, offsets, conn, elem);
+  int rc = launch_forward(table, net, spins, ns, nullptr, lp, st);
+  if (rc != QGX_OK) return rc;
+  if ((rc = launch_forward(table, net, conn, nc, offsets + ns, lp_conn, st)) != QGX_OK) return rc;
+  rc_eloc_reduce_kernel<<<g, 128, 0, st>>>(*op, spins, ns, net.N, lp, offsets, elem, lp_conn, eloc_re, eloc_im);
+  return launch_status();
+}
+
+int64_t qgx_resconv_jacobian_workspace_bytes(int32_t L, int32_t nblocks, int32_t channels) {
+  if (L < 1 || nblocks < 1 || channels < 1) return 0;
+  // per resident CTA: X_b and A_b of every block; sized for 4 CTAs on each of up to 160 SMs
+  return 4LL * 160 * nblocks * 2 * channels * L * L * 4;
+}
+
+int qgx_resconv_jacobian(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                         const uint32_t* spins, int64_t ns, float* O_re, float* O_im, int64_t ldo, void* workspace,
+                         int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && ns >= 0);
+  QGX_CHECK_ARG(ldo >= qgx_resconv_nparams(nblocks, channels));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && O_re && workspace && workspace_bytes > 0);
+  QGX_CHECK_ARG(!complex_out || O_im);
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  float* scratch = static_cast<float*>(workspace);
+  const int64_t sf = workspace_bytes / 4;
+  cudaStream_t st = as_cuda(stream);
+  switch (channels) {
+    case 4: return launch_jacobian_c<4>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
+    case 8: return launch_jacobian_c<8>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
+    case 12: return launch_jacobian_c<12>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
+    case 16: return launch_jacobian_c<16>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
+    default: return QGX_ERR_UNSUPPORTED;
+  }
+}
+
+}  // extern "C"

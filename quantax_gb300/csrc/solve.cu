@@ -58,25 +58,40 @@ __global__ void shift_diag_kernel(double* __restrict__ T, int64_t n, int64_t ldt
   if (threadIdx.x == 0 && shift_out) *shift_out = shift;
 }
 
-// partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s]; FP32 products with y split
-// into hi + lo parts, FP64 across chunks
+// partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s] in FP64 (the reference forms
+// x = A^T y in float64, solver.py:58-61, 144-146); four columns per thread, 16-byte loads
 __global__ void project_partial_kernel(const float* __restrict__ A, int64_t nrow, int64_t ncol, int64_t lda,
-                                       const double* __restrict__ y, double* __restrict__ part) {
-  const int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+                                       const double* __restrict__ y, double* __restrict__ part, bool vec4) {
+  const int64_t c0 = 4 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
   const int64_t r0 = (int64_t)blockIdx.y * kProjRows;
   const int64_t r1 = min(nrow, r0 + kProjRows);
-  if (col >= ncol) return;
-  float hi = 0.0f, lo = 0.0f;
-#pragma unroll 8
-  for (int64_t s = r0; s < r1; ++s) {
-    const double ys = y[s];
-    const float yh = (float)ys;
-    const float yl = (float)(ys - (double)yh);
-    const float a = __ldg(A + s * lda + col);
-    hi = fmaf(a, yh, hi);
-    lo = fmaf(a, yl, lo);
+  if (c0 >= ncol) return;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  if (vec4 && c0 + 3 < ncol) {
+#pragma unroll 4
+    for (int64_t s = r0; s < r1; ++s) {
+      const double ys = y[s];
+      const float4 v = __ldg(reinterpret_cast<const float4*>(A + s * lda + c0));
+      a0 = fma((double)v.x, ys, a0);
+      a1 = fma((double)v.y, ys, a1);
+      a2 = fma((double)v.z, ys, a2);
+      a3 = fma((double)v.w, ys, a3);
+    }
+  } else {
+    for (int64_t s = r0; s < r1; ++s) {
+      const double ys = y[s];
+      const float* row = A + s * lda;
+      a0 = fma((double)__ldg(row + c0), ys, a0);
+      if (c0 + 1 < ncol) a1 = fma((double)__ldg(row + c0 + 1), ys, a1);
+      if (c0 + 2 < ncol) a2 = fma((double)__ldg(row + c0 + 2), ys, a2);
+      if (c0 + 3 < ncol) a3 = fma((double)__ldg(row + c0 + 3), ys, a3);
+    }
   }
-  part[blockIdx.y * ncol + col] = (double)hi + (double)lo;
+  double* p = part + blockIdx.y * ncol + c0;
+  p[0] = a0;
+  if (c0 + 1 < ncol) p[1] = a1;
+  if (c0 + 2 < ncol) p[2] = a2;
+  if (c0 + 3 < ncol) p[3] = a3;
 }
 
 __global__ void sum_partials_kernel(const double* __restrict__ part, int64_t nchunk, int64_t ncol,
@@ -159,6 +174,48 @@ __global__ void uv_partial_kernel(const double* __restrict__ U, int64_t n, const
   part[blockIdx.y * n + t] = acc;
 }
 
+constexpr int kRefineIters = 10;
+constexpr double kRefineTol = 1e-12;
+
+__global__ void to_f32_kernel(const double* __restrict__ in, int64_t count, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// r = b - T y (FP64, T symmetric row-major n x n), warp per row; ||r||^2 and ||b||^2 into acc[0..1]
+__global__ void residual_kernel(const double* __restrict__ T, int64_t n, const double* __restrict__ y,
+                                const double* __restrict__ b, double* __restrict__ r, float* __restrict__ r32,
+                                double* __restrict__ acc) {
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double* t = T + row * n;
+  double s = 0.0;
+  for (int64_t j = lane; j < n; j += 32) s = fma(t[j], y[j], s);
+  s = warp_sum(s);
+  if (lane == 0) {
+    const double v = b[row] - s;
+    r[row] = v;
+    r32[row] = (float)v;
+    atomicAdd(&acc[0], v * v);
+    atomicAdd(&acc[1], b[row] * b[row]);
+  }
+}
+
+__global__ void accumulate_kernel(double* __restrict__ y, const float* __restrict__ d, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += (double)d[i];
+}
+
+// info = the factorisation's info if it failed, else -1 when the final relative residual
+// exceeds the tolerance, else 0
+__global__ void refine_check_kernel(const double* __restrict__ acc, const int* __restrict__ fact_info,
+                                    int* __restrict__ info, double tol) {
+  int v = *fact_info;
+  if (v == 0 && acc[1] > 0.0 && !(acc[0] <= tol * tol * acc[1])) v = -1;
+  *info = v;
+}
+
 struct SolveWs {
   void* cus;
   size_t cus_bytes;
@@ -170,6 +227,10 @@ struct SolveWs {
   double* part;   // nchunk * max(n, np)
   double* shift;  // 1
   int* info;      // 1
+  float* t32;     // n * n (SHIFT_MIXED)
+  float* r32;     // n
+  double* r;      // n
+  double* acc;    // 2 per refinement round
 };
 
 int query_cusolver_bytes(int64_t n, int method, size_t* dev_bytes, size_t* host_bytes) {
@@ -180,6 +241,9 @@ int query_cusolver_bytes(int64_t n, int method, size_t* dev_bytes, size_t* host_
   cusolverStatus_t s;
   if (method == QGX_SOLVE_SHIFT) {
     s = cusolverDnXpotrf_bufferSize(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, nullptr, n, CUDA_R_64F, dev_bytes,
+                                    host_bytes);
+  } else if (method == QGX_SOLVE_SHIFT_MIXED) {
+    s = cusolverDnXpotrf_bufferSize(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, nullptr, n, CUDA_R_32F, dev_bytes,
                                     host_bytes);
   } else {
     s = cusolverDnXsyevd_bufferSize(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, nullptr, n,
@@ -209,6 +273,11 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   const int64_t o_part = take(nchunk * wide * 8);
   const int64_t o_shift = take(8);
   const int64_t o_info = take(8);
+  const bool mixed = method == QGX_SOLVE_SHIFT_MIXED;
+  const int64_t o_t32 = take(mixed ? n * n * 4 : 0);
+  const int64_t o_r32 = take(mixed ? n * 4 : 0);
+  const int64_t o_r = take(mixed ? n * 8 : 0);
+  const int64_t o_acc = take(mixed ? 2 * 8 * kRefineIters : 0);
   *need = off;
   if (!base) return QGX_OK;
   if (bytes < off) return QGX_ERR_ARG;
@@ -223,6 +292,10 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   ws->part = reinterpret_cast<double*>(b + o_part);
   ws->shift = reinterpret_cast<double*>(b + o_shift);
   ws->info = reinterpret_cast<int*>(b + o_info);
+  ws->t32 = reinterpret_cast<float*>(b + o_t32);
+  ws->r32 = reinterpret_cast<float*>(b + o_r32);
+  ws->r = reinterpret_cast<double*>(b + o_r);
+  ws->acc = reinterpret_cast<double*>(b + o_acc);
   if (hb > g_host_ws.size()) g_host_ws.resize(hb);
   return QGX_OK;
 }
@@ -232,8 +305,9 @@ int project(const float* A, int64_t nrow, int64_t ncol, int64_t lda, const doubl
             cudaStream_t st) {
   const int64_t nchunk = (nrow + kProjRows - 1) / kProjRows;
   if (nchunk > 65535) return QGX_ERR_UNSUPPORTED;
-  project_partial_kernel<<<dim3((unsigned)((ncol + 255) / 256), (unsigned)nchunk), 256, 0, st>>>(A, nrow, ncol, lda, y,
-                                                                                                  part);
+  const bool vec4 = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && (lda % 4 == 0);
+  project_partial_kernel<<<dim3((unsigned)((ncol + 1023) / 1024), (unsigned)nchunk), 256, 0, st>>>(
+      A, nrow, ncol, lda, y, part, vec4);
   sum_partials_kernel<<<(unsigned)((ncol + 255) / 256), 256, 0, st>>>(part, nchunk, ncol, x);
   return launch_status();
 }
@@ -260,6 +334,34 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
       return QGX_ERR_SOLVER;
     return QGX_OK;
   }
+  if (method == QGX_SOLVE_SHIFT_MIXED) {
+    shift_diag_kernel<<<1, 1024, 0, st>>>(T, n, n, rshift, ashift, ws.shift);
+    const unsigned g = (unsigned)std::min<int64_t>((n * n + 255) / 256, 8192);
+    to_f32_kernel<<<g, 256, 0, st>>>(T, n * n, ws.t32);
+    if ((rc = launch_status()) != QGX_OK) return rc;
+    if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.cus, ws.cus_bytes, hws,
+                         g_host_ws.size(), ws.info) != CUSOLVER_STATUS_SUCCESS)
+      return QGX_ERR_SOLVER;
+    // y = 0, r = b: the first round solves with the FP32 factor from the FP64 right-hand side
+    QGX_CHECK_CUDA(cudaMemsetAsync(ws.y, 0, n * sizeof(double), st));
+    QGX_CHECK_CUDA(cudaMemsetAsync(ws.acc, 0, 2 * kRefineIters * sizeof(double), st));
+    const unsigned gr = (unsigned)((n * 32 + 255) / 256);
+    const unsigned gv = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
+    for (int it = 0; it < kRefineIters; ++it) {
+      residual_kernel<<<gr, 256, 0, st>>>(T, n, ws.y, b, ws.r, ws.r32, ws.acc + 2 * it);
+      if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.r32, n,
+                           ws.info + 1) !=
+          CUSOLVER_STATUS_SUCCESS)
+        return QGX_ERR_SOLVER;
+      accumulate_kernel<<<gv, 256, 0, st>>>(ws.y, ws.r32, n);
+    }
+    // final residual of the refined solution
+    double* last = ws.acc + 2 * (kRefineIters - 1);
+    QGX_CHECK_CUDA(cudaMemsetAsync(last, 0, 2 * sizeof(double), st));
+    residual_kernel<<<gr, 256, 0, st>>>(T, n, ws.y, b, ws.r, ws.r32, last);
+    refine_check_kernel<<<1, 1, 0, st>>>(last, ws.info, dinfo, kRefineTol);
+    return launch_status();
+  }
   if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.w,
                        CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
     return QGX_ERR_SOLVER;
@@ -279,7 +381,7 @@ using namespace qgx;
 extern "C" {
 
 int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* bytes) {
-  QGX_CHECK_ARG(n > 0 && np > 0 && bytes && (method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV));
+  QGX_CHECK_ARG(n > 0 && np > 0 && bytes && method >= QGX_SOLVE_SHIFT && method <= QGX_SOLVE_SHIFT_MIXED);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   SolveWs ws;
   return workspace_layout(n, np, method, nullptr, 0, &ws, bytes);
@@ -289,7 +391,7 @@ int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t ld
                     double rshift, double ashift, double rtol, double atol, double tol_snr, double* x, int32_t* info,
                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
   QGX_CHECK_ARG(n > 0 && np > 0 && lda >= np && T && A && b && x && workspace);
-  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV || method == QGX_SOLVE_SHIFT_MIXED);
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   SolveWs ws;

@@ -4,6 +4,10 @@
     python -m quantax_gb300.kernel_bench sweep --ns 8192 --n 64 --m 256 --steps 64
     python -m quantax_gb300.kernel_bench eloc --ns 8192 --n 64 --m 256
     python -m quantax_gb300.kernel_bench obar --ns 8192 --n 64 --m 256
+    python -m quantax_gb300.kernel_bench rc_forward --ns 16384 --L 10 --blocks 8 --channels 16
+    python -m quantax_gb300.kernel_bench rc_sweep --ns 16384 --steps 4
+    python -m quantax_gb300.kernel_bench rc_eloc --ns 16384
+    python -m quantax_gb300.kernel_bench rc_jacobian --ns 2048
 
 Prints one JSON line with the mean device time per launch (CUDA events, after warm-up).
 """
@@ -42,9 +46,64 @@ def _rbm(n, m, ns, seed=0):
     return table, spins
 
 
+def _resconv(a, st):
+    import ctypes as C
+    import quantax_gb300 as qtx
+    Ls, B, Cc, ns = a.L, a.blocks, a.channels, a.ns
+    n = Ls * Ls
+    npar = int(L.lib().qgx_resconv_nparams(B, Cc))
+    rng = np.random.default_rng(0)
+    params = torch.as_tensor(rng.normal(0, 0.1, npar).astype(np.float32)).cuda()
+    table = torch.empty(L.lib().qgx_resconv_table_floats(B, Cc), dtype=torch.float32, device="cuda")
+    L.call("qgx_resconv_prepare", L.ptr(params), B, Cc, L.ptr(table), st)
+    spins = torch.empty((ns, (n + 31) // 32), dtype=torch.int32, device="cuda")
+    L.call("qgx_spins_init_fixed_up", L.ptr(spins), ns, n, n // 2, 5, st)
+    flop_fwd = 2.0 * n * 9 * Cc * (1 + (2 * B - 1) * Cc)  # 2 x MACs per forward
+    res = dict(ns=ns, L=Ls, blocks=B, channels=Cc, flop_per_forward=flop_fwd)
+    if a.kernel == "rc_forward":
+        lp = torch.empty((ns, 2), dtype=torch.float32, device="cuda")
+        fn = lambda: L.call("qgx_resconv_log_psi", L.ptr(table), Ls, B, Cc, 1, L.ptr(spins), ns, L.ptr(lp), st)
+        ms = _events(fn, a.reps)
+        res.update(ms=ms, forwards_per_s=ns / ms * 1e3, tflops=flop_fwd * ns / ms / 1e9)
+    elif a.kernel == "rc_sweep":
+        qtx.sites.Square(Ls, Nparticles=(n // 2, n // 2))
+        nbr = torch.as_tensor(qtx.get_sites().neighbor_table(1)).cuda()
+        lp = torch.empty((ns, 2), dtype=torch.float32, device="cuda")
+        ws = torch.empty(L.lib().qgx_resconv_sweep_workspace_bytes(Ls, ns), dtype=torch.uint8, device="cuda")
+        fn = lambda: L.call("qgx_resconv_sweep", L.ptr(table), Ls, B, Cc, 1, L.ptr(spins), L.ptr(lp), None, ns,
+                            a.steps, 7, 0, 2.0, L.ptr(nbr), nbr.shape[1], 1, L.ptr(ws), ws.numel(), st)
+        ms = _events(fn, a.reps)
+        res.update(steps=a.steps, ms=ms, proposals_per_s=ns * a.steps / ms * 1e3,
+                   tflops=flop_fwd * ns * (a.steps + 1) / ms / 1e9)
+    elif a.kernel == "rc_eloc":
+        qtx.sites.Square(Ls, Nparticles=(n // 2, n // 2))
+        op = qtx.operator.Heisenberg(J=[1.0, 0.5], n_neighbor=[1, 2], msr=True).compiled()
+        max_conn = len(op.host["f1"]) + len(op.host["f2"])
+        ws = torch.empty(L.lib().qgx_resconv_eloc_workspace_bytes(Ls, ns, max_conn), dtype=torch.uint8,
+                         device="cuda")
+        er = torch.empty(ns, dtype=torch.float64, device="cuda")
+        ei = torch.empty(ns, dtype=torch.float64, device="cuda")
+        fn = lambda: L.call("qgx_resconv_eloc", L.ptr(table), Ls, B, Cc, 1, C.byref(op.struct), L.ptr(spins), ns,
+                            L.ptr(er), L.ptr(ei), L.ptr(ws), ws.numel(), st)
+        ms = _events(fn, a.reps)
+        res.update(ms=ms, samples_per_s=ns / ms * 1e3)
+    else:
+        O = torch.empty((2 * ns, npar), dtype=torch.float32, device="cuda")
+        ws = torch.empty(L.lib().qgx_resconv_jacobian_workspace_bytes(Ls, B, Cc), dtype=torch.uint8, device="cuda")
+        fn = lambda: L.call("qgx_resconv_jacobian", L.ptr(table), Ls, B, Cc, 1, L.ptr(spins), ns, L.ptr(O[:ns]),
+                            L.ptr(O[ns:]), npar, L.ptr(ws), ws.numel(), st)
+        ms = _events(fn, a.reps)
+        res.update(ms=ms, samples_per_s=ns / ms * 1e3, o_write_gbs=2 * ns * npar * 4 / ms / 1e6)
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["gram", "sweep", "eloc", "obar"])
+    ap.add_argument("kernel", choices=["gram", "sweep", "eloc", "obar", "rc_forward", "rc_sweep", "rc_eloc",
+                                       "rc_jacobian"])
+    ap.add_argument("--L", type=int, default=10)
+    ap.add_argument("--blocks", type=int, default=8)
+    ap.add_argument("--channels", type=int, default=16)
     ap.add_argument("--mode", default="tf32", choices=["fp32", "tf32", "bf16", "3xtf32"])
     ap.add_argument("--rows", type=int, default=2048)
     ap.add_argument("--k", type=int, default=16640)
@@ -71,6 +130,8 @@ def main():
         syrk = float(a.rows) * (a.rows + 1) * a.k
         out.update(mode=a.mode, rows=a.rows, k=a.k, ms=ms, syrk_tflops=syrk / ms / 1e9,
                    gemm_equiv_tflops=2.0 * a.rows * a.rows * a.k / ms / 1e9)
+    elif a.kernel.startswith("rc_"):
+        out.update(_resconv(a, st))
     else:
         table, spins = _rbm(a.n, a.m, a.ns)
         if a.kernel == "sweep":

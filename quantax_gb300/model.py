@@ -3,6 +3,9 @@
 RBM_Dense mirrors quantax/model/shallow_nets.py:35-126: psi(s) = prod_i cosh(W s + b)_i,
 optionally times exp(a.s) (a visible bias, absent in the reference). Parameters are
 flattened in the reference's ravel order: W (M x N, row-major), b (M), then a (N).
+
+ResConv mirrors quantax/model/conv_nets.py:95-183 (residual CNN, 3x3 circular
+convolutions, tanh-GELU, mean-exp pooling, optional complex output via pair_cpl).
 """
 from __future__ import annotations
 
@@ -125,3 +128,83 @@ class RBM_Dense:
         _lib.call("qgx_rbm_obar", _lib.ptr(table), self.N, self.M, int(self.visible_bias), _lib.ptr(packed),
                   _lib.ptr(r), packed.shape[0], _lib.ptr(out), out.stride(0), _lib.ptr(omean), _lib.ptr(workspace),
                   workspace.numel(), _lib.stream_ptr())
+
+
+class ResConv:
+    """Deep convolutional residual network (conv_nets.py:95-183) on a periodic L x L lattice."""
+
+    kind = "resconv"
+    holomorphic = False
+
+    def __init__(self, nblocks: int, channels: int, kernel_size: int = 3, final_activation=None, trans_symm=None,
+                 dtype=np.float32, out_dtype=None, seed: Optional[int] = None):
+        from .global_defs import get_lattice
+        if kernel_size != 3 or final_activation is not None or trans_symm is not None:
+            raise NotImplementedError("quantax_gb300 ResConv: 3x3 kernels, exp_by_scale output and the default "
+                                      "translation symmetrisation only")
+        if np.dtype(dtype) != np.float32:
+            raise NotImplementedError("ResConv runs with float32 parameters")
+        lat = get_lattice()
+        if lat.ndim != 2 or lat.shape[1] != lat.shape[2] or not np.all(lat.boundary == 1):
+            raise NotImplementedError("ResConv needs a periodic square lattice")
+        self.L = lat.shape[1]
+        self.N = lat.Nsites
+        self.nblocks = int(nblocks)
+        self.channels = int(channels)
+        self.complex_output = out_dtype is not None and np.issubdtype(np.dtype(out_dtype), np.complexfloating)
+        rng = np.random.default_rng(get_subkeys() if seed is None else seed)
+        parts = []
+        for b in range(self.nblocks):
+            for layer in range(2):
+                cin = 1 if (b == 0 and layer == 0) else self.channels
+                w = _truncated_normal(rng, (self.channels, cin, 3, 3), np.sqrt(2.0 / (cin * 9)))  # He normal
+                parts.append(w.ravel())
+                if not (layer == 1 and b == self.nblocks - 1):
+                    parts.append(np.zeros(self.channels))
+        self.init_params = np.concatenate(parts).astype(np.float32)
+
+    @property
+    def nparams(self) -> int:
+        return int(self.init_params.size)
+
+    def table_floats(self) -> int:
+        return int(_lib.lib().qgx_resconv_table_floats(self.nblocks, self.channels))
+
+    def prepare(self, params, table):
+        _lib.call("qgx_resconv_prepare", _lib.ptr(params), self.nblocks, self.channels, _lib.ptr(table),
+                  _lib.stream_ptr())
+
+    def _args(self):
+        return (self.L, self.nblocks, self.channels, int(self.complex_output))
+
+    def log_psi(self, table, packed, out):
+        """out: (ns, 2) float32 (re, im)."""
+        _lib.call("qgx_resconv_log_psi", _lib.ptr(table), *self._args(), _lib.ptr(packed), packed.shape[0],
+                  _lib.ptr(out), _lib.stream_ptr())
+
+    def sweep_workspace_bytes(self, ns):
+        return int(_lib.lib().qgx_resconv_sweep_workspace_bytes(self.L, ns))
+
+    def sweep(self, table, packed, log_psi, accepts, nsteps, seed, step0, reweight, proposal, nbr, z, hop,
+              workspace):
+        if proposal != _lib.PROPOSAL_SPIN_EXCHANGE:
+            raise NotImplementedError("the ResConv sampler implements SpinExchange proposals")
+        _lib.call("qgx_resconv_sweep", _lib.ptr(table), *self._args(), _lib.ptr(packed), _lib.ptr(log_psi),
+                  _lib.ptr(accepts), packed.shape[0], int(nsteps), int(seed), int(step0), float(reweight),
+                  _lib.ptr(nbr), int(z), int(hop), _lib.ptr(workspace), workspace.numel(), _lib.stream_ptr())
+
+    def eloc_workspace_bytes(self, ns, max_conn):
+        return int(_lib.lib().qgx_resconv_eloc_workspace_bytes(self.L, ns, max_conn))
+
+    def eloc(self, table, compiled_op, packed, out_re, out_im, workspace):
+        _lib.call("qgx_resconv_eloc", _lib.ptr(table), *self._args(), C.byref(compiled_op.struct),
+                  _lib.ptr(packed), packed.shape[0], _lib.ptr(out_re), _lib.ptr(out_im), _lib.ptr(workspace),
+                  workspace.numel(), _lib.stream_ptr())
+
+    def jacobian_workspace_bytes(self):
+        return int(_lib.lib().qgx_resconv_jacobian_workspace_bytes(self.L, self.nblocks, self.channels))
+
+    def jacobian(self, table, packed, o_re, o_im, ldo, workspace):
+        _lib.call("qgx_resconv_jacobian", _lib.ptr(table), *self._args(), _lib.ptr(packed), packed.shape[0],
+                  _lib.ptr(o_re), _lib.ptr(o_im), int(ldo), _lib.ptr(workspace), workspace.numel(),
+                  _lib.stream_ptr())

@@ -77,6 +77,12 @@ class CompiledOperator:
                                     p(self.f2_ij), p(self.f2_J))
 
     @property
+    def max_site(self) -> int:
+        h = self.host
+        sites = list(h["z"]) + [i for ij in h["zz"] for i in ij] + list(h["f1"]) + [i for ij in h["f2"] for i in ij]
+        return max(sites) if sites else -1
+
+    @property
     def max_flips(self) -> int:
         return 2 if len(self.host["f2"]) else (1 if len(self.host["f1"]) else 0)
 

@@ -27,6 +27,7 @@ class Solver:
     rtol: Optional[float] = None
     atol: float = 0.0
     tol_snr: float = 0.0
+    precision: str = "fp64"   # "fp64" or "mixed" (FP32 Cholesky + FP64 refinement, shift only)
 
     def use_minnorm(self, ns: int, np_: int) -> bool:
         if self.branch == "auto":
@@ -49,14 +50,15 @@ def lstsq_pinv_eig(rtol: Optional[float] = None, atol: float = 0.0, tol_snr: flo
     return Solver("pinv", "lstsq", rtol=rtol, atol=atol, tol_snr=tol_snr)
 
 
-def auto_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
-    """solver.py:80-91"""
-    return Solver("shift", "auto", rshift=rshift, ashift=ashift)
+def auto_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4, precision: str = "fp64") -> Solver:
+    """solver.py:80-91. precision="mixed" factors in FP32 and refines the solution in FP64
+    (MinSR branch); it falls back to the FP64 factorisation when the refinement stalls."""
+    return Solver("shift", "auto", rshift=rshift, ashift=ashift, precision=precision)
 
 
-def minnorm_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
-    """solver.py:50-62"""
-    return Solver("shift", "minnorm", rshift=rshift, ashift=ashift)
+def minnorm_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4, precision: str = "fp64") -> Solver:
+    """solver.py:50-62 (see auto_shift_eig for precision)"""
+    return Solver("shift", "minnorm", rshift=rshift, ashift=ashift, precision=precision)
 
 
 def lstsq_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
@@ -82,6 +84,7 @@ class QNGD:
         self._Omean = None
         self._buf = {}
         self.marks = None  # optional list: solve() appends ("gram", event) after the Gram build
+        self.last_solve_fallback = False
 
     @property
     def state(self):
@@ -103,14 +106,13 @@ class QNGD:
 
     def get_Obar(self, samples) -> torch.Tensor:
         """Obar = (O - <O>) sqrt(r / Ns) (sr.py:79-88)."""
-        out = self._buffer("obar", (samples.nsamples, self._state.nparams), torch.float32)
+        out = self._buffer("obar", (self._state.obar_rows(samples.nsamples), self._state.nparams), torch.float32)
         obar, self._Omean = self._state.obar(samples, out)
         return obar
 
     def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
         """step = solver(Obar, Ebar) in FP64 (sr.py:90-113)."""
-        if self.vs_type != VS_TYPE.real_or_holomorphic:
-            raise NotImplementedError("complex-output states are solved by the stacked real path")
+        # real_to_complex states arrive stacked: Obar rows [Re; Im], Ebar [Re; Im] (sr.py:99-105)
         A = Obar
         b = Ebar.to(torch.float64).contiguous()
         ns, np_ = A.shape
@@ -126,12 +128,31 @@ class QNGD:
         nbytes = C.c_int64(0)
         if sv.use_minnorm(ns, np_):
             T = self._buffer("gram", (ns, ns), torch.float64)
-            _lib.call("qgx_gram", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(T), ns, self._gram, st)
+            if self._gram == _lib.GRAM_BF16:
+                Ab = self._buffer("obar_bf16", (ns, np_), torch.bfloat16)
+                _lib.call("qgx_f32_to_bf16", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(Ab), np_, st)
+                _lib.call("qgx_gram_tc", _lib.ptr(Ab), 1, ns, np_, np_, _lib.ptr(T), ns, None, st)
+            else:
+                _lib.call("qgx_gram", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(T), ns, self._gram, st)
             self._mark("gram")
+            if sv.kind == "shift" and sv.precision == "mixed":
+                method = _lib.SOLVE_SHIFT_MIXED
             _lib.call("qgx_solve_workspace_bytes", ns, np_, method, C.byref(nbytes))
             ws = self._state.workspace("solve", nbytes.value)
             _lib.call("qgx_minsr_solve", _lib.ptr(T), ns, _lib.ptr(A), np_, A.stride(0), _lib.ptr(b), method, rshift,
                       sv.ashift, rtol, sv.atol, sv.tol_snr, _lib.ptr(x), _lib.ptr(info), _lib.ptr(ws), ws.numel(), st)
+            if method == _lib.SOLVE_SHIFT_MIXED:
+                code = int(info.item())
+                self.last_solve_fallback = code != 0
+                if code > 0:
+                    raise RuntimeError(f"T + shift is not positive definite (cuSOLVER info {code})")
+                if code < 0:
+                    # refinement stalled: factor the (already shifted) FP64 matrix instead
+                    _lib.call("qgx_solve_workspace_bytes", ns, np_, _lib.SOLVE_SHIFT, C.byref(nbytes))
+                    ws = self._state.workspace("solve", nbytes.value)
+                    _lib.call("qgx_minsr_solve", _lib.ptr(T), ns, _lib.ptr(A), np_, A.stride(0), _lib.ptr(b),
+                              _lib.SOLVE_SHIFT, 0.0, 0.0, rtol, sv.atol, sv.tol_snr, _lib.ptr(x), _lib.ptr(info),
+                              _lib.ptr(ws), ws.numel(), st)
         else:
             S = self._buffer("gram", (np_, np_), torch.float64)
             _lib.call("qgx_gram_t", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(S), np_, st)
@@ -185,10 +206,15 @@ class SR(QNGD):
         E = self._hamiltonian.Oloc(self._state, samples)
         ns = samples.nsamples
         stats = self._buffer("stats", (3,), torch.float64)
-        ebar = torch.empty(ns, dtype=torch.float64, device=E.device)
-        _lib.call("qgx_energy_stats", _lib.ptr(E), None, _lib.ptr(samples.reweight_factor), ns, _lib.ptr(stats),
-                  _lib.ptr(ebar), None, _lib.stream_ptr())
+        cplx = E.is_complex()
+        ebar = torch.empty(2 * ns if cplx else ns, dtype=torch.float64, device=E.device)
+        er = E.real.contiguous() if cplx else E
+        ei = E.imag.contiguous() if cplx else None
+        _lib.call("qgx_energy_stats", _lib.ptr(er), _lib.ptr(ei), _lib.ptr(samples.reweight_factor), ns,
+                  _lib.ptr(stats), _lib.ptr(ebar[:ns]), _lib.ptr(ebar[ns:]) if cplx else None, _lib.stream_ptr())
         self._stats = stats
+        if cplx and self.vs_type != VS_TYPE.real_to_complex:
+            raise ValueError("complex local energies need a complex-output state")
         return ebar
 
 

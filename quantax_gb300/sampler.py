@@ -38,7 +38,8 @@ class Samples:
 
     @property
     def psi(self) -> torch.Tensor:
-        return torch.exp(self.log_psi.double())
+        lp = self.log_psi
+        return torch.exp(lp.to(torch.complex128 if lp.is_complex() else torch.float64))
 
     @classmethod
     def from_spins(cls, spins, log_psi=None):
@@ -65,7 +66,9 @@ class Metropolis:
         self._step = 0
         self._initial_spins = initial_spins
         dev = state.params.device
-        self._log_psi = torch.empty(self._nsamples, dtype=torch.float32, device=dev)
+        self._resconv = state.model.kind == "resconv"
+        shape = (self._nsamples, 2) if self._resconv else (self._nsamples,)
+        self._log_psi = torch.empty(shape, dtype=torch.float32, device=dev)
         self._accepts = torch.empty(self._nsamples, dtype=torch.int32, device=dev)
         self._nbr = torch.zeros(1, dtype=torch.int32, device=dev)
         self._z = 1
@@ -110,7 +113,7 @@ class Metropolis:
                 s = np.tile(s, (self._nsamples, 1))
             return pack_spins(s.reshape(self._nsamples, n), n)
         packed = torch.empty((self._nsamples, (n + 31) // 32), dtype=torch.int32, device=dev)
-        nparticles = get_sites().Nparticles
+        nparticles = self._state.sites.Nparticles
         if isinstance(nparticles, tuple):
             _lib.call("qgx_spins_init_fixed_up", _lib.ptr(packed), self._nsamples, n, nparticles[0], get_subkeys(),
                       _lib.stream_ptr())
@@ -128,15 +131,24 @@ class Metropolis:
         """nsweeps proposals per chain (metropolis.py:171-215); default sweep_steps."""
         n = self._sweep_steps if nsweeps is None else int(nsweeps)
         st = self._state
-        st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, n, self._seed, self._step,
-                       self._reweight, self.proposal, self._nbr, self._z, self._hop)
+        if self._resconv:
+            ws = st.workspace("sweep", st.model.sweep_workspace_bytes(self._nsamples))
+            st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, n, self._seed, self._step,
+                           self._reweight, self.proposal, self._nbr, self._z, self._hop, ws)
+            lp_real = self._log_psi[:, 0].contiguous()
+            lp = torch.view_as_complex(self._log_psi.clone()) if st.is_complex else lp_real
+        else:
+            st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, n, self._seed, self._step,
+                           self._reweight, self.proposal, self._nbr, self._z, self._hop)
+            lp_real = self._log_psi
+            lp = self._log_psi.clone()
         self._step += n
         r = None
         if self._reweight != 2.0:
             r = torch.empty(self._nsamples, dtype=torch.float64, device=self._log_psi.device)
-            _lib.call("qgx_reweight_factor", _lib.ptr(self._log_psi), self._nsamples, self._reweight, _lib.ptr(r),
+            _lib.call("qgx_reweight_factor", _lib.ptr(lp_real), self._nsamples, self._reweight, _lib.ptr(r),
                       _lib.stream_ptr())
-        return Samples(self._packed.clone(), self._log_psi.clone(), self.Nmodes, r)
+        return Samples(self._packed.clone(), lp, self.Nmodes, r)
 
 
 class LocalFlip(Metropolis):
@@ -158,7 +170,7 @@ class SpinExchange(Metropolis):
     def __init__(self, state, nsamples: int, reweight: float = 2.0, thermal_steps: Optional[int] = None,
                  sweep_steps: Optional[int] = None, initial_spins=None,
                  n_neighbor: Union[int, Sequence[int]] = 1):
-        sites = get_sites()
+        sites = state.sites
         if isinstance(sites.Nparticles, int):
             raise ValueError("The number spin-up and spin-down particles should be specified in sites for "
                              "`SpinExchange` sampler.")
@@ -166,7 +178,7 @@ class SpinExchange(Metropolis):
         super().__init__(state, nsamples, reweight, thermal_steps, sweep_steps, initial_spins)
 
     def _setup(self) -> None:
-        sites = get_sites()
+        sites = self._state.sites
         table = sites.neighbor_table(self._n_neighbor)
         self._nbr = torch.as_tensor(table, dtype=torch.int32, device=self._log_psi.device).contiguous()
         self._z = table.shape[1]

@@ -51,6 +51,7 @@ class Variational:
             raise NotImplementedError("symmetry projection is not implemented in quantax_gb300")
         self._model = model
         self._dev = device()
+        self._sites = get_sites()  # the lattice this state was built on (kept, not re-read)
         params = model.init_params
         if param_file is not None:
             params = np.load(param_file).astype(np.float32).reshape(-1)
@@ -62,6 +63,8 @@ class Variational:
         self._flag_host = torch.zeros(1, dtype=torch.int32).pin_memory()
         self._flag_event = None
         self._use_ref = use_ref
+        if getattr(model, "complex_output", False) and not is_default_cpl():
+            raise ValueError("a complex-output model needs set_default_dtype(np.complex128) (VS_TYPE real_to_complex)")
         is_cpl = is_default_cpl() and getattr(model, "complex_output", False)
         self._vs_type = VS_TYPE.real_to_complex if is_cpl else VS_TYPE.real_or_holomorphic
         self._ws = {}
@@ -77,12 +80,16 @@ class Variational:
         return self._model.nparams
 
     @property
+    def sites(self):
+        return self._sites
+
+    @property
     def Nsites(self) -> int:
-        return get_sites().Nsites
+        return self._sites.Nsites
 
     @property
     def Nmodes(self) -> int:
-        return get_sites().Nmodes
+        return self._sites.Nmodes
 
     @property
     def vs_type(self) -> VS_TYPE:
@@ -113,42 +120,90 @@ class Variational:
         return buf
 
     # ---- forward ------------------------------------------------------------------------
+    @property
+    def is_complex(self) -> bool:
+        return bool(getattr(self._model, "complex_output", False))
+
     def log_psi_packed(self, packed: torch.Tensor) -> torch.Tensor:
-        out = torch.empty(packed.shape[0], dtype=torch.float32, device=self._dev)
+        """log psi of packed configurations: float32, or complex64 for complex-output models."""
+        if self._model.kind == "rbm":
+            out = torch.empty(packed.shape[0], dtype=torch.float32, device=self._dev)
+            self._model.log_psi(self._table, packed, out)
+            return out
+        out = torch.empty((packed.shape[0], 2), dtype=torch.float32, device=self._dev)
         self._model.log_psi(self._table, packed, out)
-        return out
+        return torch.view_as_complex(out) if self.is_complex else out[:, 0].contiguous()
 
     def log_psi(self, s) -> torch.Tensor:
         return self.log_psi_packed(pack_spins(s, self.Nmodes))
 
     def __call__(self, s) -> torch.Tensor:
-        """psi(s) as float64 (variational.py:325-347); use log_psi for large systems."""
-        return torch.exp(self.log_psi(s).double())
+        """psi(s) as float64 / complex128 (variational.py:325-347); use log_psi for large systems."""
+        lp = self.log_psi(s)
+        return torch.exp(lp.to(torch.complex128 if lp.is_complex() else torch.float64))
 
     def init_internal(self, s):
         return None
 
     # ---- local energies and log-derivatives ---------------------------------------------
     def local_energy(self, op, samples) -> torch.Tensor:
-        out = torch.empty(samples.nsamples, dtype=torch.float64, device=self._dev)
-        self._model.eloc(self._table, op.compiled(), samples.packed, out)
-        return out
+        """E_loc per sample: float64, or complex128 for complex-output models."""
+        comp = op.compiled()
+        if comp.max_site >= self.Nmodes:
+            raise ValueError("the operator acts on sites beyond the state's lattice")
+        ns = samples.nsamples
+        out = torch.empty(ns, dtype=torch.float64, device=self._dev)
+        if self._model.kind == "rbm":
+            self._model.eloc(self._table, comp, samples.packed, out)
+            return out
+        out_im = torch.empty(ns, dtype=torch.float64, device=self._dev) if self.is_complex else None
+        max_conn = len(comp.host["f1"]) + len(comp.host["f2"])
+        ws = self.workspace("eloc", self._model.eloc_workspace_bytes(ns, max_conn))
+        self._model.eloc(self._table, comp, samples.packed, out, out_im, ws)
+        return torch.complex(out, out_im) if out_im is not None else out
 
     def jacobian(self, s) -> torch.Tensor:
-        """O_sk = d log psi(s) / d theta_k, (ns, nparams) float32 (variational.py:497-511)."""
+        """O_sk = d log psi(s) / d theta_k, (ns, nparams) float32 or complex64
+        (variational.py:497-511)."""
         packed = s if isinstance(s, torch.Tensor) and s.dtype == torch.int32 else pack_spins(s, self.Nmodes)
-        out = torch.empty((packed.shape[0], self.nparams), dtype=torch.float32, device=self._dev)
-        self._model.jacobian(self._table, packed, out)
-        return out
+        ns = packed.shape[0]
+        if self._model.kind == "rbm":
+            out = torch.empty((ns, self.nparams), dtype=torch.float32, device=self._dev)
+            self._model.jacobian(self._table, packed, out)
+            return out
+        rows = 2 * ns if self.is_complex else ns
+        out = torch.empty((rows, self.nparams), dtype=torch.float32, device=self._dev)
+        ws = self.workspace("jac", self._model.jacobian_workspace_bytes())
+        self._model.jacobian(self._table, packed, out[:ns], out[ns:] if self.is_complex else None, self.nparams, ws)
+        return torch.complex(out[:ns], out[ns:]) if self.is_complex else out
+
+    def obar_rows(self, ns: int) -> int:
+        """Rows of the matrix QNGD.solve works on: 2 ns ([Re; Im]) for complex output."""
+        return 2 * ns if self.is_complex else ns
 
     def obar(self, samples, out: Optional[torch.Tensor] = None):
-        """Centred and scaled Obar and the weighted mean Omean (sr.py:76-88)."""
+        """Centred and scaled Obar and the weighted mean Omean (sr.py:76-88); for complex
+        output the rows are [Re Obar; Im Obar] as QNGD.solve stacks them (sr.py:99-105)."""
         ns = samples.nsamples
         if out is None:
-            out = torch.empty((ns, self.nparams), dtype=torch.float32, device=self._dev)
-        omean = torch.empty(self.nparams, dtype=torch.float64, device=self._dev)
-        ws = self.workspace("obar", self._model.obar_workspace_bytes(ns))
-        self._model.obar(self._table, samples.packed, samples.reweight_factor, out, omean, ws)
+            out = torch.empty((self.obar_rows(ns), self.nparams), dtype=torch.float32, device=self._dev)
+        if self._model.kind == "rbm":
+            omean = torch.empty(self.nparams, dtype=torch.float64, device=self._dev)
+            ws = self.workspace("obar", self._model.obar_workspace_bytes(ns))
+            self._model.obar(self._table, samples.packed, samples.reweight_factor, out, omean, ws)
+            return out, omean
+        ws = self.workspace("jac", self._model.jacobian_workspace_bytes())
+        cplx = self.is_complex
+        self._model.jacobian(self._table, samples.packed, out[:ns], out[ns:] if cplx else None, self.nparams, ws)
+        cws = self.workspace("center", _lib.lib().qgx_center_columns_workspace_bytes(ns, self.nparams))
+        halves = [out[:ns], out[ns:]] if cplx else [out]
+        means = []
+        for h in halves:
+            m = torch.empty(self.nparams, dtype=torch.float64, device=self._dev)
+            _lib.call("qgx_center_columns", _lib.ptr(h), ns, self.nparams, self.nparams,
+                      _lib.ptr(samples.reweight_factor), _lib.ptr(m), _lib.ptr(cws), cws.numel(), _lib.stream_ptr())
+            means.append(m)
+        omean = torch.complex(means[0], means[1]) if cplx else means[0]
         return out, omean
 
     # ---- parameter update ------------------------------------------------------------------

@@ -107,3 +107,17 @@ def test_solver_descriptors():
     assert s.kind == "shift" and s.use_minnorm(10, 20) and not s.use_minnorm(20, 10)
     assert opt.minnorm_pinv_eig().use_minnorm(30, 20)
     assert not opt.lstsq_pinv_eig().use_minnorm(10, 20)
+
+
+def test_serving_job_stream_and_estimates():
+    from quantax_gb300.serving import JobSpec, poisson_jobs
+    jobs = poisson_jobs(20, seed=3)
+    assert len(jobs) == 20 and all(a.arrival < b.arrival for a, b in zip(jobs, jobs[1:]))
+    assert {j.kind for j in jobs} == {"tfim", "j1j2"}
+    # the parameter count formula matches the ResConv oracle's
+    from oracle import resconv
+    j = JobSpec("x", "j1j2", 6, 1024, 1, 0, blocks=5, channels=12)
+    assert j.nparams() == resconv.nparams(5, 12)
+    t = JobSpec("y", "tfim", 64, 8192, 1, 0, alpha=4)
+    assert t.nparams() == 256 * 64 + 256
+    assert t.hbm_bytes() > 8192 * 16640 * 4 + 8192 * 8192 * 8

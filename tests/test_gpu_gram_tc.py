@@ -23,11 +23,17 @@ def tc_gram(A, dtype):
     return T.cpu().numpy()
 
 
-# bound |T - A A^T| <= c ||a_r|| ||a_c||: TF32 keeps 10 mantissa bits, bf16 keeps 7
-TOL = {0: 2.5e-3, 1: 1.0e-2}
+# bound |T - A A^T| <= c ||a_r|| ||a_c||: TF32 keeps 10 mantissa bits, bf16 keeps 7; the
+# hi/lo split of FP32 into two TF32 parts keeps ~21 bits per product, and the tensor core's
+# FP32 accumulation adds up to ~k 2^-25 on sums of same-sign terms (the diagonal)
+TOL = {0: 2.5e-3, 1: 1.0e-2, 2: None}
 
 
-@pytest.mark.parametrize("dtype", [0, 1])
+def tol(dtype, k):
+    return TOL[dtype] if TOL[dtype] is not None else 3e-6 + 3e-8 * k
+
+
+@pytest.mark.parametrize("dtype", [0, 1, 2])
 @pytest.mark.parametrize("shape", [(128, 64), (300, 1000), (129, 40), (1024, 4160)])
 def test_tc_gram(cuda, dtype, shape):
     A = np.random.default_rng(shape[0] + shape[1]).normal(size=shape).astype(np.float32)
@@ -37,9 +43,9 @@ def test_tc_gram(cuda, dtype, shape):
     d = np.sqrt(np.diag(ref))
     assert np.isfinite(T).all()
     err = np.abs(T - ref) / np.outer(d, d)
-    assert err.max() < TOL[dtype], err.max()
+    assert err.max() < tol(dtype, shape[1]), err.max()
     # the mirror of every off-diagonal tile is the same accumulator element
-    np.testing.assert_allclose(T, T.T, rtol=0, atol=TOL[dtype] * np.outer(d, d).max())
+    np.testing.assert_allclose(T, T.T, rtol=0, atol=tol(dtype, shape[1]) * np.outer(d, d).max())
 
 
 def test_tc_gram_through_qgx_gram_mode(cuda):

@@ -70,7 +70,19 @@ def test_minsr_shift_solve(cuda, n, np_):
     b = rng.normal(size=n)
     x = solve_minsr(A, b, 0, ashift=1e-4)
     ref = osr.minnorm_shift(A.astype(np.float64), b, ashift=1e-4)
-    np.testing.assert_allclose(x, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+    np.testing.assert_allclose(x, ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("n,np_", [(64, 144), (500, 2000)])
+def test_minsr_shift_mixed_solve(cuda, n, np_):
+    """FP32 Cholesky + FP64 refinement reaches the FP64 solution (stated: 1e-9 relative;
+    the projection x = A^T y accumulates in FP64 like the reference)."""
+    rng = np.random.default_rng(n + 1)
+    A = rng.normal(size=(n, np_)).astype(np.float32) / np.sqrt(np_)
+    b = rng.normal(size=n)
+    x = solve_minsr(A, b, 2, ashift=1e-4)
+    ref = osr.minnorm_shift(A.astype(np.float64), b, ashift=1e-4)
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-9
 
 
 @pytest.mark.parametrize("tol_snr", [0.0, 0.5])

@@ -284,6 +284,33 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None):
     return out
 
 
+def run_serving(args, rank):
+    """A seeded Poisson stream of VMC jobs (TFIM chains with RBM_Dense, J1-J2 squares with
+    ResConv, sample counts 1024-8192), served with continuous batching on one GPU."""
+    from quantax_gb300.serving import VMCServer, poisson_jobs
+    specs = poisson_jobs(args.jobs, seed=2024 + rank, steps=args.job_steps)
+    srv = VMCServer(max_active=8)
+    for sp in specs:
+        srv.submit(sp)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    out = srv.run()
+    clk = clocks.stop()
+    steps = out["steps"]
+    if rank == 0:
+        line = {"metric": METRIC, "value": steps / out["wall_s"], "unit": UNIT, "n_gpus": 1, "steps": steps,
+                "warmup": 0, "ms_per_step": 1000.0 * out["wall_s"] / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 solve)", "data": "synthetic",
+                "config": {"workload": f"serving: {args.jobs} Poisson jobs x {args.job_steps} SR steps "
+                                       "(config-5 mixture)", "max_active": 8},
+                "jobs_per_s": out["jobs_per_s"], "samples_per_s": out["samples_per_s"],
+                "p50_step_ms": out["p50_step_ms"], "p99_step_ms": out["p99_step_ms"], "wall_s": out["wall_s"],
+                "jobs": [{"name": j["name"], "final_energy": j["energies"][-1],
+                          "mean_step_ms": sum(j["latencies_ms"]) / len(j["latencies_ms"])} for j in out["jobs"]],
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def percentile(lat, q):
     s = sorted(lat)
     return s[min(len(s) - 1, int(round(q * (len(s) - 1))))]
@@ -299,8 +326,11 @@ def main():
     ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
-    ap.add_argument("--workload", default="rbm", choices=["rbm", "resconv"],
-                    help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv)")
+    ap.add_argument("--workload", default="rbm", choices=["rbm", "resconv", "serving"],
+                    help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv); "
+                         "serving: a Poisson stream of config-5 jobs through quantax_gb300.serving")
+    ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
+    ap.add_argument("--job-steps", type=int, default=5, help="serving: SR steps per job")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -318,6 +348,10 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from quantax_gb300 import _build
     _build.build()
+
+    if args.workload == "serving":
+        run_serving(args, rank)
+        return
 
     plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)
     forms = {}

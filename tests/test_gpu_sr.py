@@ -66,7 +66,7 @@ def solve_minsr(A, b, method, **kw):
 @pytest.mark.parametrize("n,np_", [(64, 144), (200, 1000)])
 def test_minsr_shift_solve(cuda, n, np_):
     rng = np.random.default_rng(n)
-    A = rng.normal(size=(n, np_)).astype(np.float32) / np.sqrt(np_)
+    A = (rng.normal(size=(n, np_)) / np.sqrt(np_)).astype(np.float32)
     b = rng.normal(size=n)
     x = solve_minsr(A, b, 0, ashift=1e-4)
     ref = osr.minnorm_shift(A.astype(np.float64), b, ashift=1e-4)
@@ -78,7 +78,7 @@ def test_minsr_shift_mixed_solve(cuda, n, np_):
     """FP32 Cholesky + FP64 refinement reaches the FP64 solution (stated: 1e-9 relative;
     the projection x = A^T y accumulates in FP64 like the reference)."""
     rng = np.random.default_rng(n + 1)
-    A = rng.normal(size=(n, np_)).astype(np.float32) / np.sqrt(np_)
+    A = (rng.normal(size=(n, np_)) / np.sqrt(np_)).astype(np.float32)
     b = rng.normal(size=n)
     x = solve_minsr(A, b, 2, ashift=1e-4)
     ref = osr.minnorm_shift(A.astype(np.float64), b, ashift=1e-4)

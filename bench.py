@@ -154,7 +154,7 @@ WORKLOAD_RESCONV = dict(workload="j1j2_square10_resconv8x16_minsr16384", lattice
                         l2="Obar (4.6 GB) and T (8.6 GB) exceed the 129 MB L2 every step")
 
 
-def build_workload(qtx, rank, gram, solve, workload="rbm"):
+def build_workload(qtx, rank, gram, solve, workload="rbm", conv="fp32"):
     import numpy as np
     qtx.set_random_seed(1234 + rank)
     solver = qtx.optimizer.minnorm_shift_eig(ashift=1e-4, precision=solve)
@@ -162,7 +162,7 @@ def build_workload(qtx, rank, gram, solve, workload="rbm"):
         qtx.set_default_dtype(np.complex128)
         qtx.sites.Square(10, Nparticles=(50, 50))
         H = qtx.operator.Heisenberg(J=[1.0, 0.5], n_neighbor=[1, 2], msr=True)
-        state = qtx.state.Variational(qtx.model.ResConv(8, 16, out_dtype=np.complex64))
+        state = qtx.state.Variational(qtx.model.ResConv(8, 16, out_dtype=np.complex64, conv_precision=conv))
         sampler = qtx.sampler.SpinExchange(state, 16384, thermal_steps=200, sweep_steps=200)
     else:
         qtx.set_default_dtype(np.float64)
@@ -174,14 +174,14 @@ def build_workload(qtx, rank, gram, solve, workload="rbm"):
     return state, sampler, opt
 
 
-def run_form(args, rank, world, gram, solve, e2e=True, clocks=None):
+def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32"):
     """Warm-up + timed SR steps of one form; returns timings, phases, energies, e2e."""
     import torch
     import torch.distributed as dist
     import quantax_gb300 as qtx
     from quantax_gb300 import _lib
 
-    state, sampler, opt = build_workload(qtx, rank, gram, solve, args.workload)
+    state, sampler, opt = build_workload(qtx, rank, gram, solve, args.workload, conv)
     lr = 1e-2
     energies = []
 
@@ -356,16 +356,24 @@ def main():
     plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)
     forms = {}
     if not args.no_forms:
-        # precision form: tcgen05 TF32 Gram + FP32 Cholesky with FP64 refinement, same seed
-        prec = run_form(args, rank, world, "tf32", "mixed", e2e=False)
-        de = [abs(a - b) / abs(b) for a, b in zip(prec["energies"], plain["energies"])]
-        forms["precision_tf32_gram_mixed_solve"] = {
-            "value": world * args.steps / prec["elapsed"], "unit": UNIT,
-            "ms_per_step": 1000.0 * prec["elapsed"] / args.steps,
-            "p50_step_ms": percentile(prec["lat"], 0.5), "p99_step_ms": percentile(prec["lat"], 0.99),
-            "phases_ms": {k: round(v, 4) for k, v in prec["phases"].items()},
-            "speedup_vs_plain": plain["elapsed"] / prec["elapsed"],
-            "energy_rel_diff_vs_plain_max": max(de), "energy_rel_diff_vs_plain_last": de[-1]}
+        # precision forms, same seed: tcgen05 Gram (+ tensor-core convolutions for ResConv)
+        # and FP32 Cholesky with FP64 refinement
+        if args.workload == "resconv":
+            variants = [("precision_tf32_conv_tf32_gram_mixed_solve", "tf32", "tf32"),
+                        ("precision_bf16_conv_bf16_gram_mixed_solve", "bf16", "bf16")]
+        else:
+            variants = [("precision_tf32_gram_mixed_solve", "fp32", "tf32")]
+        for name, conv, gram in variants:
+            prec = run_form(args, rank, world, gram, "mixed", e2e=False, conv=conv)
+            de = [abs(a - b) / abs(b) for a, b in zip(prec["energies"], plain["energies"])]
+            forms[name] = {
+                "value": world * args.steps / prec["elapsed"], "unit": UNIT, "conv": conv, "gram": gram,
+                "solve": "mixed",
+                "ms_per_step": 1000.0 * prec["elapsed"] / args.steps,
+                "p50_step_ms": percentile(prec["lat"], 0.5), "p99_step_ms": percentile(prec["lat"], 0.99),
+                "phases_ms": {k: round(v, 4) for k, v in prec["phases"].items()},
+                "speedup_vs_plain": plain["elapsed"] / prec["elapsed"],
+                "energy_rel_diff_vs_plain_max": max(de), "energy_rel_diff_vs_plain_last": de[-1]}
 
     if rank == 0:
         hbm, bf16, src = peaks()

@@ -173,13 +173,21 @@ int qgx_rbm_obar_noalloc(const float* table, int32_t n, int32_t m, int32_t has_v
  * Cin = 1 in block 0. Supported: L x L periodic lattices with L*L <= 256, C in {4,8,12,16}. */
 int64_t qgx_resconv_nparams(int32_t nblocks, int32_t channels);
 int64_t qgx_resconv_table_floats(int32_t nblocks, int32_t channels);
+/* Convolution arithmetic of the forward pass (log_psi, sweep, eloc). FP32: CUDA-core FMA
+ * in FP32. TF32 / BF16: the 3x3 convolutions of blocks run as tcgen05 MMAs with TF32 or
+ * BF16 operands and FP32 accumulation (residual stream, GELU, biases and the log-sum-exp
+ * stay FP32; the first, one-channel convolution stays on the CUDA cores). The tensor-core
+ * forms take C <= 16 (run padded to 16 channels) and L <= 16. */
+#define QGX_CONV_FP32 0
+#define QGX_CONV_TF32 1
+#define QGX_CONV_BF16 2
 /* Reorder the parameters into the kernels' table; re-run after every parameter update. */
 int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, float* table,
                         qgx_stream_t stream);
 /* log psi(s) as (re, im) float pairs (2*ns floats); im = 0 for real output
  * (Variational.__call__, quantax/state/variational.py:325-347). */
 int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t channels,
-                        int32_t complex_out, const uint32_t* spins, int64_t ns, float* log_psi,
+                        int32_t complex_out, int32_t conv_precision, const uint32_t* spins, int64_t ns, float* log_psi,
                         qgx_stream_t stream);
 int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns);
 /* nsteps SpinExchange proposals per chain (common_samplers.py:58-162, metropolis.py:246-322):
@@ -187,7 +195,7 @@ int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns);
  * accepts in log space on the shared Philox stream. log_psi: (re, im) pairs, in/out
  * (recomputed at the start). */
 int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels,
-                      int32_t complex_out, uint32_t* spins, float* log_psi, int32_t* accepts,
+                      int32_t complex_out, int32_t conv_precision, uint32_t* spins, float* log_psi, int32_t* accepts,
                       int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0, float reweight,
                       const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
                       int64_t workspace_bytes, qgx_stream_t stream);
@@ -197,7 +205,7 @@ int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn
  * quantax/operator/operator.py:510-562, with the nonzero compaction of :144-165);
  * eloc_im may be NULL for real output. */
 int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t channels,
-                     int32_t complex_out, const qgx_operator_t* op, const uint32_t* spins, int64_t ns,
+                     int32_t complex_out, int32_t conv_precision, const qgx_operator_t* op, const uint32_t* spins, int64_t ns,
                      double* eloc_re, double* eloc_im, void* workspace, int64_t workspace_bytes,
                      qgx_stream_t stream);
 

@@ -29,6 +29,9 @@ GRAM_FP32 = 0
 GRAM_TF32 = 1
 GRAM_BF16 = 2
 GRAM_3XTF32 = 3
+CONV_FP32 = 0
+CONV_TF32 = 1
+CONV_BF16 = 2
 
 vp = C.c_void_p
 i32 = C.c_int32
@@ -72,12 +75,12 @@ SIGNATURES = {
     "qgx_resconv_nparams": (i64, [i32, i32]),
     "qgx_resconv_table_floats": (i64, [i32, i32]),
     "qgx_resconv_prepare": (C.c_int, [vp, i32, i32, vp, vp]),
-    "qgx_resconv_log_psi": (C.c_int, [vp, i32, i32, i32, i32, vp, i64, vp, vp]),
+    "qgx_resconv_log_psi": (C.c_int, [vp, i32, i32, i32, i32, i32, vp, i64, vp, vp]),
     "qgx_resconv_sweep_workspace_bytes": (i64, [i32, i64]),
-    "qgx_resconv_sweep": (C.c_int, [vp, i32, i32, i32, i32, vp, vp, vp, i64, i32, u64, u64, f32, vp, i32, i32, vp,
+    "qgx_resconv_sweep": (C.c_int, [vp, i32, i32, i32, i32, i32, vp, vp, vp, i64, i32, u64, u64, f32, vp, i32, i32, vp,
                                     i64, vp]),
     "qgx_resconv_eloc_workspace_bytes": (i64, [i32, i64, i32]),
-    "qgx_resconv_eloc": (C.c_int, [vp, i32, i32, i32, i32, C.POINTER(Operator), vp, i64, vp, vp, vp, i64, vp]),
+    "qgx_resconv_eloc": (C.c_int, [vp, i32, i32, i32, i32, i32, C.POINTER(Operator), vp, i64, vp, vp, vp, i64, vp]),
     "qgx_resconv_jacobian_workspace_bytes": (i64, [i32, i32, i32]),
     "qgx_resconv_jacobian": (C.c_int, [vp, i32, i32, i32, i32, vp, i64, vp, vp, i64, vp, i64, vp]),
     "qgx_energy_stats": (C.c_int, [vp, vp, vp, i64, vp, vp, vp, vp]),
@@ -119,7 +122,7 @@ def _kernels(name, args):
     if name == "qgx_minsr_solve":
         return {SOLVE_SHIFT: 3, SOLVE_PINV: 6, SOLVE_SHIFT_MIXED: 36}[args[6]]
     if name == "qgx_resconv_sweep":
-        return 1 + 3 * int(args[9])
+        return 1 + 3 * int(args[10])
     if name == "qgx_sr_solve":
         return 3 if args[6] == SOLVE_SHIFT else 6
     return KERNELS_PER_CALL.get(name, 0)

@@ -17,6 +17,7 @@
 #include <cstdio>
 
 #include "qgx_common.cuh"
+#include "qgx_resconv.cuh"
 
 namespace qgx {
 namespace {
@@ -27,16 +28,9 @@ constexpr int kMaxSitesConv = 256;  // L <= 16
 struct ConvNet {
   int L, N, B, C;
   bool cplx;
+  int prec;  // QGX_CONV_*: arithmetic of the forward convolutions
 };
 
-// per-layer table: W'[i][tap][o] (cin x 9 x C) then bias[o] (C)
-__host__ __device__ inline int layer_cin(int l, int C) { return l == 0 ? 1 : C; }
-__host__ __device__ inline int64_t layer_floats(int l, int C) { return (int64_t)layer_cin(l, C) * 9 * C + C; }
-__host__ __device__ inline int64_t layer_offset(int l, int C) {
-  int64_t off = 0;
-  for (int k = 0; k < l; ++k) off += layer_floats(k, C);
-  return off;
-}
 inline int64_t table_floats_rc(int B, int C) { return layer_offset(2 * B, C); }
 __host__ __device__ inline int64_t nparams_rc(int B, int C) {
   // reference ravel order: per block conv1.weight, conv1.bias, conv2.weight, conv2.bias (not in the last block)
@@ -67,11 +61,6 @@ __global__ void rc_prepare_kernel(const float* __restrict__ params, int B, int C
       table[toff + (int64_t)cin * 9 * C + o] = has_bias ? params[pofs + nw + o] : 0.0f;
     pofs += nw + (has_bias ? C : 0);
   }
-}
-
-__device__ inline float gelu_tanh(float x) {
-  const float k0 = 0.7978845608028654f;  // sqrt(2 / pi)
-  return 0.5f * x * (1.0f + tanhf(k0 * fmaf(0.044715f * x, x * x, x)));
 }
 
 __device__ inline void stage_floats(float* dst, const float* src, int64_t n) {
@@ -666,6 +655,9 @@ int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg
 
 int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                    float2* out, cudaStream_t st) {
+  if (net.prec != QGX_CONV_FP32)
+    return rc_launch_forward_tc(table, net.L, net.B, net.C, net.cplx, cfg, ncfg, n_live, out,
+                                net.prec == QGX_CONV_BF16 ? 1 : 0, st);
   switch (net.C) {
     case 4: return launch_forward_c<4>(table, net, cfg, ncfg, n_live, out, st);
     case 8: return launch_forward_c<8>(table, net, cfg, ncfg, n_live, out, st);
@@ -679,6 +671,8 @@ bool valid_net(int L, int B, int C, int cplx) {
   return L >= 3 && L * L <= kMaxSitesConv && B >= 1 && B <= 64 && (C == 4 || C == 8 || C == 12 || C == 16) &&
          (!cplx || C % 2 == 0);
 }
+
+bool valid_prec(int p) { return p == QGX_CONV_FP32 || p == QGX_CONV_TF32 || p == QGX_CONV_BF16; }
 
 inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
 
@@ -707,11 +701,12 @@ int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, 
 }
 
 int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-                        const uint32_t* spins, int64_t ns, float* log_psi, qgx_stream_t stream) {
-  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && ns >= 0);
+                        int32_t conv_precision, const uint32_t* spins, int64_t ns, float* log_psi,
+                        qgx_stream_t stream) {
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && log_psi);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
   return launch_forward(table, net, spins, ns, nullptr, reinterpret_cast<float2*>(log_psi), as_cuda(stream));
 }
 
@@ -722,17 +717,18 @@ int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns) {
 }
 
 int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-                      uint32_t* spins, float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed,
+                      int32_t conv_precision, uint32_t* spins, float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed,
                       uint64_t step0, float reweight, const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
                       int64_t workspace_bytes, qgx_stream_t stream) {
-  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && ns >= 0 && nsteps >= 0);
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0 &&
+                nsteps >= 0);
   QGX_CHECK_ARG(nbr && z > 0 && (hop == 1 || hop == -1));
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && log_psi && workspace);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_workspace_bytes(L, ns));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   cudaStream_t st = as_cuda(stream);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
   const int nw = words_for(net.N);
   char* ws = static_cast<char*>(workspace);
   uint32_t* prop = reinterpret_cast<uint32_t*>(ws);
@@ -760,16 +756,16 @@ int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn
 }
 
 int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-                     const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im,
+                     int32_t conv_precision, const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im,
                      void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
-  QGX_CHECK_ARG(op && valid_net(L, nblocks, channels, complex_out) && ns >= 0);
+  QGX_CHECK_ARG(op && valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && eloc_re && workspace);
   const int max_conn = op->n_f1 + op->n_f2;
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_workspace_bytes(L, ns, max_conn));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   cudaStream_t st = as_cuda(stream);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
   const int nw = words_for(net.N);
   const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
   char* ws = static_cast<char*>(workspace);
@@ -810,7 +806,7 @@ int qgx_resconv_jacobian(const float* table, int32_t L, int32_t nblocks, int32_t
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && O_re && workspace && workspace_bytes > 0);
   QGX_CHECK_ARG(!complex_out || O_im);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0};
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, QGX_CONV_FP32};
   float* scratch = static_cast<float*>(workspace);
   const int64_t sf = workspace_bytes / 4;
   cudaStream_t st = as_cuda(stream);

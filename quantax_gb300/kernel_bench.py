@@ -4,7 +4,7 @@
     python -m quantax_gb300.kernel_bench sweep --ns 8192 --n 64 --m 256 --steps 64
     python -m quantax_gb300.kernel_bench eloc --ns 8192 --n 64 --m 256
     python -m quantax_gb300.kernel_bench obar --ns 8192 --n 64 --m 256
-    python -m quantax_gb300.kernel_bench rc_forward --ns 16384 --L 10 --blocks 8 --channels 16
+    python -m quantax_gb300.kernel_bench rc_forward --ns 16384 --L 10 --blocks 8 --channels 16 --conv bf16
     python -m quantax_gb300.kernel_bench rc_sweep --ns 16384 --steps 4
     python -m quantax_gb300.kernel_bench rc_eloc --ns 16384
     python -m quantax_gb300.kernel_bench rc_jacobian --ns 2048
@@ -59,10 +59,11 @@ def _resconv(a, st):
     spins = torch.empty((ns, (n + 31) // 32), dtype=torch.int32, device="cuda")
     L.call("qgx_spins_init_fixed_up", L.ptr(spins), ns, n, n // 2, 5, st)
     flop_fwd = 2.0 * n * 9 * Cc * (1 + (2 * B - 1) * Cc)  # 2 x MACs per forward
-    res = dict(ns=ns, L=Ls, blocks=B, channels=Cc, flop_per_forward=flop_fwd)
+    prec = {"fp32": L.CONV_FP32, "tf32": L.CONV_TF32, "bf16": L.CONV_BF16}[a.conv]
+    res = dict(ns=ns, L=Ls, blocks=B, channels=Cc, conv=a.conv, flop_per_forward=flop_fwd)
     if a.kernel == "rc_forward":
         lp = torch.empty((ns, 2), dtype=torch.float32, device="cuda")
-        fn = lambda: L.call("qgx_resconv_log_psi", L.ptr(table), Ls, B, Cc, 1, L.ptr(spins), ns, L.ptr(lp), st)
+        fn = lambda: L.call("qgx_resconv_log_psi", L.ptr(table), Ls, B, Cc, 1, prec, L.ptr(spins), ns, L.ptr(lp), st)
         ms = _events(fn, a.reps)
         res.update(ms=ms, forwards_per_s=ns / ms * 1e3, tflops=flop_fwd * ns / ms / 1e9)
     elif a.kernel == "rc_sweep":
@@ -70,7 +71,7 @@ def _resconv(a, st):
         nbr = torch.as_tensor(qtx.get_sites().neighbor_table(1)).cuda()
         lp = torch.empty((ns, 2), dtype=torch.float32, device="cuda")
         ws = torch.empty(L.lib().qgx_resconv_sweep_workspace_bytes(Ls, ns), dtype=torch.uint8, device="cuda")
-        fn = lambda: L.call("qgx_resconv_sweep", L.ptr(table), Ls, B, Cc, 1, L.ptr(spins), L.ptr(lp), None, ns,
+        fn = lambda: L.call("qgx_resconv_sweep", L.ptr(table), Ls, B, Cc, 1, prec, L.ptr(spins), L.ptr(lp), None, ns,
                             a.steps, 7, 0, 2.0, L.ptr(nbr), nbr.shape[1], 1, L.ptr(ws), ws.numel(), st)
         ms = _events(fn, a.reps)
         res.update(steps=a.steps, ms=ms, proposals_per_s=ns * a.steps / ms * 1e3,
@@ -83,7 +84,7 @@ def _resconv(a, st):
                          device="cuda")
         er = torch.empty(ns, dtype=torch.float64, device="cuda")
         ei = torch.empty(ns, dtype=torch.float64, device="cuda")
-        fn = lambda: L.call("qgx_resconv_eloc", L.ptr(table), Ls, B, Cc, 1, C.byref(op.struct), L.ptr(spins), ns,
+        fn = lambda: L.call("qgx_resconv_eloc", L.ptr(table), Ls, B, Cc, 1, prec, C.byref(op.struct), L.ptr(spins), ns,
                             L.ptr(er), L.ptr(ei), L.ptr(ws), ws.numel(), st)
         ms = _events(fn, a.reps)
         res.update(ms=ms, samples_per_s=ns / ms * 1e3)
@@ -105,6 +106,8 @@ def main():
     ap.add_argument("--blocks", type=int, default=8)
     ap.add_argument("--channels", type=int, default=16)
     ap.add_argument("--mode", default="tf32", choices=["fp32", "tf32", "bf16", "3xtf32"])
+    ap.add_argument("--conv", default="fp32", choices=["fp32", "tf32", "bf16"],
+                    help="ResConv forward convolution arithmetic")
     ap.add_argument("--rows", type=int, default=2048)
     ap.add_argument("--k", type=int, default=16640)
     ap.add_argument("--ns", type=int, default=8192)

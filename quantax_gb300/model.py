@@ -137,7 +137,10 @@ class ResConv:
     holomorphic = False
 
     def __init__(self, nblocks: int, channels: int, kernel_size: int = 3, final_activation=None, trans_symm=None,
-                 dtype=np.float32, out_dtype=None, seed: Optional[int] = None):
+                 dtype=np.float32, out_dtype=None, seed: Optional[int] = None, conv_precision: str = "fp32"):
+        """conv_precision: arithmetic of the forward convolutions used by sampling and local
+        energies -- "fp32" (CUDA cores), "tf32" or "bf16" (tensor-core operands, FP32
+        accumulation). The log-derivatives are always computed in FP32."""
         from .global_defs import get_lattice
         if kernel_size != 3 or final_activation is not None or trans_symm is not None:
             raise NotImplementedError("quantax_gb300 ResConv: 3x3 kernels, exp_by_scale output and the default "
@@ -152,6 +155,7 @@ class ResConv:
         self.nblocks = int(nblocks)
         self.channels = int(channels)
         self.complex_output = out_dtype is not None and np.issubdtype(np.dtype(out_dtype), np.complexfloating)
+        self.conv_precision = conv_precision
         rng = np.random.default_rng(get_subkeys() if seed is None else seed)
         parts = []
         for b in range(self.nblocks):
@@ -174,12 +178,27 @@ class ResConv:
         _lib.call("qgx_resconv_prepare", _lib.ptr(params), self.nblocks, self.channels, _lib.ptr(table),
                   _lib.stream_ptr())
 
+    @property
+    def conv_precision(self) -> str:
+        return self._conv_precision
+
+    @conv_precision.setter
+    def conv_precision(self, p: str):
+        codes = {"fp32": _lib.CONV_FP32, "tf32": _lib.CONV_TF32, "bf16": _lib.CONV_BF16}
+        if p not in codes:
+            raise ValueError(f"conv_precision must be one of {sorted(codes)}, got {p!r}")
+        self._conv_precision = p
+        self._conv_code = codes[p]
+
     def _args(self):
         return (self.L, self.nblocks, self.channels, int(self.complex_output))
 
+    def _fwd_args(self):
+        return self._args() + (self._conv_code,)
+
     def log_psi(self, table, packed, out):
         """out: (ns, 2) float32 (re, im)."""
-        _lib.call("qgx_resconv_log_psi", _lib.ptr(table), *self._args(), _lib.ptr(packed), packed.shape[0],
+        _lib.call("qgx_resconv_log_psi", _lib.ptr(table), *self._fwd_args(), _lib.ptr(packed), packed.shape[0],
                   _lib.ptr(out), _lib.stream_ptr())
 
     def sweep_workspace_bytes(self, ns):
@@ -189,7 +208,7 @@ class ResConv:
               workspace):
         if proposal != _lib.PROPOSAL_SPIN_EXCHANGE:
             raise NotImplementedError("the ResConv sampler implements SpinExchange proposals")
-        _lib.call("qgx_resconv_sweep", _lib.ptr(table), *self._args(), _lib.ptr(packed), _lib.ptr(log_psi),
+        _lib.call("qgx_resconv_sweep", _lib.ptr(table), *self._fwd_args(), _lib.ptr(packed), _lib.ptr(log_psi),
                   _lib.ptr(accepts), packed.shape[0], int(nsteps), int(seed), int(step0), float(reweight),
                   _lib.ptr(nbr), int(z), int(hop), _lib.ptr(workspace), workspace.numel(), _lib.stream_ptr())
 
@@ -197,7 +216,7 @@ class ResConv:
         return int(_lib.lib().qgx_resconv_eloc_workspace_bytes(self.L, ns, max_conn))
 
     def eloc(self, table, compiled_op, packed, out_re, out_im, workspace):
-        _lib.call("qgx_resconv_eloc", _lib.ptr(table), *self._args(), C.byref(compiled_op.struct),
+        _lib.call("qgx_resconv_eloc", _lib.ptr(table), *self._fwd_args(), C.byref(compiled_op.struct),
                   _lib.ptr(packed), packed.shape[0], _lib.ptr(out_re), _lib.ptr(out_im), _lib.ptr(workspace),
                   workspace.numel(), _lib.stream_ptr())
 

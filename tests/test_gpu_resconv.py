@@ -37,11 +37,11 @@ class Net:
         Lb.call("qgx_resconv_prepare", Lb.ptr(self.pt), B, Cc, Lb.ptr(self.table), Lb.stream_ptr())
         self.oracle = resconv.ResConv(self.p, L, B, Cc, cplx)
 
-    def log_psi(self, packed):
+    def log_psi(self, packed, prec=0):
         from quantax_gb300 import _lib as Lb
         out = torch.empty((packed.shape[0], 2), dtype=torch.float32, device="cuda")
-        Lb.call("qgx_resconv_log_psi", Lb.ptr(self.table), self.L, self.B, self.C, int(self.cplx), Lb.ptr(packed),
-                packed.shape[0], Lb.ptr(out), Lb.stream_ptr())
+        Lb.call("qgx_resconv_log_psi", Lb.ptr(self.table), self.L, self.B, self.C, int(self.cplx), prec,
+                Lb.ptr(packed), packed.shape[0], Lb.ptr(out), Lb.stream_ptr())
         o = out.cpu().numpy().astype(np.float64)
         return o[:, 0] + 1j * o[:, 1]
 
@@ -77,7 +77,7 @@ def test_resconv_spin_exchange_sweep_bit_exact(cuda):
     acc = torch.empty(32, dtype=torch.int32, device="cuda")
     nbr_t = torch.as_tensor(nbr).cuda()
     ws = torch.empty(Lb.lib().qgx_resconv_sweep_workspace_bytes(L, 32), dtype=torch.uint8, device="cuda")
-    Lb.call("qgx_resconv_sweep", Lb.ptr(net.table), L, B, Cc, 1, Lb.ptr(packed), Lb.ptr(lp), Lb.ptr(acc), 32, nsteps,
+    Lb.call("qgx_resconv_sweep", Lb.ptr(net.table), L, B, Cc, 1, 0, Lb.ptr(packed), Lb.ptr(lp), Lb.ptr(acc), 32, nsteps,
             seed, 0, 2.0, Lb.ptr(nbr_t), nbr.shape[1], 1, Lb.ptr(ws), ws.numel(), Lb.stream_ptr())
     assert (_unpack(packed, n) == want).all()
     assert (acc.cpu().numpy() == st["accepts"]).all()
@@ -99,7 +99,7 @@ def test_resconv_local_energy_j1j2(cuda, cplx):
     ws = torch.empty(Lb.lib().qgx_resconv_eloc_workspace_bytes(L, 40, max_conn), dtype=torch.uint8, device="cuda")
     er = torch.empty(40, dtype=torch.float64, device="cuda")
     ei = torch.empty(40, dtype=torch.float64, device="cuda")
-    Lb.call("qgx_resconv_eloc", Lb.ptr(net.table), L, B, Cc, int(cplx), C.byref(op.struct), Lb.ptr(_pack(s)), 40,
+    Lb.call("qgx_resconv_eloc", Lb.ptr(net.table), L, B, Cc, int(cplx), 0, C.byref(op.struct), Lb.ptr(_pack(s)), 40,
             Lb.ptr(er), Lb.ptr(ei), Lb.ptr(ws), ws.numel(), Lb.stream_ptr())
     got = er.cpu().numpy() + 1j * ei.cpu().numpy()
     np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-4 * np.abs(want).max())

@@ -181,7 +181,8 @@ int64_t qgx_resconv_table_floats(int32_t nblocks, int32_t channels);
 #define QGX_CONV_FP32 0
 #define QGX_CONV_TF32 1
 #define QGX_CONV_BF16 2
-/* Reorder the parameters into the kernels' table; re-run after every parameter update. */
+/* Reorder the parameters into the kernels' table (FP32 layers, then the BF16 and TF32
+ * weight images of the tensor-core forward); re-run after every parameter update. */
 int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, float* table,
                         qgx_stream_t stream);
 /* log psi(s) as (re, im) float pairs (2*ns floats); im = 0 for real output

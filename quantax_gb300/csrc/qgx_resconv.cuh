@@ -1,6 +1,10 @@
 // ResConv parameter-table layout shared by the CUDA-core and the tensor-core kernels.
-// Per layer l (two per block): W'[i][tap][o] (cin x 9 x C floats; tap = 3 (dy+1) + (dx+1))
-// followed by bias[o] (C floats, zero for the last block's second convolution).
+// FP32 part, per layer l (two per block): W'[i][tap][o] (cin x 9 x C floats; tap =
+// 3 (dy+1) + (dx+1)) followed by bias[o] (C floats, zero for the last block's second
+// convolution). Then, 256-byte aligned, the tensor-core weight images: per layer the smem
+// image of the MMA B operand for 16 channels (zero-padded), [tap][chunk][o][e] with 16-byte
+// chunks of e = 8 bf16 / 4 tf32 input channels, followed by 16 FP32 biases; first the BF16
+// image of all layers, then the TF32 one (values rounded to nearest).
 #pragma once
 
 #include <cstdint>
@@ -16,12 +20,45 @@ __host__ __device__ inline int64_t layer_offset(int l, int C) {
   return off;
 }
 
+inline int64_t table_floats_fp32(int B, int C) { return layer_offset(2 * B, C); }
+
+constexpr int kTcCh = 16;  // channel width of the tensor-core tiles
+// bytes of one layer's weight image; esz: operand bytes (2 bf16, 4 tf32)
+__host__ __device__ inline int64_t tc_layer_bytes(int esz) { return 9LL * (kTcCh * esz / 16) * 256 + 64; }
+__host__ __device__ inline int64_t al256_i64(int64_t b) { return (b + 255) / 256 * 256; }
+// byte offset of an image from the table start; kind 1: BF16, 0: TF32
+__host__ __device__ inline int64_t tc_image_offset(int B, int C, int kind) {
+  int64_t off = al256_i64(layer_offset(2 * B, C) * 4);
+  if (kind == 0) off += al256_i64(2LL * B * tc_layer_bytes(2));
+  return off;
+}
+inline int64_t table_floats_rc(int B, int C) { return (tc_image_offset(B, C, 0) + 2LL * B * tc_layer_bytes(4)) / 4; }
+
+// TF32 operand value: round to nearest (ties away) on 10 mantissa bits; the MMA itself
+// would drop the low 13 bits, a bias that accumulates through the residual stack
+__device__ inline float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
 __device__ inline float gelu_tanh(float x) {
   const float k0 = 0.7978845608028654f;  // sqrt(2 / pi)
   return 0.5f * x * (1.0f + tanhf(k0 * fmaf(0.044715f * x, x * x, x)));
 }
 
+// the same function as 0.5 x (1 + tanh u) = x / (1 + exp(-2u)), with the fast exponential;
+// exp overflow gives x / inf = 0, the limit of gelu at -inf
+__device__ inline float gelu_fast(float x) {
+  const float k0 = 0.7978845608028654f;
+  const float u = k0 * fmaf(0.044715f * x, x * x, x);
+  return __fdividef(x, 1.0f + __expf(-2.0f * u));
+}
+
 }  // namespace
+
+// writes both tensor-core weight images from the FP32 part of the table (resconv_tc.cu)
+int rc_prepare_tc_images(float* table, int B, int C, cudaStream_t st);
 
 // tensor-core forward (resconv_tc.cu); kind 0: TF32 operands, 1: BF16 operands
 int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,

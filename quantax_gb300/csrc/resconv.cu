@@ -31,7 +31,6 @@ struct ConvNet {
   int prec;  // QGX_CONV_*: arithmetic of the forward convolutions
 };
 
-inline int64_t table_floats_rc(int B, int C) { return layer_offset(2 * B, C); }
 __host__ __device__ inline int64_t nparams_rc(int B, int C) {
   // reference ravel order: per block conv1.weight, conv1.bias, conv2.weight, conv2.bias (not in the last block)
   int64_t n = 0;
@@ -697,7 +696,9 @@ int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, 
   QGX_CHECK_ARG(params && table && nblocks >= 1 && (channels == 4 || channels == 8 || channels == 12 || channels == 16));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(table) & 15) == 0);
   rc_prepare_kernel<<<16, 256, 0, as_cuda(stream)>>>(params, nblocks, channels, table);
-  return launch_status();
+  const int rc = launch_status();
+  if (rc != QGX_OK) return rc;
+  return rc_prepare_tc_images(table, nblocks, channels, as_cuda(stream));
 }
 
 int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,

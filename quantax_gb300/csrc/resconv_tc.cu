@@ -10,9 +10,15 @@
 // W_tap[16 x 16]. No im2col tile is built; the descriptor (no swizzle, K-major: 16-byte
 // core-matrix rows, leading offset = one chunk plane, stride offset = 8 rows) points into
 // the activation buffer directly. All tiles of a layer accumulate in TMEM at once (16
-// columns each); one commit, then the epilogue applies bias, GELU / the residual add and
-// refills the halo. The residual stream x stays in FP32; the one-channel first convolution
-// runs on the CUDA cores.
+// columns each) and one commit signals the layer.
+//
+// Threads: three warpgroups; thread t owns TMEM lane t % 128 of the tiles j = t / 128,
+// t / 128 + 3, ... (at most three), i.e. the same padded rows in every layer, so the FP32
+// residual stream of those rows lives in its registers. The epilogue of a convolution
+// reads the accumulator row, applies bias and GELU (or the residual add followed by the
+// next block's pre-activation) and writes the packed 16-byte chunks of the row and of its
+// periodic halo copies. Layer weights come from a pre-converted image in the parameter
+// table, fetched one layer ahead with cp.async.bulk into a double buffer.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -24,16 +30,29 @@
 namespace qgx {
 namespace {
 
-constexpr int kThreadsTc = 128;
-constexpr int kCh = 16;  // channel width of the tiles; C < 16 runs zero-padded
+constexpr int kMaxTiles = 9;  // 128-row tiles per CTA
+constexpr int kCh = kTcCh;
+// launch shapes of the library's forward (warpgroups, tile rows per thread, CTAs per SM),
+// from timings on GB300 at L = 10, 16 channels
+template <int KIND>
+struct TcLaunch;
+template <>
+struct TcLaunch<1> {
+  static constexpr int WG = 2, RPT = 2, CTAS = 3;
+};
+template <>
+struct TcLaunch<0> {
+  static constexpr int WG = 2, RPT = 2, CTAS = 2;
+};
 constexpr int kGuard = 32;
 
 template <int KIND>  // 1: bf16, 0: tf32
 struct TcCfg {
   static constexpr int esz = KIND == 1 ? 2 : 4;
-  static constexpr int epc = 16 / esz;           // elements per 16-byte chunk
-  static constexpr int chunks = kCh / epc;       // chunk planes of the 16 channels
-  static constexpr int mma_per_tap = chunks / 2; // an MMA covers 32 bytes of K
+  static constexpr int epc = 16 / esz;            // elements per 16-byte chunk
+  static constexpr int chunks = kCh / epc;        // chunk planes of the 16 channels
+  static constexpr int mma_per_tap = chunks / 2;  // an MMA covers 32 bytes of K
+  static constexpr int layer_bytes = 9 * chunks * 256 + 64;
   static constexpr uint32_t fmt = KIND == 1 ? 1u : 2u;
   static constexpr uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(kCh >> 3) << 17) |
                                     ((uint32_t)(128 >> 4) << 24);
@@ -42,50 +61,40 @@ struct TcCfg {
 struct TcShape {
   int L, N, Lp, NP, B, C, S, ntiles, rows_tot;
   bool cplx;
-  // byte offsets in shared memory
-  int oX, oP, oQ, oW, oBias, oW0, oHalo, oNbr, oBar;
+  int oP, oQ, oW, oBar;  // byte offsets in shared memory
+  int wbuf;              // bytes between the two weight buffers
   int smem;
   uint32_t tmem_cols;
 };
 
-// samples per CTA: enough padded rows for nine 128-row tiles at L = 10
-inline int tc_samples_per_cta(int L) { return std::max(1, std::min(32, 1152 / ((L + 2) * (L + 2)))); }
+// samples per CTA: as many as fit in `tiles` 128-row tiles
+inline int tc_samples_per_cta(int L, int tiles) { return std::max(1, std::min(32, tiles * 128 / ((L + 2) * (L + 2)))); }
 
 inline TcShape tc_shape(int L, int B, int C, bool cplx, int esz, int S) {
   TcShape s;
   s.L = L;
-  s.C = C;
   s.N = L * L;
   s.Lp = L + 2;
   s.NP = s.Lp * s.Lp;
   s.B = B;
+  s.C = C;
   s.cplx = cplx;
   s.S = S;
-  const int rows = s.S * s.NP;
-  s.ntiles = (rows + 127) / 128;
+  s.ntiles = (S * s.NP + 127) / 128;
   s.rows_tot = kGuard + s.ntiles * 128 + kGuard;
   auto al = [](int x, int a) { return (x + a - 1) / a * a; };
+  const int plane = s.rows_tot * 16, chunks = kCh * esz / 16;
+  const int lb = (int)tc_layer_bytes(esz);
   int o = 0;
-  s.oX = o;
-  o = al(o + s.S * kCh * s.N * 4, 128);
-  const int plane = s.rows_tot * 16;
-  const int chunks = kCh * esz / 16;
   s.oP = o;
   o = al(o + chunks * plane, 128);
   s.oQ = o;
   o = al(o + chunks * plane, 128);
   s.oW = o;
-  o = al(o + 9 * chunks * 256, 128);
-  s.oBias = o;
-  o += kCh * 4;
-  s.oW0 = o;
-  o += (9 * kCh + kCh) * 4;
-  s.oHalo = o;
-  o = al(o + s.NP * 2, 16);
-  s.oNbr = o;
-  o = al(o + s.N * 9 * 2, 16);
+  s.wbuf = al(lb, 128);
+  o += 2 * s.wbuf;
   s.oBar = o;
-  o += 16;
+  o += 32;
   s.smem = o + 1024;  // slack for aligning the base to 1024 bytes
   uint32_t cols = 32;
   while (cols < (uint32_t)(s.ntiles * 16)) cols <<= 1;
@@ -117,6 +126,13 @@ __device__ inline void mma_tc(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t 
   }
 }
 
+__device__ inline void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ inline void tmem_ld_16cols(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
   asm volatile(
@@ -130,108 +146,111 @@ __device__ inline void tmem_ld_16cols(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// TF32 operand value: round to nearest (ties away) on 10 mantissa bits; the MMA itself
-// would drop the low 13 bits, a bias that accumulates through the residual stack
-__device__ inline float to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+// GELU of a value that is next rounded to the operand type: BF16 keeps 8 bits, below the
+// error of the hardware tanh (about 2^-11); TF32 uses the exponential form
+__device__ inline float gelu_tanh_hw(float x) {
+  const float k0 = 0.7978845608028654f;
+  const float u = k0 * fmaf(0.044715f * x, x * x, x);
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  const float h = 0.5f * x;
+  return fmaf(h, t, h);
 }
 
-// store one channel value of padded row m (absolute row index incl. guard) into a chunk-major buffer
 template <int KIND>
-__device__ inline void put(uint8_t* buf, int rows_tot, int m, int ch, float v) {
-  using Cfg = TcCfg<KIND>;
-  uint8_t* p = buf + (ch / Cfg::epc) * rows_tot * 16 + m * 16 + (ch % Cfg::epc) * Cfg::esz;
-  if (KIND == 1)
-    *reinterpret_cast<__nv_bfloat16*>(p) = __float2bfloat16_rn(v);
-  else
-    *reinterpret_cast<float*>(p) = to_tf32(v);
+__device__ inline float gelu_op(float x) {
+  return KIND == 1 ? gelu_tanh_hw(x) : gelu_fast(x);
 }
 
-// halo rows of every sample repeat their periodic interior rows (all chunk planes)
+// The padded row of a thread's tile row: sample slot a, grid position (py, px); interior
+// rows (1 <= py, px <= L) of live samples carry sites, the others are halo or padding.
+struct RowPos {
+  int a, py, px;
+  bool live;
+};
+
+__device__ inline RowPos row_pos(int m, const TcShape& sh, int s_here) {
+  RowPos r;
+  r.a = m / sh.NP;
+  const int p = m - r.a * sh.NP;
+  r.py = p / sh.Lp;
+  r.px = p - r.py * sh.Lp;
+  r.live = r.a < s_here && r.py >= 1 && r.py <= sh.L && r.px >= 1 && r.px <= sh.L;
+  return r;
+}
+
+// a live row packed in one register (a << 16 | py << 8 | px), -1 otherwise
+__device__ inline int pack_pos(const RowPos& r) { return r.live ? (r.a << 16) | (r.py << 8) | r.px : -1; }
+__device__ inline RowPos unpack_pos(int v) { return RowPos{v >> 16, (v >> 8) & 255, v & 255, v >= 0}; }
+
+// Write the 16 channel values of a live row as packed chunks, into the row and into each
+// halo row that repeats it (one more row at a boundary, three at a corner).
 template <int KIND>
-__device__ inline void fill_halo(uint8_t* buf, const TcShape& sh, const int16_t* halo, int s_here) {
+__device__ inline void put_row(uint8_t* buf, const TcShape& sh, const RowPos& rp, const float (&val)[16]) {
   using Cfg = TcCfg<KIND>;
-  const int per = sh.NP * Cfg::chunks;
-  for (int e = threadIdx.x; e < s_here * per; e += blockDim.x) {
-    const int a = e / per, rem = e % per;
-    const int p = rem / Cfg::chunks, c = rem % Cfg::chunks;
-    const int src = halo[p];
-    if (src == p) continue;
-    const int base = kGuard + a * sh.NP;
-    uint8_t* plane = buf + c * sh.rows_tot * 16;
-    *reinterpret_cast<uint4*>(plane + (base + p) * 16) = *reinterpret_cast<const uint4*>(plane + (base + src) * 16);
+  uint4 ch[Cfg::chunks];
+  if (KIND == 1) {
+#pragma unroll
+    for (int c = 0; c < Cfg::chunks; ++c) {
+      uint32_t w[4];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(val[8 * c + 2 * h], val[8 * c + 2 * h + 1]);
+        w[h] = *reinterpret_cast<const uint32_t*>(&b2);
+      }
+      ch[c] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < Cfg::chunks; ++c)
+      ch[c] = make_uint4(__float_as_uint(to_tf32(val[4 * c])), __float_as_uint(to_tf32(val[4 * c + 1])),
+                         __float_as_uint(to_tf32(val[4 * c + 2])), __float_as_uint(to_tf32(val[4 * c + 3])));
+  }
+  const int L = sh.L;
+  const int y2 = rp.py == 1 ? L + 1 : (rp.py == L ? 0 : -1);
+  const int x2 = rp.px == 1 ? L + 1 : (rp.px == L ? 0 : -1);
+  const int base = kGuard + rp.a * sh.NP;
+  const int plane = sh.rows_tot * 16;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int yy = (k & 2) ? y2 : rp.py, xx = (k & 1) ? x2 : rp.px;
+    if (yy < 0 || xx < 0) continue;
+    uint8_t* dst = buf + (size_t)(base + yy * sh.Lp + xx) * 16;
+#pragma unroll
+    for (int c = 0; c < Cfg::chunks; ++c) *reinterpret_cast<uint4*>(dst + c * plane) = ch[c];
   }
 }
 
-// W_smem[tap][chunk][n][epc] from the FP32 table slice [i][tap][o] (+ bias); channels >= C are zero
-template <int KIND>
-__device__ inline void stage_weights(uint8_t* wsm, float* bias, const float* tl, int C) {
-  using Cfg = TcCfg<KIND>;
-  const int total = 9 * Cfg::chunks * kCh * Cfg::epc;
-  for (int e = threadIdx.x; e < total; e += blockDim.x) {
-    const int tap = e / (Cfg::chunks * kCh * Cfg::epc);
-    const int rem = e % (Cfg::chunks * kCh * Cfg::epc);
-    const int c = rem / (kCh * Cfg::epc);
-    const int n = (rem / Cfg::epc) % kCh;
-    const int k = rem % Cfg::epc;
-    const int i = c * Cfg::epc + k;
-    const float w = (i < C && n < C) ? __ldg(tl + (i * 9 + tap) * C + n) : 0.0f;
-    uint8_t* dst = wsm + ((tap * Cfg::chunks + c) * kCh + n) * 16 + k * Cfg::esz;
-    if (KIND == 1)
-      *reinterpret_cast<__nv_bfloat16*>(dst) = __float2bfloat16_rn(w);
-    else
-      *reinterpret_cast<float*>(dst) = to_tf32(w);
-  }
-  for (int o = threadIdx.x; o < kCh; o += blockDim.x) bias[o] = o < C ? __ldg(tl + C * 9 * C + o) : 0.0f;
-}
-
-__device__ inline int padded_row(int r, int L) { return (r / L + 1) * (L + 2) + (r % L) + 1; }
-
-template <int KIND>
-__global__ void __launch_bounds__(kThreadsTc, 1)
-    rc_forward_tc_kernel(const float* __restrict__ table, TcShape sh, const uint32_t* __restrict__ cfg, int64_t ncfg,
-                         const int64_t* __restrict__ n_live, float2* __restrict__ out, int32_t* __restrict__ status) {
+// WG warpgroups, RPT tile rows per thread (tiles j = wg, wg + WG, ...), MINB CTAs per SM
+template <int KIND, int WG, int RPT, int MINB>
+__global__ void __launch_bounds__(128 * WG, MINB)
+    rc_forward_tc_kernel(const uint8_t* __restrict__ wimg, TcShape sh, const uint32_t* __restrict__ cfg,
+                         int64_t ncfg, const int64_t* __restrict__ n_live, float2* __restrict__ out) {
   using Cfg = TcCfg<KIND>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float* X = reinterpret_cast<float*>(sm + sh.oX);
   uint8_t* P = sm + sh.oP;
   uint8_t* Q = sm + sh.oQ;
   uint8_t* W = sm + sh.oW;
-  float* bias = reinterpret_cast<float*>(sm + sh.oBias);
-  float* W0 = reinterpret_cast<float*>(sm + sh.oW0);
-  int16_t* halo = reinterpret_cast<int16_t*>(sm + sh.oHalo);
-  int16_t* nbr = reinterpret_cast<int16_t*>(sm + sh.oNbr);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + sh.oBar);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + sh.oBar + 8);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + sh.oBar);
+  uint64_t* wbar = mbar + 1;  // two: one per weight buffer
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + sh.oBar + 24);
   __shared__ int fail;
 
-  const int L = sh.L, N = sh.N, Lp = sh.Lp, NP = sh.NP, S = sh.S, nw = words_for(N);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kThreads = 128 * WG;
+  const int L = sh.L, N = sh.N, S = sh.S, nw = words_for(N);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, wg = tid >> 7, row_in_tile = tid & 127;
   const int plane = sh.rows_tot * 16;
+  const int nlayers = 2 * sh.B;
+  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
 
-  for (int p = threadIdx.x; p < NP; p += blockDim.x) {
-    const int py = p / Lp, px = p % Lp;
-    const int sy = (py - 1 + L) % L, sx = (px - 1 + L) % L;
-    halo[p] = (int16_t)((sy + 1) * Lp + sx + 1);
-  }
-  for (int e = threadIdx.x; e < N * 9; e += blockDim.x) {
-    const int r = e / 9, t = e % 9, y = r / L, x = r % L;
-    nbr[e] = (int16_t)(((y + t / 3 - 1 + L) % L) * L + (x + t % 3 - 1 + L) % L);
-  }
-  // guard rows and both buffers start zeroed (rows outside any sample stay finite)
-  for (int e = threadIdx.x; e < Cfg::chunks * plane / 16; e += blockDim.x) {
+  // P and Q start zeroed: guard and padding rows stay finite
+  for (int e = tid; e < 2 * Cfg::chunks * plane / 16; e += blockDim.x)
     reinterpret_cast<uint4*>(P)[e] = make_uint4(0, 0, 0, 0);
-    reinterpret_cast<uint4*>(Q)[e] = make_uint4(0, 0, 0, 0);
-  }
-  for (int e = threadIdx.x; e < 10 * kCh; e += blockDim.x) {
-    const int t = e / kCh, o = e % kCh;  // t = 9: bias
-    W0[e] = o < sh.C ? __ldg(table + t * sh.C + o) : 0.0f;
-  }
-  if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
+  if (tid == 0) {
+    mbar_init(mbar, 1);
+    mbar_init(wbar, 1);
+    mbar_init(wbar + 1, 1);
     fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -245,123 +264,153 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  uint32_t phase = 0;
+  const uint32_t tmem_lane = (uint32_t)(32 * (warp & 3)) << 16;
+  uint32_t lc = 0;                       // convolutions run by this CTA so far
+  uint32_t w_issued = 0, w_done = 0;     // weight loads issued / waited for (thread 0)
+  if (tid == 0 && (int64_t)blockIdx.x * S < total) {
+    mbar_expect_tx(wbar, Cfg::layer_bytes);
+    bulk_load(W, wimg, Cfg::layer_bytes, wbar);
+    w_issued = 1;
+  }
 
-  // one convolution with C input channels from buffer `in`: accumulate every tile in TMEM
-  auto conv_tc = [&](const uint8_t* in) -> bool {
+  // one convolution of the buffer `in` into TMEM (all tiles); false on a timed-out wait
+  auto conv = [&](const uint8_t* in, bool more_after) -> bool {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
     __syncthreads();
-    tc_fence_after();
-    if (threadIdx.x == 0) {
-      const uint32_t ib = smem_u32(in), wb = smem_u32(W);
-      for (int j = 0; j < sh.ntiles; ++j) {
-        const int row0 = kGuard + j * 128;
-        for (int t = 0; t < 9; ++t) {
-          const int off = (t / 3 - 1) * Lp + (t % 3 - 1);
+    const int buf = lc & 1;
+    if (tid == 0) {
+      tc_fence_after();
+      if (!mbar_wait(wbar + buf, (lc >> 1) & 1)) {
+        fail = 1;
+      } else {
+        w_done = lc + 1;
+        // descriptors advance in 16-byte units of the start-address field (addresses stay
+        // below 256 KB, so the additions never leave the 14-bit field)
+        const uint64_t da0 = desc_noswizzle(smem_u32(in) + kGuard * 16, (uint32_t)plane, 128);
+        const uint64_t db0 = desc_noswizzle(smem_u32(W + buf * sh.wbuf), 256, 128);
+        for (int j = 0; j < sh.ntiles; ++j) {
+          const uint64_t daj = da0 + (uint64_t)(j * 128);
+          const uint32_t dj = tmem + (uint32_t)(16 * j);
 #pragma unroll
-          for (int q = 0; q < Cfg::mma_per_tap; ++q) {
-            const uint64_t da = desc_noswizzle(ib + (uint32_t)((row0 + off) * 16 + 2 * q * plane), (uint32_t)plane, 128);
-            const uint64_t db = desc_noswizzle(wb + (uint32_t)((t * Cfg::chunks + 2 * q) * 256), 256, 128);
-            mma_tc<KIND>(tmem + (uint32_t)(16 * j), da, db, (t > 0 || q > 0) ? 1u : 0u);
+          for (int t = 0; t < 9; ++t) {
+            const int off = (t / 3 - 1) * sh.Lp + (t % 3 - 1);
+#pragma unroll
+            for (int q = 0; q < Cfg::mma_per_tap; ++q)
+              mma_tc<KIND>(dj, daj + (uint64_t)(int64_t)(off + 2 * q * sh.rows_tot),
+                           db0 + (uint64_t)((t * Cfg::chunks + 2 * q) * 16), (t > 0 || q > 0) ? 1u : 0u);
           }
         }
+        mma_commit(mbar);
+        if (more_after) {  // next layer's weights into the other buffer (its last reader has finished)
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          mbar_expect_tx(wbar + (buf ^ 1), Cfg::layer_bytes);
+          bulk_load(W + (buf ^ 1) * sh.wbuf, wimg + (size_t)((lc + 1) % nlayers) * Cfg::layer_bytes,
+                    Cfg::layer_bytes, wbar + (buf ^ 1));
+          w_issued = lc + 2;
+        }
       }
-      mma_commit(bar);
     }
-    const bool ok = mbar_wait(bar, phase & 1u);
-    phase++;
-    if (!ok) fail = 1;
+    // thread 0 waits for the commit; the others wait at the barrier without taking issue
+    // slots from the other CTAs on the SM
+    if (tid == 0 && !fail && !mbar_wait(mbar, lc & 1)) fail = 1;
     __syncthreads();
+    ++lc;
     tc_fence_after();
     return fail == 0;
   };
 
-  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
-  for (int64_t base = (int64_t)blockIdx.x * S; base < total && !fail; base += (int64_t)gridDim.x * S) {
+  int64_t base = (int64_t)blockIdx.x * S;
+  for (; base < total; base += (int64_t)gridDim.x * S) {
     const int s_here = (int)(total - base < S ? total - base : S);
-    __syncthreads();
-    for (int e = threadIdx.x; e < S * N; e += blockDim.x) {
-      const int a = e / N, r = e % N;
-      float v = 0.0f;
-      if (a < s_here) v = ((cfg[(base + a) * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
-      for (int c = 0; c < kCh; ++c) X[(a * kCh + c) * N + r] = c < sh.C ? v : 0.0f;
-    }
-    __syncthreads();
-    // block 0, conv1 (one input channel) on the CUDA cores: Q = gelu(conv(s / sqrt 2) + b1)
-    for (int e = threadIdx.x; e < s_here * N; e += blockDim.x) {
-      const int a = e / N, r = e % N;
-      float acc[kCh];
+    const bool next_group = base + (int64_t)gridDim.x * S < total;
+    float x[RPT][16];  // residual stream of this thread's rows
+    int pos[RPT];      // packed RowPos of those rows
+    // x = s on the C channels; P = s / sqrt 2 on channel 0 (block 0's conv1 has one input channel)
 #pragma unroll
-      for (int o = 0; o < kCh; ++o) acc[o] = W0[9 * kCh + o];
+    for (int k = 0; k < RPT; ++k) {
+      const int j = wg + WG * k;
+      pos[k] = j < sh.ntiles ? pack_pos(row_pos(j * 128 + row_in_tile, sh, s_here)) : -1;
+      const RowPos rp = unpack_pos(pos[k]);
+      if (!rp.live) continue;
+      const int r = (rp.py - 1) * L + (rp.px - 1);
+      const float sv = ((cfg[(base + rp.a) * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
+      float v[16];
 #pragma unroll
-      for (int t = 0; t < 9; ++t) {
-        const float v = X[(a * kCh) * N + nbr[r * 9 + t]] * 0.70710678118654752f;
-#pragma unroll
-        for (int o = 0; o < kCh; ++o) acc[o] = fmaf(v, W0[t * kCh + o], acc[o]);
+      for (int c = 0; c < 16; ++c) {
+        x[k][c] = c < sh.C ? sv : 0.0f;
+        v[c] = c == 0 ? sv * 0.70710678118654752f : 0.0f;
       }
-      const int m = kGuard + a * NP + padded_row(r, L);
-#pragma unroll
-      for (int o = 0; o < kCh; ++o) put<KIND>(Q, sh.rows_tot, m, o, gelu_tanh(acc[o]));
+      put_row<KIND>(P, sh, rp, v);
     }
-    __syncthreads();
-    fill_halo<KIND>(Q, sh, halo, s_here);
+    bool ok = true;
     for (int b = 0; b < sh.B; ++b) {
-      if (b > 0) {
-        // P = gelu(x / sqrt(b + 1)), conv1 on the tensor cores, Q = gelu(acc + b1)
-        const float scale = rsqrtf((float)(b + 1));
-        __syncthreads();
-        for (int e = threadIdx.x; e < s_here * kCh * N; e += blockDim.x) {
-          const int a = e / (kCh * N), rem = e % (kCh * N), c = rem / N, r = rem % N;
-          put<KIND>(P, sh.rows_tot, kGuard + a * NP + padded_row(r, L), c, gelu_tanh(X[e] * scale));
-        }
-        __syncthreads();
-        fill_halo<KIND>(P, sh, halo, s_here);
-        stage_weights<KIND>(W, bias, table + layer_offset(2 * b, sh.C), sh.C);
-        if (!conv_tc(P)) break;
-        for (int j = 0; j < sh.ntiles; ++j) {
+      // conv1: Q = gelu(conv(P) + b1)
+      if (!(ok = conv(P, true))) break;
+      {
+        const float* bias = reinterpret_cast<const float*>(W + ((lc - 1) & 1) * sh.wbuf + 9 * Cfg::chunks * 256);
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+          const int j = wg + WG * k;
+          if (j >= sh.ntiles) break;
           float v[16];
-          tmem_ld_16cols(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * j), v);
-          const int m = j * 128 + threadIdx.x, a = m / NP, p = m % NP, py = p / Lp, px = p % Lp;
-          if (a < s_here && py >= 1 && py <= L && px >= 1 && px <= L) {
+          tmem_ld_16cols(tmem + tmem_lane + (uint32_t)(16 * j), v);
+          const RowPos rp = unpack_pos(pos[k]);
+          if (!rp.live) continue;
 #pragma unroll
-            for (int o = 0; o < kCh; ++o) put<KIND>(Q, sh.rows_tot, kGuard + m, o, gelu_tanh(v[o] + bias[o]));
+          for (int c = 0; c < 16; ++c) v[c] = gelu_op<KIND>(v[c] + bias[c]);
+          put_row<KIND>(Q, sh, rp, v);
+        }
+      }
+      // conv2: x += conv(Q) + b2; then the next block's P = gelu(x / sqrt(b + 2))
+      if (!(ok = conv(Q, b + 1 < sh.B || next_group))) break;
+      {
+        const float* bias = reinterpret_cast<const float*>(W + ((lc - 1) & 1) * sh.wbuf + 9 * Cfg::chunks * 256);
+        const float scale = rsqrtf((float)(b + 2));
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+          const int j = wg + WG * k;
+          if (j >= sh.ntiles) break;
+          float v[16];
+          tmem_ld_16cols(tmem + tmem_lane + (uint32_t)(16 * j), v);
+          const RowPos rp = unpack_pos(pos[k]);
+          if (!rp.live) continue;
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            x[k][c] += v[c] + bias[c];
+            v[c] = gelu_op<KIND>(x[k][c] * scale);
           }
-        }
-        tc_fence_before();
-        __syncthreads();
-        fill_halo<KIND>(Q, sh, halo, s_here);
-      }
-      // conv2 on the tensor cores, x += acc + b2
-      stage_weights<KIND>(W, bias, table + layer_offset(2 * b + 1, sh.C), sh.C);
-      if (!conv_tc(Q)) break;
-      for (int j = 0; j < sh.ntiles; ++j) {
-        float v[16];
-        tmem_ld_16cols(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * j), v);
-        const int m = j * 128 + threadIdx.x, a = m / NP, p = m % NP, py = p / Lp, px = p % Lp;
-        if (a < s_here && py >= 1 && py <= L && px >= 1 && px <= L) {
-          const int r = (py - 1) * L + (px - 1);
-#pragma unroll
-          for (int o = 0; o < kCh; ++o) X[(a * kCh + o) * N + r] += v[o] + bias[o];
+          if (b + 1 < sh.B) put_row<KIND>(P, sh, rp, v);
         }
       }
-      tc_fence_before();
-      __syncthreads();
     }
-    if (fail) break;
-    // log sum exp over (channel, site) per sample, one warp per sample
+    if (!ok) break;
+    // log sum exp over (channel, site) per sample: z = x / sqrt(B + 1) of the C channels
+    // is gathered in shared memory (over P and Q, free now), one warp per sample
+    float* Z = reinterpret_cast<float*>(P);
+    __syncthreads();
     const float fs = rsqrtf((float)(sh.B + 1));
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const RowPos rp = unpack_pos(pos[k]);
+      if (!rp.live) continue;
+      const int r = (rp.py - 1) * L + (rp.px - 1);
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c < sh.C) Z[(rp.a * sh.C + c) * N + r] = x[k][c] * fs;
+    }
+    __syncthreads();
     const int cp = sh.cplx ? sh.C / 2 : sh.C;
-    for (int a = warp; a < s_here; a += kThreadsTc / 32) {
-      const float* xa = X + a * kCh * N;
+    for (int a = warp; a < s_here; a += kThreads / 32) {
+      const float* za = Z + a * sh.C * N;
       float mx = -INFINITY;
-      for (int e = lane; e < cp * N; e += 32) mx = fmaxf(mx, xa[e] * fs);
+      for (int e = lane; e < cp * N; e += 32) mx = fmaxf(mx, za[e]);
       mx = warp_max(mx);
       float sr = 0.0f, si = 0.0f;
       for (int e = lane; e < cp * N; e += 32) {
-        const float ex = expf(xa[e] * fs - mx);
+        const float ex = expf(za[e] - mx);
         float sn = 0.0f, cs = 1.0f;
-        if (sh.cplx) sincosf(xa[cp * N + e] * fs, &sn, &cs);
+        if (sh.cplx) sincosf(za[cp * N + e], &sn, &cs);
         sr = fmaf(ex, cs, sr);
         si = fmaf(ex, sn, si);
       }
@@ -370,8 +419,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       if (lane == 0)
         out[base + a] = make_float2(mx + 0.5f * logf(sr * sr + si * si) - logf((float)(cp * N)), atan2f(si, sr));
     }
+    __syncthreads();  // Z is overwritten by the next group's P
   }
-  if (fail && threadIdx.x == 0 && status) atomicExch(status, QGX_ERR_TIMEOUT);
+  if (base < total) {
+    // a wait timed out: this CTA's remaining outputs become NaN, so the failure shows in
+    // every energy and update computed from them
+    for (int64_t b2 = base; b2 < total; b2 += (int64_t)gridDim.x * S)
+      for (int a = tid; a < S && b2 + a < total; a += blockDim.x) out[b2 + a] = make_float2(NAN, NAN);
+    if (tid == 0 && w_issued > w_done) {
+      // a weight copy may still be in flight: give it the bounded wait before the CTA exits
+      mbar_wait(wbar + (w_done & 1), (w_done >> 1) & 1);
+    }
+  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -380,25 +439,80 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   }
 }
 
+// weight images for the tensor-core kernels from the FP32 table slices
+__global__ void rc_tc_image_kernel(float* __restrict__ table, int B, int C) {
+  uint8_t* tb = reinterpret_cast<uint8_t*>(table);
+  uint8_t* img_bf = tb + tc_image_offset(B, C, 1);
+  uint8_t* img_tf = tb + tc_image_offset(B, C, 0);
+  const int lb_bf = (int)tc_layer_bytes(2), lb_tf = (int)tc_layer_bytes(4);
+  const int per_layer = 9 * kCh * kCh + kCh;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)2 * B * per_layer;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(e / per_layer), rem = (int)(e % per_layer);
+    const int cin = layer_cin(l, C);
+    const float* tl = table + layer_offset(l, C);
+    if (rem >= 9 * kCh * kCh) {
+      const int o = rem - 9 * kCh * kCh;
+      const float bv = o < C ? tl[cin * 9 * C + o] : 0.0f;
+      reinterpret_cast<float*>(img_bf + (size_t)l * lb_bf + 9 * 2 * 256)[o] = bv;
+      reinterpret_cast<float*>(img_tf + (size_t)l * lb_tf + 9 * 4 * 256)[o] = bv;
+      continue;
+    }
+    const int tap = rem / (kCh * kCh), i = (rem / kCh) % kCh, o = rem % kCh;
+    const float w = (i < cin && o < C) ? tl[(i * 9 + tap) * C + o] : 0.0f;
+    // [tap][chunk][o][e]: chunk = i / (elements per chunk), e = i % (elements per chunk)
+    *reinterpret_cast<__nv_bfloat16*>(img_bf + (size_t)l * lb_bf + ((tap * 2 + i / 8) * kCh + o) * 16 + (i % 8) * 2) =
+        __float2bfloat16_rn(w);
+    *reinterpret_cast<float*>(img_tf + (size_t)l * lb_tf + ((tap * 4 + i / 4) * kCh + o) * 16 + (i % 4) * 4) =
+        to_tf32(w);
+  }
+}
+
+}  // namespace
+
+int rc_prepare_tc_images(float* table, int B, int C, cudaStream_t st) {
+  rc_tc_image_kernel<<<16, 256, 0, st>>>(table, B, C);
+  return launch_status();
+}
+
+namespace {
+
+template <int KIND, int WG, int RPT, int MINB>
+int launch_tc_variant(const uint8_t* wimg, const TcShape& sh, const uint32_t* cfg, int64_t ncfg,
+                      const int64_t* n_live, float2* out, cudaStream_t st) {
+  auto k = rc_forward_tc_kernel<KIND, WG, RPT, MINB>;
+  // MINB CTAs per SM: the launch bounds cap the registers for it, the shape's shared memory
+  // and TMEM columns were checked against it; the dynamic shared memory requested is raised
+  // so that no more than MINB CTAs (and their TMEM allocations) share an SM
+  const int smem = std::max(sh.smem, std::min(device_max_smem_optin(), (227 * 1024) / (MINB + 1) + 1024));
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  const int64_t want = (ncfg + sh.S - 1) / sh.S;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)device_sm_count() * MINB, want));
+  k<<<grid, 128 * WG, smem, st>>>(wimg, sh, cfg, ncfg, n_live, out);
+  return launch_status();
+}
+
+template <int KIND>
+int launch_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,
+              const int64_t* n_live, float2* out, cudaStream_t st) {
+  using T = TcLaunch<KIND>;
+  constexpr int tiles = T::WG * T::RPT;
+  if ((L + 2) * (L + 2) > tiles * 128) return QGX_ERR_UNSUPPORTED;
+  const TcShape sh = tc_shape(L, B, C, cplx, TcCfg<KIND>::esz, tc_samples_per_cta(L, tiles));
+  if (sh.ntiles > tiles || sh.smem * T::CTAS > 227 * 1024 || sh.smem > device_max_smem_optin() ||
+      sh.tmem_cols * T::CTAS > 512)
+    return QGX_ERR_UNSUPPORTED;
+  const uint8_t* wimg = reinterpret_cast<const uint8_t*>(table) + tc_image_offset(B, C, KIND);
+  return launch_tc_variant<KIND, T::WG, T::RPT, T::CTAS>(wimg, sh, cfg, ncfg, n_live, out, st);
+}
+
 }  // namespace
 
 int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,
                          const int64_t* n_live, float2* out, int kind, cudaStream_t st) {
-  if (C < 1 || C > kCh || L < 3 || L + 3 > kGuard || (L + 2) * (L + 2) > 1152) return QGX_ERR_UNSUPPORTED;
-  const TcShape sh = tc_shape(L, B, C, cplx, kind == 1 ? 2 : 4, tc_samples_per_cta(L));
-  if (sh.smem > device_max_smem_optin() || sh.tmem_cols > 512) return QGX_ERR_UNSUPPORTED;
-  const int64_t want = (ncfg + sh.S - 1) / sh.S;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(device_sm_count(), want));
-  if (kind == 1) {
-    auto k = rc_forward_tc_kernel<1>;
-    QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
-    k<<<grid, kThreadsTc, sh.smem, st>>>(table, sh, cfg, ncfg, n_live, out, nullptr);
-  } else {
-    auto k = rc_forward_tc_kernel<0>;
-    QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
-    k<<<grid, kThreadsTc, sh.smem, st>>>(table, sh, cfg, ncfg, n_live, out, nullptr);
-  }
-  return launch_status();
+  if (C < 1 || C > kCh || L < 3 || L + 3 > kGuard) return QGX_ERR_UNSUPPORTED;
+  if (kind == 1) return launch_tc<1>(table, L, B, C, cplx, cfg, ncfg, n_live, out, st);
+  return launch_tc<0>(table, L, B, C, cplx, cfg, ncfg, n_live, out, st);
 }
 
 }  // namespace qgx

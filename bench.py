@@ -250,7 +250,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
         phases["cusolver_and_projection"] = phases.pop("solve")
     energies = [float(x[0]) for x in stats]
     out = dict(elapsed=elapsed, lat=lat, phases=phases, energies=energies, launches=launches, clocks=clk,
-               nparams=state.nparams)
+               nparams=state.nparams, fallbacks=opt.solve_fallbacks)
 
     if e2e:
         # end to end through the public API with host buffers: parameters in from pinned host
@@ -300,15 +300,65 @@ def run_serving(args, rank):
     if rank == 0:
         line = {"metric": METRIC, "value": steps / out["wall_s"], "unit": UNIT, "n_gpus": 1, "steps": steps,
                 "warmup": 0, "ms_per_step": 1000.0 * out["wall_s"] / steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 solve)", "data": "synthetic",
+                "scaling": "weak", "vs_baseline": None, "dtype": "bf16 conv / bf16 Gram / FP64 solve",
+                "data": "synthetic",
                 "config": {"workload": f"serving: {args.jobs} Poisson jobs x {args.job_steps} SR steps "
-                                       "(config-5 mixture)", "max_active": 8},
+                                       "(config-5 mixture)", "max_active": 8, "conv": specs[0].conv,
+                           "gram": specs[0].gram, "solve": specs[0].solve},
                 "jobs_per_s": out["jobs_per_s"], "samples_per_s": out["samples_per_s"],
                 "p50_step_ms": out["p50_step_ms"], "p99_step_ms": out["p99_step_ms"], "wall_s": out["wall_s"],
                 "jobs": [{"name": j["name"], "final_energy": j["energies"][-1],
                           "mean_step_ms": sum(j["latencies_ms"]) / len(j["latencies_ms"])} for j in out["jobs"]],
                 "clocks": clk}
         print(json.dumps(line), flush=True)
+
+
+def run_trajectory(args, rank):
+    """Energy trajectories of the plain path and the precision forms from identical initial
+    parameters and seeds: J1-J2 (J2 = 0.5, MSR) on the 10x10 square, ResConv(8 blocks, 16
+    channels, complex output), SpinExchange with 200 proposals per sweep, MinSR with diagonal
+    shift 1e-4, learning rate 1e-2. The chain count is reduced from 16384 to --chains (the
+    FP64 plain path factorises a 2Ns x 2Ns matrix every step). Reports every form's energies,
+    the mean and standard error over the last quarter, and the relative difference of that
+    mean to the plain path's."""
+    import numpy as np
+    import torch
+    import quantax_gb300 as qtx
+    forms = [tuple(f.split(":")) for f in args.forms.split(",")]
+    out = {}
+    for name, conv, gram, solve in forms:
+        qtx.set_random_seed(4321)
+        qtx.set_default_dtype(np.complex128)
+        qtx.sites.Square(10, Nparticles=(50, 50))
+        H = qtx.operator.Heisenberg(J=[1.0, 0.5], n_neighbor=[1, 2], msr=True)
+        state = qtx.state.Variational(qtx.model.ResConv(8, 16, out_dtype=np.complex64, conv_precision=conv))
+        sampler = qtx.sampler.SpinExchange(state, args.chains, thermal_steps=200, sweep_steps=200)
+        opt = qtx.optimizer.SR(state, H, solver=qtx.optimizer.minnorm_shift_eig(ashift=1e-4, precision=solve),
+                               gram=gram)
+        stats = []
+        skipped = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step = opt.get_step(sampler.sweep())
+            skipped += int(not bool(torch.isfinite(step).all()))
+            state.update(step * 1e-2)
+            stats.append(opt.stats.clone())
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        e = np.array([float(x[0]) for x in stats])
+        tail = e[-max(1, len(e) // 4):]
+        out[name] = {"conv": conv, "gram": gram, "solve": solve, "s_per_step": wall / len(e),
+                     "fp64_fallbacks": opt.solve_fallbacks, "nonfinite_steps": skipped,
+                     "energies": [round(float(v), 6) for v in e], "tail_mean": float(tail.mean()),
+                     "tail_stderr": float(tail.std(ddof=1) / np.sqrt(len(tail))) if len(tail) > 1 else None}
+        qtx.set_default_dtype(np.float64)
+    ref = out[forms[0][0]]["tail_mean"]
+    for name in out:
+        out[name]["tail_rel_diff_vs_plain"] = abs(out[name]["tail_mean"] - ref) / abs(ref)
+    if rank == 0:
+        print(json.dumps({"workload": "trajectory: J1-J2 10x10, ResConv(8, 16) complex, MinSR shift 1e-4",
+                          "chains": args.chains, "steps": args.steps, "forms": out}), flush=True)
 
 
 def percentile(lat, q):
@@ -326,10 +376,14 @@ def main():
     ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
-    ap.add_argument("--workload", default="rbm", choices=["rbm", "resconv", "serving"],
+    ap.add_argument("--workload", default="rbm", choices=["rbm", "resconv", "serving", "trajectory"],
                     help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv); "
                          "serving: a Poisson stream of config-5 jobs through quantax_gb300.serving")
     ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
+    ap.add_argument("--chains", type=int, default=2048, help="trajectory: Markov chains (samples per step)")
+    ap.add_argument("--forms", default="plain:fp32:fp32:fp64,precision_bf16:bf16:bf16:mixed,"
+                                       "precision_tf32:tf32:tf32:mixed",
+                    help="trajectory: comma-separated name:conv:gram:solve; the first is the reference run")
     ap.add_argument("--job-steps", type=int, default=5, help="serving: SR steps per job")
     args = ap.parse_args()
 
@@ -352,6 +406,9 @@ def main():
     if args.workload == "serving":
         run_serving(args, rank)
         return
+    if args.workload == "trajectory":
+        run_trajectory(args, rank)
+        return
 
     plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)
     forms = {}
@@ -373,6 +430,7 @@ def main():
                 "p50_step_ms": percentile(prec["lat"], 0.5), "p99_step_ms": percentile(prec["lat"], 0.99),
                 "phases_ms": {k: round(v, 4) for k, v in prec["phases"].items()},
                 "speedup_vs_plain": plain["elapsed"] / prec["elapsed"],
+                "fp64_fallbacks": prec["fallbacks"],
                 "energy_rel_diff_vs_plain_max": max(de), "energy_rel_diff_vs_plain_last": de[-1]}
 
     if rank == 0:

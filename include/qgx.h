@@ -42,9 +42,11 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
 
 #define QGX_SOLVE_SHIFT 0  /* diagonal-shifted Cholesky (minnorm_shift_eig) */
 #define QGX_SOLVE_PINV 1   /* soft pseudo-inverse via eigh (minnorm_pinv_eig) */
-/* diagonal-shifted system solved with an FP32 Cholesky factor and FP64 iterative
- * refinement against the FP64 matrix (residuals in FP64); info = -1 when the refined
- * residual stays above 1e-12 relative (the caller then falls back to QGX_SOLVE_SHIFT) */
+/* diagonal-shifted system solved by FP64 conjugate gradients preconditioned with the FP32
+ * Cholesky factor of the shifted matrix (cuSOLVER, BF16x9-emulated FP32); when that factor
+ * breaks down it is recomputed once with 4 sqrt(n) 2^-24 tr(T) more on the diagonal.
+ * info = -1 when the true FP64 residual stays above 1e-10 relative after 100 iterations
+ * (the caller then falls back to QGX_SOLVE_SHIFT) */
 #define QGX_SOLVE_SHIFT_MIXED 2
 
 #define QGX_GRAM_FP32 0    /* FP32 SIMT FMA, FP32 accumulation */
@@ -268,13 +270,20 @@ int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* by
 /* MinSR branch: given T = A A^T (n x n FP64, overwritten), b (n), A (n x np FP32):
  *   SHIFT: (T + (rshift tr T + ashift) I) y = b by Cholesky, x = A^T y
  *   PINV:  T = U diag(l) U^T, x = A^T U diag(l+) rho, rho = sum_without_noise(U^T o b)
- *   SHIFT_MIXED: as SHIFT, factor in FP32, refined in FP64 (see QGX_SOLVE_SHIFT_MIXED)
- * x (np doubles). info (device int, may be NULL) receives the cuSOLVER info (-1: the
- * mixed-precision refinement did not converge). */
+ *   SHIFT_MIXED: as SHIFT; FP64 conjugate gradients preconditioned by the FP32 Cholesky factor
+ *                (see QGX_SOLVE_SHIFT_MIXED); synchronises the stream with the host
+ * x (np doubles). info (device int, may be NULL) receives the cuSOLVER info: > 0 the
+ * shifted matrix is not positive definite at that leading minor (x is then NaN, like the
+ * reference's Cholesky solve); -1 the mixed-precision refinement did not converge (x holds
+ * the last iterate; factor the shifted T, still in place, with SHIFT and zero shifts). */
 int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t lda,
                     const double* b, int32_t method, double rshift, double ashift,
                     double rtol, double atol, double tol_snr, double* x, int32_t* info,
                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+/* Number of qgx kernels the last qgx_minsr_solve / qgx_sr_solve call of this host thread
+ * launched (library kernels such as cuSOLVER's not counted; SHIFT_MIXED varies with its
+ * iteration count). */
+int64_t qgx_last_solve_kernels(void);
 /* SR branch: given S = A^T A (np x np FP64, overwritten): x = S^-1 A^T b with the same
  * two regularisations (lstsq_shift_eig / lstsq_pinv_eig). */
 int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda,

@@ -93,6 +93,7 @@ SIGNATURES = {
     "qgx_f32_to_bf16": (C.c_int, [vp, i64, i64, i64, vp, i64, vp]),
     "qgx_solve_workspace_bytes": (C.c_int, [i64, i64, i32, C.POINTER(i64)]),
     "qgx_minsr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
+    "qgx_last_solve_kernels": (i64, []),
     "qgx_sr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_apply_update": (C.c_int, [vp, vp, i64, vp, vp]),
 }
@@ -119,12 +120,10 @@ launch_count = 0
 
 
 def _kernels(name, args):
-    if name == "qgx_minsr_solve":
-        return {SOLVE_SHIFT: 3, SOLVE_PINV: 6, SOLVE_SHIFT_MIXED: 36}[args[6]]
+    if name in ("qgx_minsr_solve", "qgx_sr_solve"):
+        return int(lib().qgx_last_solve_kernels())
     if name == "qgx_resconv_sweep":
         return 1 + 3 * int(args[10])
-    if name == "qgx_sr_solve":
-        return 3 if args[6] == SOLVE_SHIFT else 6
     return KERNELS_PER_CALL.get(name, 0)
 
 

@@ -1,14 +1,19 @@
 // Tensor-core Gram matrix T = A A^T on sm_103a with tcgen05 (quantax/optimizer/solver.py:139).
 //
 // One CTA computes one 128 x 128 tile of T on or below the diagonal:
-//   warp 1 / lane 0  TMA producer: 128 x 128-byte K-major tiles of the row block and of the
+//   warp 4 / lane 0  TMA producer: 128 x 128-byte K-major tiles of the row block and of the
 //                    column block, 128B-swizzled, into a ring of kStages shared-memory stages;
-//   warp 2 / lane 0  MMA issuer: tcgen05.mma M=128 N=128 (K = 8 for tf32, 16 for bf16; four
-//                    per 128-byte k-block), accumulator in 128 TMEM columns, tcgen05.commit
-//                    frees a stage when its MMAs are done;
-//   all 4 warps      epilogue: tcgen05.ld of the accumulator (warp w owns TMEM lanes
-//                    32w..32w+31, i.e. tile rows), FP64 stores of the tile and its mirror,
-//                    both coalesced (the direct tile goes through a shared-memory transpose).
+//   warp 5 / lane 0  MMA issuer: tcgen05.mma M=128 N=128 (K = 8 for tf32, 16 for bf16; four
+//                    per 128-byte k-block); tcgen05.commit frees a stage when its MMAs are done;
+//   warps 6-9        (split tf32 only) split the staged operands into hi and lo parts;
+//   warps 0-3        epilogue (warp w owns TMEM lanes 32w..32w+31, i.e. tile rows).
+// K is accumulated in chunks of kChunkElems elements, alternately in two 128-column TMEM
+// accumulators, each chunk starting from zero. The epilogue adds every finished chunk into
+// FP32 registers (round to nearest) while the next chunk is computed, then stores the tile and
+// its mirror in FP64, both coalesced (the direct tile goes through a shared-memory transpose).
+// The tensor core's FP32 accumulation of one long K loses up to ~k 2^-25 relative with a
+// systematic sign; with chunks that bias is bounded by the chunk length, and the rounding of
+// the chunk sums is unbiased: T stays accurate enough for a diagonal shift of 1e-6 tr(T).
 // Every mbarrier wait is bounded by a wall-clock limit; a wait that runs out records
 // QGX_ERR_TIMEOUT in the optional status word, the CTA releases its TMEM and returns.
 #include <cuda.h>
@@ -27,14 +32,17 @@ constexpr int kTile = 128;          // rows / columns of a T tile
 constexpr int kRowBytes = 128;      // bytes of one operand row per k-block (one swizzle atom)
 constexpr int kBlockBytes = kTile * kRowBytes;  // one operand block of a stage
 // KIND 0: tf32, 1: bf16, 2: split tf32 (hi*hi + hi*lo + lo*hi, FP32-class accuracy)
+constexpr int kChunkElems = 256;  // K elements accumulated in TMEM before the epilogue takes them
 template <int KIND>
 struct GramCfg {
   static constexpr int kStageBytes = (KIND == 2 ? 4 : 2) * kBlockBytes;  // A, B (+ A lo, B lo)
-  static constexpr int kStages = KIND == 2 ? 3 : 3;
-  static constexpr int kThreads = KIND == 2 ? 256 : 128;  // KIND 2: warps 4..7 split the operands
+  static constexpr int kStages = 3;
+  static constexpr int kThreads = KIND == 2 ? 320 : 192;  // epilogue 0-3, producer 4, MMA 5, split 6-9
   static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 256;
+  static constexpr int kElems = KIND == 1 ? 64 : 32;      // elements per 128-byte k-block
+  static constexpr int kChunkBlocks = kChunkElems / kElems;
 };
-constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kTmemCols = 256;  // two chunk accumulators
 
 // K-major operand tile, 128-byte rows, 128B swizzle: 8-row core groups 1024 bytes apart
 __device__ inline uint64_t smem_desc_sw128(uint32_t saddr) {
@@ -86,9 +94,10 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
   uint64_t* empty = full + kStages;
   uint64_t* split = empty + kStages;  // KIND 2: operands split into hi / lo
-  uint64_t* done = split + kStages;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-  int* fail = reinterpret_cast<int*>(tmem_slot + 1);
+  uint64_t* acc_full = split + kStages;   // two: a chunk accumulator is complete
+  uint64_t* acc_empty = acc_full + 2;     // two: the epilogue has taken a chunk accumulator
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   // lower-triangular tile index -> (bi, bj), bi >= bj
   const int64_t tile = blockIdx.x;
@@ -105,7 +114,10 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
       mbar_init(&empty[s], 1);
       mbar_init(&split[s], 128);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+    }
     *fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -120,54 +132,69 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  constexpr int kElems = KIND == 1 ? 64 : 32;  // elements per 128-byte k-block
+  constexpr int kElems = Cfg::kElems;
+  constexpr int kChunkBlocks = Cfg::kChunkBlocks;
+  const int64_t nchunk = (nkb + kChunkBlocks - 1) / kChunkBlocks;
 
-  if (warp == 1 && lane == 0) {
-    for (int64_t kb = 0; kb < nkb; ++kb) {
-      const int s = (int)(kb % kStages);
-      const uint32_t ph = (uint32_t)((kb / kStages) & 1);
-      if (!mbar_wait(&empty[s], ph ^ 1u)) {
-        *fail = 1;
-        break;
-      }
-      uint8_t* a = smem + s * kStageBytes;
-      uint8_t* b = a + kBlockBytes;
-      mbar_expect_tx(&full[s], 2 * kBlockBytes);
-      tma_load_2d(a, &tmap, &full[s], (int)(kb * kElems), row0);
-      tma_load_2d(b, &tmap, &full[s], (int)(kb * kElems), col0);
-    }
-  } else if (warp == 2 && lane == 0) {
-    for (int64_t kb = 0; kb < nkb; ++kb) {
-      const int s = (int)(kb % kStages);
-      const uint32_t ph = (uint32_t)((kb / kStages) & 1);
-      if (!mbar_wait(KIND == 2 ? &split[s] : &full[s], ph)) {
-        *fail = 1;
-        break;
-      }
-      tc_fence_after();
-      const uint32_t base = smem_u32(smem + s * kStageBytes);
-      const uint64_t da = smem_desc_sw128(base);
-      const uint64_t db = smem_desc_sw128(base + kBlockBytes);
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk)  // 32 bytes of K per instruction
-        mma<KIND>(tmem, da + 2 * kk, db + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
-      if (KIND == 2) {
-        const uint64_t la = smem_desc_sw128(base + 2 * kBlockBytes);
-        const uint64_t lb = smem_desc_sw128(base + 3 * kBlockBytes);
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          mma<KIND>(tmem, da + 2 * kk, lb + 2 * kk, 1u);
-          mma<KIND>(tmem, la + 2 * kk, db + 2 * kk, 1u);
+  if (warp == 4) {
+    if (lane == 0) {
+      for (int64_t kb = 0; kb < nkb && !*fail; ++kb) {
+        const int s = (int)(kb % kStages);
+        const uint32_t ph = (uint32_t)((kb / kStages) & 1);
+        if (!mbar_wait(&empty[s], ph ^ 1u)) {
+          *fail = 1;
+          break;
         }
+        uint8_t* a = smem + s * kStageBytes;
+        uint8_t* b = a + kBlockBytes;
+        mbar_expect_tx(&full[s], 2 * kBlockBytes);
+        tma_load_2d(a, &tmap, &full[s], (int)(kb * kElems), row0);
+        tma_load_2d(b, &tmap, &full[s], (int)(kb * kElems), col0);
       }
-      mma_commit(&empty[s]);
     }
-    mma_commit(done);
-  } else if (KIND == 2 && warp >= 4) {
+  } else if (warp == 5) {
+    if (lane == 0) {
+      for (int64_t kb = 0; kb < nkb && !*fail; ++kb) {
+        const int64_t c = kb / kChunkBlocks;
+        const bool first = kb % kChunkBlocks == 0;
+        const bool last = kb % kChunkBlocks == kChunkBlocks - 1 || kb == nkb - 1;
+        const uint32_t acc = tmem + (uint32_t)(128 * (c & 1));
+        // the accumulator of chunk c - 2 must have been taken by the epilogue
+        if (first && c >= 2 && !mbar_wait(&acc_empty[c & 1], (uint32_t)((c >> 1) - 1) & 1)) {
+          *fail = 1;
+          break;
+        }
+        const int s = (int)(kb % kStages);
+        const uint32_t ph = (uint32_t)((kb / kStages) & 1);
+        if (!mbar_wait(KIND == 2 ? &split[s] : &full[s], ph)) {
+          *fail = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t base = smem_u32(smem + s * kStageBytes);
+        const uint64_t da = smem_desc_sw128(base);
+        const uint64_t db = smem_desc_sw128(base + kBlockBytes);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)  // 32 bytes of K per instruction
+          mma<KIND>(acc, da + 2 * kk, db + 2 * kk, (first && kk == 0) ? 0u : 1u);
+        if (KIND == 2) {
+          const uint64_t la = smem_desc_sw128(base + 2 * kBlockBytes);
+          const uint64_t lb = smem_desc_sw128(base + 3 * kBlockBytes);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            mma<KIND>(acc, da + 2 * kk, lb + 2 * kk, 1u);
+            mma<KIND>(acc, la + 2 * kk, db + 2 * kk, 1u);
+          }
+        }
+        mma_commit(&empty[s]);
+        if (last) mma_commit(&acc_full[c & 1]);
+      }
+    }
+  } else if (KIND == 2 && warp >= 6) {
     // split x = hi + lo: hi keeps the 10 explicit mantissa bits the tensor core reads
     // (written in place), lo = x - hi exactly (second buffer, same swizzled layout)
-    const int t = threadIdx.x - 128;
-    for (int64_t kb = 0; kb < nkb; ++kb) {
+    const int t = threadIdx.x - 192;
+    for (int64_t kb = 0; kb < nkb && !*fail; ++kb) {
       const int s = (int)(kb % kStages);
       const uint32_t ph = (uint32_t)((kb / kStages) & 1);
       if (!mbar_wait(&full[s], ph)) {
@@ -192,32 +219,50 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
     }
   }
 
-  // epilogue: warps 0..3 (KIND 0/1) or 4..7 (KIND 2) read TMEM lanes 32 (warp % 4) ...
-  if (!mbar_wait(done, 0)) *fail = 1;
-  __syncthreads();
-  const bool epi = KIND == 2 ? warp >= 4 : true;
+  // epilogue warps 0..3: take every chunk accumulator into the running sums
+  float sum[kTile];
+#pragma unroll
+  for (int j = 0; j < kTile; ++j) sum[j] = 0.0f;
+  const int q = warp & 3;
+  if (warp < 4) {
+    for (int64_t c = 0; c < nchunk; ++c) {
+      if (*fail || !mbar_wait(&acc_full[c & 1], (uint32_t)(c >> 1) & 1)) {
+        *fail = 1;
+        break;
+      }
+      tc_fence_after();
+#pragma unroll
+      for (int g = 0; g < kTile / 32; ++g) {
+        float v[32];
+        tmem_ld_32cols(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(128 * (c & 1) + 32 * g), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sum[32 * g + j] += v[j];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[c & 1])) : "memory");
+    }
+  }
+  __syncthreads();  // every role has finished: the stage memory is free for the transpose
   if (*fail) {
     if (threadIdx.x == 0) record_status(status, QGX_ERR_TIMEOUT);
-  } else if (epi) {
-    tc_fence_after();
-    const int q = warp & 3;
-    float* tr = reinterpret_cast<float*>(smem) + q * 32 * 33;  // stage memory is free now
+  } else if (warp < 4) {
+    float* tr = reinterpret_cast<float*>(smem) + q * 32 * 33;
     const int r_local = 32 * q + lane;
-    for (int c = 0; c < kTile / 32; ++c) {
-      float v[32];
-      tmem_ld_32cols(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * c), v);
+#pragma unroll
+    for (int g = 0; g < kTile / 32; ++g) {
       // mirror: T[col][row], consecutive lanes -> consecutive rows of T's column
       const int64_t r = row0 + r_local;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const int64_t cc = col0 + 32 * c + j;
-        if (r < n && cc < n) T[cc * ldt + r] = (double)v[j];
+        const int64_t cc = col0 + 32 * g + j;
+        if (r < n && cc < n) T[cc * ldt + r] = (double)sum[32 * g + j];
       }
       if (bi != bj) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) tr[lane * 33 + j] = v[j];
+        for (int j = 0; j < 32; ++j) tr[lane * 33 + j] = sum[32 * g + j];
         __syncwarp();
-        const int64_t cc = col0 + 32 * c + lane;
+        const int64_t cc = col0 + 32 * g + lane;
         for (int j = 0; j < 32; ++j) {
           const int64_t rr = row0 + 32 * q + j;
           if (rr < n && cc < n) T[rr * ldt + cc] = (double)tr[j * 33 + lane];

@@ -55,7 +55,10 @@ __global__ void shift_diag_kernel(double* __restrict__ T, int64_t n, int64_t ldt
   __syncthreads();
   const double shift = rshift * sh[0] + ashift;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) T[i * ldt + i] += shift;
-  if (threadIdx.x == 0 && shift_out) *shift_out = shift;
+  if (threadIdx.x == 0 && shift_out) {
+    shift_out[0] = shift;
+    shift_out[1] = sh[0];  // trace before the shift
+  }
 }
 
 // partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s] in FP64 (the reference forms
@@ -174,18 +177,130 @@ __global__ void uv_partial_kernel(const double* __restrict__ U, int64_t n, const
   part[blockIdx.y * n + t] = acc;
 }
 
-constexpr int kRefineIters = 10;
-constexpr double kRefineTol = 1e-12;
+// SHIFT_MIXED: preconditioned conjugate gradients in FP64 on (T + shift I) y = b, the
+// preconditioner being the FP32 Cholesky factor of the same matrix (or of T + shift' I with
+// a larger shift' when the FP32 factorisation breaks down)
+constexpr int kCgMaxIters = 100;
+constexpr double kCgTol = 1e-13;     // stop: recursive residual below this fraction of ||b||
+constexpr double kRefineTol = 1e-10;  // accept: true residual below this fraction of ||b||
+constexpr int kDotBlocks = 1024;      // fixed grid of the dot products: deterministic partial sums
+enum { kScalRZ = 0, kScalAlpha, kScalBeta, kScalRR, kScalBB, kScalCount };
 
-__global__ void to_f32_kernel(const double* __restrict__ in, int64_t count, float* __restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
+// FP32 copy of the shifted T, with `extra` added to the diagonal (the preconditioner's shift)
+__global__ void to_f32_kernel(const double* __restrict__ in, int64_t n, float* __restrict__ out,
+                              const double* __restrict__ extra) {
+  const double e = extra ? *extra : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / n;
+    out[i] = (float)(in[i] + (i - row * n == row ? e : 0.0));
+  }
+}
+
+// extra diagonal shift of the fallback preconditioner: 4 sqrt(n) 2^-24 tr(T), the size of an
+// FP32 Cholesky's backward error for a matrix whose largest eigenvalue is at most tr(T)
+__global__ void precond_shift_kernel(const double* __restrict__ shift_trace, int64_t n, double* __restrict__ extra) {
+  *extra = 4.0 * sqrt((double)n) * 5.9604644775390625e-8 * shift_trace[1];
+}
+
+__device__ inline void block_partial(double v, double* __restrict__ part) {
+  __shared__ double sh[32];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+  }
+}
+
+// q = T p (warp per row, T symmetric row-major); block partials of p . q
+__global__ void symv_dot_kernel(const double* __restrict__ T, int64_t n, const double* __restrict__ p,
+                                double* __restrict__ q, double* __restrict__ part) {
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  double pq = 0.0;
+  if (row < n) {
+    const double* t = T + row * n;
+    double s = 0.0;
+    for (int64_t j = lane; j < n; j += 32) s = fma(t[j], p[j], s);
+    s = warp_sum(s);
+    if (lane == 0) {
+      q[row] = s;
+      pq = p[row] * s;
+    }
+  }
+  block_partial(pq, part);
+}
+
+// block partials of a . b (b FP64 or FP32), fixed grid
+template <typename TB>
+__global__ void dot_kernel(const double* __restrict__ a, const TB* __restrict__ b, int64_t n, double* __restrict__ part) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s = fma(a[i], (double)b[i], s);
+  block_partial(s, part);
+}
+
+// sum of the partials in a fixed order, then one scalar step of the iteration:
+// 0 rz = s; 1 alpha = rz / s; 2 rr = s; 3 beta = s / rz, rz = s; 4 bb = s
+__global__ void reduce_step_kernel(const double* __restrict__ part, int np, double* __restrict__ scal, int mode) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  __shared__ double sh[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    if (mode == 0) scal[kScalRZ] = t;
+    if (mode == 1) scal[kScalAlpha] = scal[kScalRZ] / t;
+    if (mode == 2) scal[kScalRR] = t;
+    if (mode == 3) {
+      scal[kScalBeta] = t / scal[kScalRZ];
+      scal[kScalRZ] = t;
+    }
+    if (mode == 4) scal[kScalBB] = t;
+  }
+}
+
+// y += alpha p, r -= alpha q, r32 = r (the preconditioner's right-hand side); partials of r . r
+__global__ void cg_update_kernel(double* __restrict__ y, double* __restrict__ r, const double* __restrict__ p,
+                                 const double* __restrict__ q, float* __restrict__ r32, int64_t n,
+                                 const double* __restrict__ scal, double* __restrict__ part) {
+  const double alpha = scal[kScalAlpha];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    y[i] = fma(alpha, p[i], y[i]);
+    const double v = fma(-alpha, q[i], r[i]);
+    r[i] = v;
+    r32[i] = (float)v;
+    s = fma(v, v, s);
+  }
+  block_partial(s, part);
+}
+
+// p = z + beta p (beta = 0: p = z)
+__global__ void cg_direction_kernel(double* __restrict__ p, const float* __restrict__ z, int64_t n,
+                                    const double* __restrict__ scal, int first) {
+  const double beta = first ? 0.0 : scal[kScalBeta];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = first ? (double)z[i] : fma(beta, p[i], (double)z[i]);
+}
+
+__global__ void cg_init_kernel(double* __restrict__ y, double* __restrict__ r, float* __restrict__ r32,
+                               const double* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    y[i] = 0.0;
+    r[i] = b[i];
+    r32[i] = (float)b[i];
+  }
 }
 
 // r = b - T y (FP64, T symmetric row-major n x n), warp per row; ||r||^2 and ||b||^2 into acc[0..1]
 __global__ void residual_kernel(const double* __restrict__ T, int64_t n, const double* __restrict__ y,
-                                const double* __restrict__ b, double* __restrict__ r, float* __restrict__ r32,
-                                double* __restrict__ acc) {
+                                const double* __restrict__ b, double* __restrict__ r, double* __restrict__ acc) {
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -196,15 +311,19 @@ __global__ void residual_kernel(const double* __restrict__ T, int64_t n, const d
   if (lane == 0) {
     const double v = b[row] - s;
     r[row] = v;
-    r32[row] = (float)v;
     atomicAdd(&acc[0], v * v);
     atomicAdd(&acc[1], b[row] * b[row]);
   }
 }
 
-__global__ void accumulate_kernel(double* __restrict__ y, const float* __restrict__ d, int64_t n) {
+__global__ void set_int_kernel(int* __restrict__ dst, int v) { *dst = v; }
+
+// a failed factorisation (info > 0) makes the solution NaN, as the reference's Cholesky solve
+// does, so the update is skipped instead of taking a step from a partial factor
+__global__ void nan_if_failed_kernel(double* __restrict__ y, int64_t n, const int* __restrict__ info) {
+  if (*info <= 0) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] += (double)d[i];
+    y[i] = __longlong_as_double(0x7FF8000000000000LL);
 }
 
 // info = the factorisation's info if it failed, else -1 when the final relative residual
@@ -225,12 +344,28 @@ struct SolveWs {
   double* v;      // n
   double* f;      // n  right-hand side of the SR branch (A^T b)
   double* part;   // nchunk * max(n, np)
-  double* shift;  // 1
-  int* info;      // 1
+  double* shift;  // 2: shift, trace
+  int* info;      // 2
   float* t32;     // n * n (SHIFT_MIXED)
   float* r32;     // n
   double* r;      // n
-  double* acc;    // 2 per refinement round
+  double* acc;    // 16: iteration scalars and residual norms
+};
+
+// The FP32 factorisation of SHIFT_MIXED runs with cuSOLVER's BF16x9 emulation of FP32
+// arithmetic on the tensor cores (measured on GB300 at n = 32768: 125 ms against 210 ms, the
+// same |L L^T - T| on sampled entries); the FP64 iteration and its residual check follow
+// unchanged. The mode is set around the FP32 calls only and the default restored after, so
+// the FP64 paths that share the handle are unaffected.
+struct Fp32EmulationScope {
+  cusolverDnHandle_t h;
+  bool on;
+  Fp32EmulationScope(cusolverDnHandle_t handle, bool enable) : h(handle), on(enable) {
+    if (on) cusolverDnSetMathMode(h, CUSOLVER_FP32_EMULATED_BF16X9_MATH);
+  }
+  ~Fp32EmulationScope() {
+    if (on) cusolverDnSetMathMode(h, CUSOLVER_DEFAULT_MATH);
+  }
 };
 
 int query_cusolver_bytes(int64_t n, int method, size_t* dev_bytes, size_t* host_bytes) {
@@ -243,6 +378,7 @@ int query_cusolver_bytes(int64_t n, int method, size_t* dev_bytes, size_t* host_
     s = cusolverDnXpotrf_bufferSize(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, nullptr, n, CUDA_R_64F, dev_bytes,
                                     host_bytes);
   } else if (method == QGX_SOLVE_SHIFT_MIXED) {
+    Fp32EmulationScope emu(h, true);
     s = cusolverDnXpotrf_bufferSize(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, nullptr, n, CUDA_R_32F, dev_bytes,
                                     host_bytes);
   } else {
@@ -271,13 +407,13 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   const int64_t o_v = take(n * 8);
   const int64_t o_f = take(n * 8);
   const int64_t o_part = take(nchunk * wide * 8);
-  const int64_t o_shift = take(8);
+  const int64_t o_shift = take(16);
   const int64_t o_info = take(8);
   const bool mixed = method == QGX_SOLVE_SHIFT_MIXED;
   const int64_t o_t32 = take(mixed ? n * n * 4 : 0);
   const int64_t o_r32 = take(mixed ? n * 4 : 0);
   const int64_t o_r = take(mixed ? n * 8 : 0);
-  const int64_t o_acc = take(mixed ? 2 * 8 * kRefineIters : 0);
+  const int64_t o_acc = take(mixed ? 16 * 8 : 0);
   *need = off;
   if (!base) return QGX_OK;
   if (bytes < off) return QGX_ERR_ARG;
@@ -300,14 +436,18 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   return QGX_OK;
 }
 
+thread_local int64_t g_kernels = 0;  // qgx kernels launched by the current solve call
+
 // x (ncol) = A^T y for A (nrow x ncol, lda)
 int project(const float* A, int64_t nrow, int64_t ncol, int64_t lda, const double* y, double* part, double* x,
             cudaStream_t st) {
   const int64_t nchunk = (nrow + kProjRows - 1) / kProjRows;
   if (nchunk > 65535) return QGX_ERR_UNSUPPORTED;
   const bool vec4 = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && (lda % 4 == 0);
+  ++g_kernels;
   project_partial_kernel<<<dim3((unsigned)((ncol + 1023) / 1024), (unsigned)nchunk), 256, 0, st>>>(
       A, nrow, ncol, lda, y, part, vec4);
+  ++g_kernels;
   sum_partials_kernel<<<(unsigned)((ncol + 255) / 256), 256, 0, st>>>(part, nchunk, ncol, x);
   return launch_status();
 }
@@ -323,52 +463,120 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
   int* dinfo = info ? info : ws.info;
   void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
   if (method == QGX_SOLVE_SHIFT) {
+    ++g_kernels;
     shift_diag_kernel<<<1, 1024, 0, st>>>(T, n, n, rshift, ashift, ws.shift);
     if ((rc = launch_status()) != QGX_OK) return rc;
     if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus, ws.cus_bytes, hws,
                          g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
       return QGX_ERR_SOLVER;
     QGX_CHECK_CUDA(cudaMemcpyAsync(ws.y, b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, dinfo) !=
+    // Xpotrs reports only argument errors; it writes its own word so that the factorisation's
+    // info (> 0: leading minor not positive definite) reaches the caller
+    if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, ws.info + 1) !=
         CUSOLVER_STATUS_SUCCESS)
       return QGX_ERR_SOLVER;
-    return QGX_OK;
+    ++g_kernels;
+    nan_if_failed_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, st>>>(ws.y, n, dinfo);
+    return launch_status();
   }
   if (method == QGX_SOLVE_SHIFT_MIXED) {
+    // host-synchronous: the factorisation's outcome and the convergence are read on the host
+    ++g_kernels;
     shift_diag_kernel<<<1, 1024, 0, st>>>(T, n, n, rshift, ashift, ws.shift);
     const unsigned g = (unsigned)std::min<int64_t>((n * n + 255) / 256, 8192);
-    to_f32_kernel<<<g, 256, 0, st>>>(T, n * n, ws.t32);
-    if ((rc = launch_status()) != QGX_OK) return rc;
-    if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.cus, ws.cus_bytes, hws,
-                         g_host_ws.size(), ws.info) != CUSOLVER_STATUS_SUCCESS)
-      return QGX_ERR_SOLVER;
-    // y = 0, r = b: the first round solves with the FP32 factor from the FP64 right-hand side
-    QGX_CHECK_CUDA(cudaMemsetAsync(ws.y, 0, n * sizeof(double), st));
-    QGX_CHECK_CUDA(cudaMemsetAsync(ws.acc, 0, 2 * kRefineIters * sizeof(double), st));
-    const unsigned gr = (unsigned)((n * 32 + 255) / 256);
-    const unsigned gv = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
-    for (int it = 0; it < kRefineIters; ++it) {
-      residual_kernel<<<gr, 256, 0, st>>>(T, n, ws.y, b, ws.r, ws.r32, ws.acc + 2 * it);
-      if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.r32, n,
-                           ws.info + 1) !=
-          CUSOLVER_STATUS_SUCCESS)
-        return QGX_ERR_SOLVER;
-      accumulate_kernel<<<gv, 256, 0, st>>>(ws.y, ws.r32, n);
+    double* extra = ws.acc + 8;
+    int hinfo = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      if (attempt == 1) {
+        ++g_kernels;
+        precond_shift_kernel<<<1, 1, 0, st>>>(ws.shift, n, extra);
+      }
+      ++g_kernels;
+      to_f32_kernel<<<g, 256, 0, st>>>(T, n, ws.t32, attempt == 1 ? extra : nullptr);
+      if ((rc = launch_status()) != QGX_OK) return rc;
+      {
+        Fp32EmulationScope emu(h, true);
+        if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.cus, ws.cus_bytes,
+                             hws, g_host_ws.size(), ws.info) != CUSOLVER_STATUS_SUCCESS)
+          return QGX_ERR_SOLVER;
+      }
+      QGX_CHECK_CUDA(cudaMemcpyAsync(&hinfo, ws.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      QGX_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (hinfo == 0) break;
     }
-    // final residual of the refined solution
-    double* last = ws.acc + 2 * (kRefineIters - 1);
+    if (hinfo != 0) {  // even the more shifted FP32 factor broke down
+      ++g_kernels;
+      set_int_kernel<<<1, 1, 0, st>>>(dinfo, hinfo);
+      ++g_kernels;
+      nan_if_failed_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, st>>>(ws.y, n, dinfo);
+      return launch_status();
+    }
+    double* scal = ws.acc;
+    double* pv = ws.w;   // search direction
+    double* qv = ws.inv; // T p
+    const unsigned gr = (unsigned)((n * 32 + 255) / 256);
+    const unsigned gd = (unsigned)std::min<int64_t>((n + 255) / 256, kDotBlocks);
+    auto precondition = [&]() -> int {  // r32 <- M^-1 r32
+      if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.r32, n,
+                           ws.info + 1) != CUSOLVER_STATUS_SUCCESS)
+        return QGX_ERR_SOLVER;
+      return QGX_OK;
+    };
+    ++g_kernels;
+    cg_init_kernel<<<gd, 256, 0, st>>>(ws.y, ws.r, ws.r32, b, n);
+    ++g_kernels;
+    dot_kernel<double><<<gd, 256, 0, st>>>(b, b, n, ws.part);
+    ++g_kernels;
+    reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gd, scal, 4);
+    if ((rc = precondition()) != QGX_OK) return rc;
+    ++g_kernels;
+    cg_direction_kernel<<<gd, 256, 0, st>>>(pv, ws.r32, n, scal, 1);
+    ++g_kernels;
+    dot_kernel<float><<<gd, 256, 0, st>>>(ws.r, ws.r32, n, ws.part);
+    ++g_kernels;
+    reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gd, scal, 0);
+    if ((rc = launch_status()) != QGX_OK) return rc;
+    double host[2];
+    for (int it = 0; it < kCgMaxIters; ++it) {
+      ++g_kernels;
+      symv_dot_kernel<<<gr, 256, 0, st>>>(T, n, pv, qv, ws.part);
+      ++g_kernels;
+      reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gr, scal, 1);
+      ++g_kernels;
+      cg_update_kernel<<<gd, 256, 0, st>>>(ws.y, ws.r, pv, qv, ws.r32, n, scal, ws.part);
+      ++g_kernels;
+      reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gd, scal, 2);
+      QGX_CHECK_CUDA(cudaMemcpyAsync(host, scal + kScalRR, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      QGX_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (!(host[0] > kCgTol * kCgTol * host[1])) break;  // converged (or NaN: caught by the check below)
+      if ((rc = precondition()) != QGX_OK) return rc;
+      ++g_kernels;
+      dot_kernel<float><<<gd, 256, 0, st>>>(ws.r, ws.r32, n, ws.part);
+      ++g_kernels;
+      reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gd, scal, 3);
+      ++g_kernels;
+      cg_direction_kernel<<<gd, 256, 0, st>>>(pv, ws.r32, n, scal, 0);
+    }
+    // the true residual of the result decides
+    double* last = ws.acc + 10;
     QGX_CHECK_CUDA(cudaMemsetAsync(last, 0, 2 * sizeof(double), st));
-    residual_kernel<<<gr, 256, 0, st>>>(T, n, ws.y, b, ws.r, ws.r32, last);
+    ++g_kernels;
+    residual_kernel<<<gr, 256, 0, st>>>(T, n, ws.y, b, ws.r, last);
+    ++g_kernels;
     refine_check_kernel<<<1, 1, 0, st>>>(last, ws.info, dinfo, kRefineTol);
     return launch_status();
   }
   if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.w,
                        CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
     return QGX_ERR_SOLVER;
+  ++g_kernels;
   eigs_inv_kernel<<<1, 1024, 0, st>>>(ws.w, n, rtol, atol, ws.inv);
+  ++g_kernels;
   rho_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(T, n, b, ws.inv, tol_snr, ws.v);
   const int64_t nchunk = (n + kProjRows - 1) / kProjRows;
+  ++g_kernels;
   uv_partial_kernel<<<dim3((unsigned)((n + 255) / 256), (unsigned)nchunk), 256, 0, st>>>(T, n, ws.v, ws.part);
+  ++g_kernels;
   sum_partials_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ws.part, nchunk, n, ws.y);
   return launch_status();
 }
@@ -387,6 +595,8 @@ int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* by
   return workspace_layout(n, np, method, nullptr, 0, &ws, bytes);
 }
 
+int64_t qgx_last_solve_kernels(void) { return g_kernels; }
+
 int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t lda, const double* b, int32_t method,
                     double rshift, double ashift, double rtol, double atol, double tol_snr, double* x, int32_t* info,
                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
@@ -394,6 +604,7 @@ int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t ld
   QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV || method == QGX_SOLVE_SHIFT_MIXED);
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
+  g_kernels = 0;
   SolveWs ws;
   int64_t need = 0;
   int rc = workspace_layout(n, np, method, workspace, workspace_bytes, &ws, &need);
@@ -412,6 +623,7 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
   // the per-sample SNR truncation of lstsq_pinv_eig needs the full (ns x np) rho matrix
   if (method == QGX_SOLVE_PINV && tol_snr > 1e-6) return QGX_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_solver_mutex);
+  g_kernels = 0;
   SolveWs ws;
   int64_t need = 0;
   int rc = workspace_layout(np, n, method, workspace, workspace_bytes, &ws, &need);

@@ -15,6 +15,10 @@ import torch
 from . import _lib
 from .state import VS_TYPE
 
+def _round8(n: int) -> int:
+    return (n + 7) // 8 * 8
+
+
 _GRAM_MODES = {"fp32": _lib.GRAM_FP32, "tf32": _lib.GRAM_TF32, "bf16": _lib.GRAM_BF16, "3xtf32": _lib.GRAM_3XTF32}
 
 
@@ -66,7 +70,11 @@ def lstsq_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Sol
     return Solver("shift", "lstsq", rshift=rshift, ashift=ashift)
 
 
-_F64_RTOL = 1e-12  # solver.py:12-21 for the float64 default dtype
+# Default relative shift / eigenvalue cut-off: solver.py:12-21 takes it from the dtype of the
+# matrix it factors (1e-12 float64, 1e-6 float32). Obar is FP32 here, so T = Obar Obar^T carries
+# FP32 rounding (~1e-7 ||T||) whatever its storage type: 1e-6 keeps T + shift positive definite
+# as ||T|| grows during training, where 1e-12 let the Cholesky break down.
+_OBAR_RTOL = 1e-6
 
 
 class QNGD:
@@ -85,6 +93,7 @@ class QNGD:
         self._buf = {}
         self.marks = None  # optional list: solve() appends ("gram", event) after the Gram build
         self.last_solve_fallback = False
+        self.solve_fallbacks = 0  # mixed solves that fell back to the FP64 factorisation
 
     @property
     def state(self):
@@ -105,9 +114,11 @@ class QNGD:
         raise NotImplementedError
 
     def get_Obar(self, samples) -> torch.Tensor:
-        """Obar = (O - <O>) sqrt(r / Ns) (sr.py:79-88)."""
-        out = self._buffer("obar", (self._state.obar_rows(samples.nsamples), self._state.nparams), torch.float32)
-        obar, self._Omean = self._state.obar(samples, out)
+        """Obar = (O - <O>) sqrt(r / Ns) (sr.py:79-88). Rows are padded to a multiple of 8
+        elements so that the tensor-core Gram can address them with TMA (16-byte strides)."""
+        np_ = self._state.nparams
+        out = self._buffer("obar", (self._state.obar_rows(samples.nsamples), _round8(np_)), torch.float32)
+        obar, self._Omean = self._state.obar(samples, out[:, :np_])
         return obar
 
     def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
@@ -118,8 +129,8 @@ class QNGD:
         ns, np_ = A.shape
         sv = self._solver
         method = _lib.SOLVE_SHIFT if sv.kind == "shift" else _lib.SOLVE_PINV
-        rshift = _F64_RTOL if sv.rshift is None else sv.rshift
-        rtol = _F64_RTOL if sv.rtol is None else sv.rtol
+        rshift = _OBAR_RTOL if sv.rshift is None else sv.rshift
+        rtol = _OBAR_RTOL if sv.rtol is None else sv.rtol
         x = torch.empty(np_, dtype=torch.float64, device=A.device)
         info = self._buffer("info", (1,), torch.int32)
         st = _lib.stream_ptr()
@@ -129,9 +140,9 @@ class QNGD:
         if sv.use_minnorm(ns, np_):
             T = self._buffer("gram", (ns, ns), torch.float64)
             if self._gram == _lib.GRAM_BF16:
-                Ab = self._buffer("obar_bf16", (ns, np_), torch.bfloat16)
-                _lib.call("qgx_f32_to_bf16", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(Ab), np_, st)
-                _lib.call("qgx_gram_tc", _lib.ptr(Ab), 1, ns, np_, np_, _lib.ptr(T), ns, None, st)
+                Ab = self._buffer("obar_bf16", (ns, _round8(np_)), torch.bfloat16)
+                _lib.call("qgx_f32_to_bf16", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(Ab), Ab.stride(0), st)
+                _lib.call("qgx_gram_tc", _lib.ptr(Ab), 1, ns, np_, Ab.stride(0), _lib.ptr(T), ns, None, st)
             else:
                 _lib.call("qgx_gram", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(T), ns, self._gram, st)
             self._mark("gram")
@@ -144,12 +155,14 @@ class QNGD:
             if method == _lib.SOLVE_SHIFT_MIXED:
                 code = int(info.item())
                 self.last_solve_fallback = code != 0
-                if code > 0:
-                    raise RuntimeError(f"T + shift is not positive definite (cuSOLVER info {code})")
-                if code < 0:
-                    # refinement stalled: factor the (already shifted) FP64 matrix instead
+                if code != 0:
+                    # the FP32 factor broke down (code > 0: pivot `code` not positive) or the
+                    # refinement stalled (code < 0): factor the already shifted FP64 matrix
+                    self.solve_fallbacks += 1
                     _lib.call("qgx_solve_workspace_bytes", ns, np_, _lib.SOLVE_SHIFT, C.byref(nbytes))
                     ws = self._state.workspace("solve", nbytes.value)
+                    # a failure here makes x NaN (the reference's Cholesky solve does the same),
+                    # and Variational.update skips the step with a warning
                     _lib.call("qgx_minsr_solve", _lib.ptr(T), ns, _lib.ptr(A), np_, A.stride(0), _lib.ptr(b),
                               _lib.SOLVE_SHIFT, 0.0, 0.0, rtol, sv.atol, sv.tol_snr, _lib.ptr(x), _lib.ptr(info),
                               _lib.ptr(ws), ws.numel(), st)

@@ -40,7 +40,8 @@ class JobSpec:
     channels: int = 8         # j1j2 ResConv width
     lr: float = 1e-2
     ashift: float = 1e-4
-    gram: str = "fp32"
+    conv: str = "bf16"        # ResConv forward convolutions: "fp32", "tf32" or "bf16"
+    gram: str = "bf16"        # Gram matrix arithmetic: "fp32", "tf32", "bf16" or "3xtf32"
     solve: str = "fp64"
     arrival: float = 0.0      # seconds after the server starts
 
@@ -95,7 +96,7 @@ class Job:
                 qtx.sites.Square(spec.L, Nparticles=(n // 2, n // 2))
                 H = qtx.operator.Heisenberg(J=[1.0, spec.J2], n_neighbor=[1, 2], msr=True)
                 self.state = qtx.state.Variational(
-                    qtx.model.ResConv(spec.blocks, spec.channels, out_dtype=np.complex64))
+                    qtx.model.ResConv(spec.blocks, spec.channels, out_dtype=np.complex64, conv_precision=spec.conv))
                 self.sampler = qtx.sampler.SpinExchange(self.state, spec.nsamples, thermal_steps=n, sweep_steps=n)
             else:
                 raise ValueError(spec.kind)

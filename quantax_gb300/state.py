@@ -194,13 +194,14 @@ class Variational:
             return out, omean
         ws = self.workspace("jac", self._model.jacobian_workspace_bytes())
         cplx = self.is_complex
-        self._model.jacobian(self._table, samples.packed, out[:ns], out[ns:] if cplx else None, self.nparams, ws)
+        ld = out.stride(0)
+        self._model.jacobian(self._table, samples.packed, out[:ns], out[ns:] if cplx else None, ld, ws)
         cws = self.workspace("center", _lib.lib().qgx_center_columns_workspace_bytes(ns, self.nparams))
         halves = [out[:ns], out[ns:]] if cplx else [out]
         means = []
         for h in halves:
             m = torch.empty(self.nparams, dtype=torch.float64, device=self._dev)
-            _lib.call("qgx_center_columns", _lib.ptr(h), ns, self.nparams, self.nparams,
+            _lib.call("qgx_center_columns", _lib.ptr(h), ns, self.nparams, ld,
                       _lib.ptr(samples.reweight_factor), _lib.ptr(m), _lib.ptr(cws), cws.numel(), _lib.stream_ptr())
             means.append(m)
         omean = torch.complex(means[0], means[1]) if cplx else means[0]

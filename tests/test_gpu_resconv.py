@@ -149,7 +149,7 @@ def test_resconv_sr_step_matches_oracle(cuda):
         E = oops.local_energy(s, ops, onet.log_psi)
         eb, em, var = osr.ebar(E)
         Ob = osr.obar(onet.jacobian(s))
-        x = osr.solve(Ob, eb, lambda A, b: osr.auto(A, b, "shift", ashift=1e-3), complex_out=True)
+        x = osr.solve(Ob, eb, lambda A, b: osr.auto(A, b, "shift", rshift=1e-6, ashift=1e-3), complex_out=True)
         assert abs(opt.energy - em) <= 1e-5 * abs(em)
         assert np.linalg.norm(step - x) / np.linalg.norm(x) < 1e-2
         state.update(torch.as_tensor(step).cuda() * 1e-2)

@@ -183,7 +183,7 @@ def test_vmc_loop_matches_oracle_and_ed(cuda):
             assert (samples.spins.cpu().numpy() == s).all(), f"samples diverged at step {it}"
             E = oops.local_energy(s, ops, net.log_psi).real
             eb, em, var = osr.ebar(E)
-            x = osr.solve(osr.obar(net.jacobian(s)), eb, lambda A, b: osr.auto(A, b, "shift", ashift=1e-4))
+            x = osr.solve(osr.obar(net.jacobian(s)), eb, lambda A, b: osr.auto(A, b, "shift", rshift=1e-6, ashift=1e-4))
             assert abs(opt.energy - em) <= 1e-6 * abs(em)
             assert abs(opt.VarE - var) <= 1e-4 * var + 1e-9
             errs.append(np.linalg.norm(step.cpu().numpy() - x) / np.linalg.norm(x))
@@ -191,3 +191,46 @@ def test_vmc_loop_matches_oracle_and_ed(cuda):
     assert max(errs) < 1e-3, errs
     e_ed = -10.2516617909660
     assert abs(np.mean(energies[-10:]) - e_ed) / abs(e_ed) < 0.02
+
+
+def _rbm_opt(solver):
+    import quantax_gb300 as qtx
+    qtx.set_default_dtype(np.float64)
+    qtx.sites.Chain(8)
+    qtx.set_random_seed(1)
+    state = qtx.state.Variational(qtx.model.RBM_Dense(16, init_std=0.01))
+    return qtx.optimizer.SR(state, qtx.operator.Ising(h=1.0), solver=solver)
+
+
+def test_mixed_solve_converges_ill_conditioned(cuda):
+    """T + shift with condition number ~1e11 (duplicated Obar rows, tiny shift) and a
+    right-hand side in the range of Obar: the FP32-preconditioned FP64 conjugate gradients
+    converge without falling back, to the FP64 oracle's solution (stated: 1e-6 relative)."""
+    import quantax_gb300 as qtx
+    opt = _rbm_opt(qtx.optimizer.minnorm_shift_eig(rshift=1e-12, ashift=1e-12, precision="mixed"))
+    rng = np.random.default_rng(5)
+    Bm = rng.normal(size=(32, 144)) / 12.0
+    A = np.concatenate([Bm, Bm]).astype(np.float32)
+    c = rng.normal(size=32)
+    b = np.concatenate([c, c])  # no component along the near-null directions of T
+    x = opt.solve(torch.as_tensor(A).cuda(), torch.as_tensor(b).cuda()).cpu().numpy()
+    assert opt.solve_fallbacks == 0
+    ref = osr.minnorm_shift(A.astype(np.float64), b, ashift=1e-12)
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def test_mixed_solve_falls_back_to_fp64(cuda):
+    """A system the mixed solve cannot finish (condition number ~1e13, right-hand side along
+    the near-null directions): it reports info -1, QNGD.solve factors the shifted FP64
+    matrix, and the step is exactly that of the FP64 path on the same inputs."""
+    import quantax_gb300 as qtx
+    rng = np.random.default_rng(6)
+    Bm = rng.normal(size=(32, 144)) / 12.0
+    A = torch.as_tensor(np.concatenate([Bm, Bm]).astype(np.float32)).cuda()
+    b = torch.as_tensor(rng.normal(size=64)).cuda()
+    mixed = _rbm_opt(qtx.optimizer.minnorm_shift_eig(rshift=0.0, ashift=1e-13, precision="mixed"))
+    x_mixed = mixed.solve(A, b).cpu().numpy()
+    assert mixed.solve_fallbacks == 1 and mixed.last_solve_fallback
+    plain = _rbm_opt(qtx.optimizer.minnorm_shift_eig(rshift=0.0, ashift=1e-13, precision="fp64"))
+    x_fp64 = plain.solve(A, b).cpu().numpy()
+    np.testing.assert_array_equal(x_mixed, x_fp64)

@@ -9,6 +9,8 @@
 
 #include <cstdint>
 
+#include "qgx_common.cuh"
+
 namespace qgx {
 namespace {
 
@@ -53,6 +55,40 @@ __device__ inline float gelu_fast(float x) {
   const float k0 = 0.7978845608028654f;
   const float u = k0 * fmaf(0.044715f * x, x * x, x);
   return __fdividef(x, 1.0f + __expf(-2.0f * u));
+}
+
+// SpinExchange proposal of one chain (common_samplers.py:58-162) on its packed words w
+// (nw <= 8, updated in place): site i uniform among the hopping spins (w0 of the draw), j
+// uniform in the padded neighbour row of i (w2; -1: no move); returns whether the swap
+// changed the configuration
+__device__ inline bool propose_exchange(uint32_t (&w)[8], int n, int nw, const u32x4& r, const int32_t* __restrict__ nbr,
+                                        int z, int hop) {
+  int total = 0;
+  for (int k = 0; k < nw; ++k) {
+    const uint32_t valid = (32 * k + 32 <= n) ? 0xffffffffu : ((1u << (n - 32 * k)) - 1u);
+    total += __popc((hop > 0 ? w[k] : ~w[k]) & valid);
+  }
+  if (total == 0) return false;
+  int pick = (int)bounded(r.x, (uint32_t)total);
+  int i = -1;
+  for (int k = 0; k < nw && i < 0; ++k) {
+    const uint32_t valid = (32 * k + 32 <= n) ? 0xffffffffu : ((1u << (n - 32 * k)) - 1u);
+    uint32_t m = (hop > 0 ? w[k] : ~w[k]) & valid;
+    const int cnt = __popc(m);
+    if (pick < cnt) {
+      for (int q = 0; q < pick; ++q) m &= m - 1u;
+      i = 32 * k + __ffs(m) - 1;
+    } else {
+      pick -= cnt;
+    }
+  }
+  int j = nbr[(int64_t)i * z + (int)bounded(r.z, (uint32_t)z)];
+  if (j < 0) j = i;
+  const uint32_t bi = (w[i >> 5] >> (i & 31)) & 1u, bj = (w[j >> 5] >> (j & 31)) & 1u;
+  if (bi == bj) return false;
+  w[i >> 5] ^= 1u << (i & 31);
+  w[j >> 5] ^= 1u << (j & 31);
+  return true;
 }
 
 }  // namespace

@@ -201,37 +201,9 @@ __global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* 
   if (c >= ns) return;
   const int nw = words_for(n);
   uint32_t w[8];
-  int total = 0;
-  for (int k = 0; k < nw; ++k) {
-    w[k] = spins[c * nw + k];
-    const uint32_t valid = (32 * k + 32 <= n) ? 0xffffffffu : ((1u << (n - 32 * k)) - 1u);
-    total += __popc((hop > 0 ? w[k] : ~w[k]) & valid);
-  }
+  for (int k = 0; k < nw; ++k) w[k] = spins[c * nw + k];
   const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
-  int8_t ch = 0;
-  if (total > 0) {
-    int pick = (int)bounded(r.x, (uint32_t)total);
-    int i = -1;
-    for (int k = 0; k < nw && i < 0; ++k) {
-      const uint32_t valid = (32 * k + 32 <= n) ? 0xffffffffu : ((1u << (n - 32 * k)) - 1u);
-      uint32_t m = (hop > 0 ? w[k] : ~w[k]) & valid;
-      const int cnt = __popc(m);
-      if (pick < cnt) {
-        for (int q = 0; q < pick; ++q) m &= m - 1u;
-        i = 32 * k + __ffs(m) - 1;
-      } else {
-        pick -= cnt;
-      }
-    }
-    int j = nbr[(int64_t)i * z + (int)bounded(r.z, (uint32_t)z)];
-    if (j < 0) j = i;
-    const uint32_t bi = (w[i >> 5] >> (i & 31)) & 1u, bj = (w[j >> 5] >> (j & 31)) & 1u;
-    if (bi != bj) {
-      w[i >> 5] ^= 1u << (i & 31);
-      w[j >> 5] ^= 1u << (j & 31);
-      ch = 1;
-    }
-  }
+  const int8_t ch = propose_exchange(w, n, nw, r, nbr, z, hop) ? 1 : 0;
   for (int k = 0; k < nw; ++k) prop[c * nw + k] = w[k];
   changed[c] = ch;
 }

@@ -221,60 +221,72 @@ __device__ inline void put_row(uint8_t* buf, const TcShape& sh, const RowPos& rp
   }
 }
 
-// WG warpgroups, RPT tile rows per thread (tiles j = wg, wg + WG, ...), MINB CTAs per SM
-template <int KIND, int WG, int RPT, int MINB>
-__global__ void __launch_bounds__(128 * WG, MINB)
-    rc_forward_tc_kernel(const uint8_t* __restrict__ wimg, TcShape sh, const uint32_t* __restrict__ cfg,
-                         int64_t ncfg, const int64_t* __restrict__ n_live, float2* __restrict__ out) {
+// The forward machinery of one CTA: shared-memory buffers, barriers, TMEM and the layer
+// pipeline state that persists from one forward to the next (the weight prefetch runs across
+// forwards). WG warpgroups, RPT tile rows per thread (tiles j = wg, wg + WG, ...).
+template <int KIND, int WG, int RPT>
+struct TcForward {
   using Cfg = TcCfg<KIND>;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* P = sm + sh.oP;
-  uint8_t* Q = sm + sh.oQ;
-  uint8_t* W = sm + sh.oW;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + sh.oBar);
-  uint64_t* wbar = mbar + 1;  // two: one per weight buffer
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + sh.oBar + 24);
-  __shared__ int fail;
+  static constexpr int kThreads = 128 * WG;
+  const TcShape& sh;
+  const uint8_t* wimg;
+  uint8_t *P, *Q, *W;
+  uint64_t *mbar, *wbar;
+  volatile int* fail;
+  uint32_t tmem, tmem_lane;
+  uint32_t lc = 0;                    // convolutions run by this CTA so far
+  uint32_t w_issued = 0, w_done = 0;  // weight loads issued / waited for (thread 0)
+  int tid, warp, lane, wg, row_in_tile, plane, nlayers;
 
-  constexpr int kThreads = 128 * WG;
-  const int L = sh.L, N = sh.N, S = sh.S, nw = words_for(N);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, wg = tid >> 7, row_in_tile = tid & 127;
-  const int plane = sh.rows_tot * 16;
-  const int nlayers = 2 * sh.B;
-  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
-
-  // P and Q start zeroed: guard and padding rows stay finite
-  for (int e = tid; e < 2 * Cfg::chunks * plane / 16; e += blockDim.x)
-    reinterpret_cast<uint4*>(P)[e] = make_uint4(0, 0, 0, 0);
-  if (tid == 0) {
-    mbar_init(mbar, 1);
-    mbar_init(wbar, 1);
-    mbar_init(wbar + 1, 1);
-    fail = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(sh.tmem_cols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-  const uint32_t tmem_lane = (uint32_t)(32 * (warp & 3)) << 16;
-  uint32_t lc = 0;                       // convolutions run by this CTA so far
-  uint32_t w_issued = 0, w_done = 0;     // weight loads issued / waited for (thread 0)
-  if (tid == 0 && (int64_t)blockIdx.x * S < total) {
-    mbar_expect_tx(wbar, Cfg::layer_bytes);
-    bulk_load(W, wimg, Cfg::layer_bytes, wbar);
-    w_issued = 1;
+  __device__ TcForward(const TcShape& shape, const uint8_t* weights, uint8_t* sm, volatile int* fail_flag)
+      : sh(shape), wimg(weights), fail(fail_flag) {
+    P = sm + sh.oP;
+    Q = sm + sh.oQ;
+    W = sm + sh.oW;
+    mbar = reinterpret_cast<uint64_t*>(sm + sh.oBar);
+    wbar = mbar + 1;  // two: one per weight buffer
+    tid = threadIdx.x;
+    warp = tid >> 5;
+    lane = tid & 31;
+    wg = tid >> 7;
+    row_in_tile = tid & 127;
+    plane = sh.rows_tot * 16;
+    nlayers = 2 * sh.B;
   }
 
-  // one convolution of the buffer `in` into TMEM (all tiles); false on a timed-out wait
-  auto conv = [&](const uint8_t* in, bool more_after) -> bool {
+  // zeroed buffers, barriers, TMEM; the first layer's weights when the CTA has work
+  __device__ void setup(uint8_t* sm, bool has_work) {
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + sh.oBar + 24);
+    // P and Q start zeroed: guard and padding rows stay finite
+    for (int e = tid; e < 2 * Cfg::chunks * plane / 16; e += blockDim.x)
+      reinterpret_cast<uint4*>(P)[e] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+      mbar_init(mbar, 1);
+      mbar_init(wbar, 1);
+      mbar_init(wbar + 1, 1);
+      *fail = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(sh.tmem_cols)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    tmem = *tmem_slot;
+    tmem_lane = (uint32_t)(32 * (warp & 3)) << 16;
+    if (tid == 0 && has_work) {
+      mbar_expect_tx(wbar, Cfg::layer_bytes);
+      bulk_load(W, wimg, Cfg::layer_bytes, wbar);
+      w_issued = 1;
+    }
+  }
+
+  // one convolution of the buffer `in` into TMEM (all tiles); false once a wait timed out
+  __device__ bool conv(const uint8_t* in, bool more_after) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
     __syncthreads();
@@ -282,7 +294,7 @@ __global__ void __launch_bounds__(128 * WG, MINB)
     if (tid == 0) {
       tc_fence_after();
       if (!mbar_wait(wbar + buf, (lc >> 1) & 1)) {
-        fail = 1;
+        *fail = 1;
       } else {
         w_done = lc + 1;
         // descriptors advance in 16-byte units of the start-address field (addresses stay
@@ -313,17 +325,18 @@ __global__ void __launch_bounds__(128 * WG, MINB)
     }
     // thread 0 waits for the commit; the others wait at the barrier without taking issue
     // slots from the other CTAs on the SM
-    if (tid == 0 && !fail && !mbar_wait(mbar, lc & 1)) fail = 1;
+    if (tid == 0 && !*fail && !mbar_wait(mbar, lc & 1)) *fail = 1;
     __syncthreads();
     ++lc;
     tc_fence_after();
-    return fail == 0;
-  };
+    return *fail == 0;
+  }
 
-  int64_t base = (int64_t)blockIdx.x * S;
-  for (; base < total; base += (int64_t)gridDim.x * S) {
-    const int s_here = (int)(total - base < S ? total - base : S);
-    const bool next_group = base + (int64_t)gridDim.x * S < total;
+  // log psi of s_here configurations (packed words, row stride nw words; global or shared
+  // memory) into out[0 .. s_here); more_after: another forward follows in this CTA. Returns
+  // false (the same in every thread) once a wait has timed out.
+  __device__ bool forward(const uint32_t* cfg, int s_here, bool more_after, float2* out) {
+    const int L = sh.L, N = sh.N, nw = words_for(N);
     float x[RPT][16];  // residual stream of this thread's rows
     int pos[RPT];      // packed RowPos of those rows
     // x = s on the C channels; P = s / sqrt 2 on channel 0 (block 0's conv1 has one input channel)
@@ -334,7 +347,7 @@ __global__ void __launch_bounds__(128 * WG, MINB)
       const RowPos rp = unpack_pos(pos[k]);
       if (!rp.live) continue;
       const int r = (rp.py - 1) * L + (rp.px - 1);
-      const float sv = ((cfg[(base + rp.a) * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
+      const float sv = ((cfg[rp.a * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
       float v[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
@@ -343,10 +356,9 @@ __global__ void __launch_bounds__(128 * WG, MINB)
       }
       put_row<KIND>(P, sh, rp, v);
     }
-    bool ok = true;
     for (int b = 0; b < sh.B; ++b) {
       // conv1: Q = gelu(conv(P) + b1)
-      if (!(ok = conv(P, true))) break;
+      if (!conv(P, true)) return false;
       {
         const float* bias = reinterpret_cast<const float*>(W + ((lc - 1) & 1) * sh.wbuf + 9 * Cfg::chunks * 256);
 #pragma unroll
@@ -363,7 +375,7 @@ __global__ void __launch_bounds__(128 * WG, MINB)
         }
       }
       // conv2: x += conv(Q) + b2; then the next block's P = gelu(x / sqrt(b + 2))
-      if (!(ok = conv(Q, b + 1 < sh.B || next_group))) break;
+      if (!conv(Q, b + 1 < sh.B || more_after)) return false;
       {
         const float* bias = reinterpret_cast<const float*>(W + ((lc - 1) & 1) * sh.wbuf + 9 * Cfg::chunks * 256);
         const float scale = rsqrtf((float)(b + 2));
@@ -384,7 +396,6 @@ __global__ void __launch_bounds__(128 * WG, MINB)
         }
       }
     }
-    if (!ok) break;
     // log sum exp over (channel, site) per sample: z = x / sqrt(B + 1) of the C channels
     // is gathered in shared memory (over P and Q, free now), one warp per sample
     float* Z = reinterpret_cast<float*>(P);
@@ -416,27 +427,54 @@ __global__ void __launch_bounds__(128 * WG, MINB)
       }
       sr = warp_sum(sr);
       si = warp_sum(si);
-      if (lane == 0)
-        out[base + a] = make_float2(mx + 0.5f * logf(sr * sr + si * si) - logf((float)(cp * N)), atan2f(si, sr));
+      if (lane == 0) out[a] = make_float2(mx + 0.5f * logf(sr * sr + si * si) - logf((float)(cp * N)), atan2f(si, sr));
     }
-    __syncthreads();  // Z is overwritten by the next group's P
+    __syncthreads();  // Z is overwritten by the next forward's P; out may be read next
+    return true;
+  }
+
+  // after a timeout: a weight copy may still be in flight; give it the bounded wait before
+  // the CTA exits, then release TMEM
+  __device__ void teardown() {
+    if (*fail && tid == 0 && w_issued > w_done) mbar_wait(wbar + (w_done & 1), (w_done >> 1) & 1);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+      tc_fence_after();
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(sh.tmem_cols) : "memory");
+    }
+  }
+};
+
+__device__ inline uint8_t* aligned_smem(uint8_t* raw) {
+  return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
+}
+
+// log psi of ncfg packed configurations (n_live, on the device, may cap the count), S per CTA
+template <int KIND, int WG, int RPT, int MINB>
+__global__ void __launch_bounds__(128 * WG, MINB)
+    rc_forward_tc_kernel(const uint8_t* __restrict__ wimg, TcShape sh, const uint32_t* __restrict__ cfg,
+                         int64_t ncfg, const int64_t* __restrict__ n_live, float2* __restrict__ out) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = aligned_smem(smem_raw);
+  __shared__ int fail;
+  const int S = sh.S, nw = words_for(sh.N);
+  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
+  TcForward<KIND, WG, RPT> f(sh, wimg, sm, &fail);
+  f.setup(sm, (int64_t)blockIdx.x * S < total);
+  int64_t base = (int64_t)blockIdx.x * S;
+  for (; base < total; base += (int64_t)gridDim.x * S) {
+    const int s_here = (int)(total - base < S ? total - base : S);
+    const bool next_group = base + (int64_t)gridDim.x * S < total;
+    if (!f.forward(cfg + base * nw, s_here, next_group, out + base)) break;
   }
   if (base < total) {
     // a wait timed out: this CTA's remaining outputs become NaN, so the failure shows in
     // every energy and update computed from them
     for (int64_t b2 = base; b2 < total; b2 += (int64_t)gridDim.x * S)
-      for (int a = tid; a < S && b2 + a < total; a += blockDim.x) out[b2 + a] = make_float2(NAN, NAN);
-    if (tid == 0 && w_issued > w_done) {
-      // a weight copy may still be in flight: give it the bounded wait before the CTA exits
-      mbar_wait(wbar + (w_done & 1), (w_done >> 1) & 1);
-    }
+      for (int a = threadIdx.x; a < S && b2 + a < total; a += blockDim.x) out[b2 + a] = make_float2(NAN, NAN);
   }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(sh.tmem_cols) : "memory");
-  }
+  f.teardown();
 }
 
 // weight images for the tensor-core kernels from the FP32 table slices
@@ -492,18 +530,38 @@ int launch_tc_variant(const uint8_t* wimg, const TcShape& sh, const uint32_t* cf
   return launch_status();
 }
 
+// shape of the tensor-core kernels for a launch configuration; false if unsupported
+template <int KIND>
+bool tc_launch_shape(int L, int B, int C, bool cplx, TcShape* sh) {
+  using T = TcLaunch<KIND>;
+  constexpr int tiles = T::WG * T::RPT;
+  if ((L + 2) * (L + 2) > tiles * 128) return false;
+  *sh = tc_shape(L, B, C, cplx, TcCfg<KIND>::esz, tc_samples_per_cta(L, tiles));
+  return sh->ntiles <= tiles && sh->smem * T::CTAS <= 227 * 1024 && sh->smem <= device_max_smem_optin() &&
+         sh->tmem_cols * T::CTAS <= 512;
+}
+
+// dynamic shared memory requested: raised so that no more than CTAS CTAs (and their TMEM
+// allocations) share an SM
+template <int KIND>
+int tc_smem_request(const TcShape& sh) {
+  return std::max(sh.smem, std::min(device_max_smem_optin(), (227 * 1024) / (TcLaunch<KIND>::CTAS + 1) + 1024));
+}
+
 template <int KIND>
 int launch_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,
               const int64_t* n_live, float2* out, cudaStream_t st) {
   using T = TcLaunch<KIND>;
-  constexpr int tiles = T::WG * T::RPT;
-  if ((L + 2) * (L + 2) > tiles * 128) return QGX_ERR_UNSUPPORTED;
-  const TcShape sh = tc_shape(L, B, C, cplx, TcCfg<KIND>::esz, tc_samples_per_cta(L, tiles));
-  if (sh.ntiles > tiles || sh.smem * T::CTAS > 227 * 1024 || sh.smem > device_max_smem_optin() ||
-      sh.tmem_cols * T::CTAS > 512)
-    return QGX_ERR_UNSUPPORTED;
+  TcShape sh;
+  if (!tc_launch_shape<KIND>(L, B, C, cplx, &sh)) return QGX_ERR_UNSUPPORTED;
   const uint8_t* wimg = reinterpret_cast<const uint8_t*>(table) + tc_image_offset(B, C, KIND);
-  return launch_tc_variant<KIND, T::WG, T::RPT, T::CTAS>(wimg, sh, cfg, ncfg, n_live, out, st);
+  auto k = rc_forward_tc_kernel<KIND, T::WG, T::RPT, T::CTAS>;
+  const int smem = tc_smem_request<KIND>(sh);
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  const int64_t want = (ncfg + sh.S - 1) / sh.S;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)device_sm_count() * T::CTAS, want));
+  k<<<grid, 128 * T::WG, smem, st>>>(wimg, sh, cfg, ncfg, n_live, out);
+  return launch_status();
 }
 
 }  // namespace

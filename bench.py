@@ -156,7 +156,8 @@ WORKLOAD_RESCONV = dict(workload="j1j2_square10_resconv8x16_minsr16384", lattice
 
 def build_workload(qtx, rank, gram, solve, workload="rbm", conv="fp32"):
     import numpy as np
-    qtx.set_random_seed(1234 + rank)
+    from quantax_gb300 import replicas
+    qtx.set_random_seed(replicas.replica_seed(1234, rank))
     solver = qtx.optimizer.minnorm_shift_eig(ashift=1e-4, precision=solve)
     if workload == "resconv":
         qtx.set_default_dtype(np.complex128)
@@ -179,7 +180,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
     import torch
     import torch.distributed as dist
     import quantax_gb300 as qtx
-    from quantax_gb300 import _lib
+    from quantax_gb300 import _lib, replicas
 
     state, sampler, opt = build_workload(qtx, rank, gram, solve, args.workload, conv)
     lr = 1e-2
@@ -211,8 +212,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
     torch.cuda.synchronize()
     if clocks is not None:
         clocks.start()
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     launches0 = _lib.launch_count
     start = torch.cuda.Event(enable_timing=True)
@@ -226,15 +226,10 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
     end = torch.cuda.Event(enable_timing=True)
     end.record()
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     clk = clocks.stop() if clocks is not None else None
     launches = _lib.launch_count - launches0
-    elapsed = start.elapsed_time(end) / 1000.0
-    if world > 1:
-        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = replicas.max_over_ranks(start.elapsed_time(end) / 1000.0, "cuda")
     lat, prev = [], start
     for e in step_events:
         lat.append(prev.elapsed_time(e))
@@ -260,8 +255,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
         host_out = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
         host_stats = torch.empty(3, dtype=torch.float64).pin_memory()
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+        replicas.barrier()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -275,11 +269,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
             host_params.copy_(host_out)
         e1.record()
         torch.cuda.synchronize()
-        e2e_s = e0.elapsed_time(e1) / 1000.0
-        if world > 1:
-            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = replicas.max_over_ranks(e0.elapsed_time(e1) / 1000.0, "cuda")
         out["e2e_s"] = e2e_s
     return out
 

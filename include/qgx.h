@@ -259,7 +259,12 @@ int qgx_gram_tc(const void* A, int32_t a_dtype, int64_t rows, int64_t k, int64_t
 /* bf16 copy of an FP32 matrix (round to nearest even), the operand of the bf16 Gram. */
 int qgx_f32_to_bf16(const float* in, int64_t rows, int64_t k, int64_t ldi, uint16_t* out,
                     int64_t ldo, qgx_stream_t stream);
-/* S = A^T A (k x k) for the SR branch (Ns >= Np). */
+/* out = A^T (cols x rows, row stride ldo elements) of an FP32 matrix (rows x cols, ldi);
+ * out_dtype 0: FP32, 1: BF16 (round to nearest even). With it the tensor-core Gram computes
+ * the SR branch's S = A^T A as the Gram of A^T (rows <= 2097120). */
+int qgx_transpose(const float* in, int64_t rows, int64_t cols, int64_t ldi, void* out, int64_t ldo,
+                  int32_t out_dtype, qgx_stream_t stream);
+/* S = A^T A (k x k) for the SR branch (Ns >= Np), FP32 on the CUDA cores. */
 int qgx_gram_t(const float* A, int64_t rows, int64_t k, int64_t lda, double* S, int64_t lds,
                qgx_stream_t stream);
 

@@ -333,6 +333,30 @@ __global__ void to_bf16_kernel(const float* __restrict__ in, int64_t rows, int64
     out[r * ldo + c] = __float2bfloat16_rn(in[r * ldi + c]);
 }
 
+// out[c][r] = in[r][c] through a 32 x 33 shared tile (coalesced reads and writes); OUT_BF16
+// rounds to nearest even
+template <bool OUT_BF16>
+__global__ void transpose_kernel(const float* __restrict__ in, int64_t rows, int64_t cols, int64_t ldi,
+                                 void* __restrict__ out, int64_t ldo) {
+  __shared__ float tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = r0 + i, c = c0 + tx;
+    tile[i][tx] = (r < rows && c < cols) ? in[r * ldi + c] : 0.0f;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t c = c0 + i, r = r0 + tx;
+    if (c < cols && r < rows) {
+      if (OUT_BF16)
+        reinterpret_cast<__nv_bfloat16*>(out)[c * ldo + r] = __float2bfloat16_rn(tile[tx][i]);
+      else
+        reinterpret_cast<float*>(out)[c * ldo + r] = tile[tx][i];
+    }
+  }
+}
+
 }  // namespace
 
 int gram_tc(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, int64_t ldt, int mode, cudaStream_t st) {
@@ -355,6 +379,20 @@ int qgx_gram_tc(const void* A, int32_t a_dtype, int64_t rows, int64_t k, int64_t
   if (a_dtype == 0) return launch_gram_tc<0>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
   if (a_dtype == 2) return launch_gram_tc<2>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
   return launch_gram_tc<1>(A, rows, k, lda, T, ldt, status, as_cuda(stream));
+}
+
+int qgx_transpose(const float* in, int64_t rows, int64_t cols, int64_t ldi, void* out, int64_t ldo, int32_t out_dtype,
+                  qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows >= 0 && cols >= 0 && ldi >= cols && ldo >= rows && (out_dtype == 0 || out_dtype == 1));
+  if (rows == 0 || cols == 0) return QGX_OK;
+  QGX_CHECK_ARG(in && out);
+  const int64_t gy = (rows + 31) / 32, gx = (cols + 31) / 32;
+  QGX_CHECK_ARG(gy <= 65535 && gx <= 2147483647LL);
+  if (out_dtype == 1)
+    transpose_kernel<true><<<dim3((unsigned)gx, (unsigned)gy), 256, 0, as_cuda(stream)>>>(in, rows, cols, ldi, out, ldo);
+  else
+    transpose_kernel<false><<<dim3((unsigned)gx, (unsigned)gy), 256, 0, as_cuda(stream)>>>(in, rows, cols, ldi, out, ldo);
+  return launch_status();
 }
 
 int qgx_f32_to_bf16(const float* in, int64_t rows, int64_t k, int64_t ldi, uint16_t* out, int64_t ldo,

@@ -168,7 +168,17 @@ class QNGD:
                               _lib.ptr(ws), ws.numel(), st)
         else:
             S = self._buffer("gram", (np_, np_), torch.float64)
-            _lib.call("qgx_gram_t", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(S), np_, st)
+            if self._gram == _lib.GRAM_FP32:
+                _lib.call("qgx_gram_t", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(S), np_, st)
+            else:
+                # S = A^T A as the tensor-core Gram of A^T (rows padded for 16-byte TMA strides)
+                bf16 = self._gram == _lib.GRAM_BF16
+                At = self._buffer("obar_t", (np_, _round8(ns)), torch.bfloat16 if bf16 else torch.float32)
+                _lib.call("qgx_transpose", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(At), At.stride(0), int(bf16), st)
+                if bf16:
+                    _lib.call("qgx_gram_tc", _lib.ptr(At), 1, np_, ns, At.stride(0), _lib.ptr(S), np_, None, st)
+                else:
+                    _lib.call("qgx_gram", _lib.ptr(At), np_, ns, At.stride(0), _lib.ptr(S), np_, self._gram, st)
             self._mark("gram")
             _lib.call("qgx_solve_workspace_bytes", np_, ns, method, C.byref(nbytes))
             ws = self._state.workspace("solve", nbytes.value)

@@ -65,3 +65,49 @@ def test_tc_gram_rejects_unaligned_stride(cuda):
     T = torch.empty((64, 64), dtype=torch.float64, device="cuda")
     rc = L.lib().qgx_gram_tc(L.ptr(A), 0, 64, 30, 30, L.ptr(T), 64, None, L.stream_ptr())
     assert rc == L.QGX_ERR_UNSUPPORTED
+
+
+def test_tc_gram_long_k_accumulation(cuda):
+    """K = 34944 (the ResConv Obar width): the tensor core accumulates 256-element chunks that
+    are summed in registers, so the accumulation error does not grow with K (a single FP32
+    TMEM accumulator lost ~k 2^-25 = 1e-3 with a systematic sign). Compared with the FP64
+    Gram of the same BF16 operands, i.e. accumulation error only (stated: 1e-5)."""
+    from quantax_gb300 import _lib as L
+    rng = np.random.default_rng(3)
+    A = (0.3 * rng.normal(size=34944)[None, :] + rng.normal(size=(256, 34944))).astype(np.float32)
+    At = torch.as_tensor(A).cuda()
+    Ab = At.to(torch.bfloat16)
+    T = torch.empty((256, 256), dtype=torch.float64, device="cuda")
+    L.call("qgx_gram_tc", L.ptr(Ab), 1, 256, 34944, 34944, L.ptr(T), 256, None, L.stream_ptr())
+    B = Ab.double().cpu().numpy()
+    ref = B @ B.T
+    d = np.sqrt(np.diag(ref))
+    err = np.abs(T.cpu().numpy() - ref) / np.outer(d, d)
+    assert err.max() < 1e-5, err.max()
+
+
+@pytest.mark.parametrize("mode", ["tf32", "bf16", "3xtf32"])
+def test_sr_gram_through_transpose(cuda, mode):
+    """SR branch (Ns >= Np): S = A^T A as the tensor-core Gram of A^T (qgx_transpose)."""
+    from quantax_gb300 import _lib as L
+    ns, np_ = 2000, 300
+    A = np.random.default_rng(9).normal(size=(ns, np_)).astype(np.float32)
+    At = torch.as_tensor(A).cuda()
+    ld = (ns + 7) // 8 * 8
+    bf16 = mode == "bf16"
+    Atr = torch.empty((np_, ld), dtype=torch.bfloat16 if bf16 else torch.float32, device="cuda")
+    L.call("qgx_transpose", L.ptr(At), ns, np_, np_, L.ptr(Atr), ld, int(bf16), L.stream_ptr())
+    if bf16:
+        assert torch.equal(Atr[:, :ns], At.t().to(torch.bfloat16))
+    else:
+        assert torch.equal(Atr[:, :ns], At.t())
+    S = torch.empty((np_, np_), dtype=torch.float64, device="cuda")
+    if bf16:
+        L.call("qgx_gram_tc", L.ptr(Atr), 1, np_, ns, ld, L.ptr(S), np_, None, L.stream_ptr())
+    else:
+        m = {"tf32": L.GRAM_TF32, "3xtf32": L.GRAM_3XTF32}[mode]
+        L.call("qgx_gram", L.ptr(Atr), np_, ns, ld, L.ptr(S), np_, m, L.stream_ptr())
+    ref = A.astype(np.float64).T @ A.astype(np.float64)
+    d = np.sqrt(np.diag(ref))
+    err = np.abs(S.cpu().numpy() - ref) / np.outer(d, d)
+    assert err.max() < tol({"tf32": 0, "bf16": 1, "3xtf32": 2}[mode], ns), err.max()

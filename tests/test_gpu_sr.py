@@ -193,13 +193,27 @@ def test_vmc_loop_matches_oracle_and_ed(cuda):
     assert abs(np.mean(energies[-10:]) - e_ed) / abs(e_ed) < 0.02
 
 
-def _rbm_opt(solver):
+def _rbm_opt(solver, gram="fp32"):
     import quantax_gb300 as qtx
     qtx.set_default_dtype(np.float64)
     qtx.sites.Chain(8)
     qtx.set_random_seed(1)
     state = qtx.state.Variational(qtx.model.RBM_Dense(16, init_std=0.01))
-    return qtx.optimizer.SR(state, qtx.operator.Ising(h=1.0), solver=solver)
+    return qtx.optimizer.SR(state, qtx.operator.Ising(h=1.0), solver=solver, gram=gram)
+
+
+@pytest.mark.parametrize("gram,tol", [("fp32", 1e-5), ("3xtf32", 1e-5), ("tf32", 5e-3), ("bf16", 2e-2)])
+def test_sr_branch_gram_modes(cuda, gram, tol):
+    """Ns >= Np: S = A^T A (tensor-core modes through qgx_transpose) and the shifted solve
+    against the FP64 oracle (stated per mode: the operand rounding of the Gram)."""
+    import quantax_gb300 as qtx
+    opt = _rbm_opt(qtx.optimizer.auto_shift_eig(ashift=1e-3), gram=gram)
+    rng = np.random.default_rng(8)
+    A = (rng.normal(size=(600, 144)) / 25.0).astype(np.float32)
+    b = rng.normal(size=600)
+    x = opt.solve(torch.as_tensor(A).cuda(), torch.as_tensor(b).cuda()).cpu().numpy()
+    ref = osr.lstsq_shift(A.astype(np.float64), b, rshift=1e-6, ashift=1e-3)
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < tol
 
 
 def test_mixed_solve_converges_ill_conditioned(cuda):

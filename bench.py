@@ -33,7 +33,14 @@ UNIT = "SR_steps/s"
 WORKLOAD = dict(workload="tfim_chain64_rbm256_minsr8192", lattice="Chain(64) PBC", hamiltonian="Ising(h=1, J=1)",
                 model="RBM_Dense(features=256)", nparams=16640, sampler="LocalFlip", chains=8192,
                 proposals_per_sweep=64, thermal_proposals=640, solver="minnorm_shift_eig(ashift=1e-4)",
-                gram="fp32", l2="Obar (545 MB) and T (537 MB) exceed the 129 MB L2 every step")
+                l2="Obar (545 MB) and T (537 MB) exceed the 129 MB L2 every step")
+
+
+# DRAM bytes per Gram launch at the bench's shapes, from
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum --clock-control none \
+#       -k regex:gram_tc -c 3 python -m quantax_gb300.kernel_bench gram --mode 3xtf32 --rows 8192 --k 16640 --reps 1
+# (mean of three launches: 6.98 GB read, 0.51 GB written; the operand is re-read from DRAM ~13x)
+GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 7.49e9}
 
 
 def peaks():
@@ -362,7 +369,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--gram", default="fp32", choices=["fp32", "tf32", "bf16", "3xtf32"])
+    ap.add_argument("--gram", default="3xtf32", choices=["fp32", "tf32", "bf16", "3xtf32"],
+                    help="plain-path Gram: split-TF32 on the tensor cores is FP32-class (accumulation error "
+                         "6.6e-6 against 8.2e-5 for fp32 on the CUDA cores)")
     ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
@@ -432,13 +441,17 @@ def main():
         t_gram = phases.get("gram", float("nan")) / 1000.0
         achieved = syrk_flop / t_gram / 1e12
         rate = {"bf16": 1.0, "tf32": 0.5, "3xtf32": 0.5 / 3.0, "fp32": None}[args.gram]
+        traffic = GRAM_TRAFFIC_BYTES.get((args.workload, args.gram))
         roof = {"kernel": f"qgx_gram {args.gram} (T = Obar Obar^T)", "bound": "tensor", "achieved": achieved,
                 "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": f"bf16 dense, {src}",
                 "mode_peak": None if rate is None else bf16 * rate,
                 "frac_of_mode_peak": None if rate is None else achieved / (bf16 * rate),
-                "traffic": None, "algorithmic": f"Ns(Ns+1)Np = {syrk_flop:.3e} FLOP per launch (symmetric rank-k)",
-                "note": ("fp32 runs on the FP32 SIMT pipes (its roofline is the FP32 FMA rate); the FP64 cuSOLVER "
-                         "factorisation dominates the plain step")}
+                "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
+                "algorithmic": f"Ns(Ns+1)Np = {syrk_flop:.3e} FLOP per launch (symmetric rank-k); operand "
+                               f"{ns * npar * 4:.3e} B read, T {ns * ns * 8:.3e} B written",
+                "note": ("the tensor-core Gram is our dominant kernel; cuSOLVER's FP64 factorisation (a library "
+                         "kernel) dominates the plain step. 3xtf32: each product is hi*hi + hi*lo + lo*hi, so its "
+                         "mode peak is a third of the TF32 rate")}
         elapsed = plain["elapsed"]
         line = {
             "metric": METRIC, "value": world * args.steps / elapsed, "unit": UNIT, "n_gpus": world,

@@ -513,9 +513,13 @@ __global__ void __launch_bounds__(NT)
     const float f = centred ? (float)sqrt((r ? r[c] : 1.0) / (double)ns) : 1.0f;
     float* row = O + c * ldo;
     if (vec4) {
-      for (int64_t e4 = lane; e4 < mn / 4; e4 += 32) {
-        const int64_t e = 4 * e4;
-        const int i = (int)(e / n), j = (int)(e % n);
+      // 32-bit indices (a row has m n < 2^31 entries); unrolled so that several loads of
+      // the column means are in flight per lane
+      const int mn32 = (int)mn;
+#pragma unroll 4
+      for (int e4 = lane; e4 < mn32 / 4; e4 += 32) {
+        const int e = 4 * e4;
+        const int i = e / n, j = e - i * n;
         const float ti = tb[i];
         const uint32_t bits = sp[j >> 5] >> (j & 31);  // j % 4 == 0 so j..j+3 share a word
         float4 v = make_float4((bits & 1u) ? ti : -ti, (bits & 2u) ? ti : -ti, (bits & 4u) ? ti : -ti,

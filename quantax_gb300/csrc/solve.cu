@@ -13,6 +13,12 @@
 #include "qgx_common.cuh"
 
 namespace qgx {
+
+int64_t trsv_chol_workspace_bytes(int64_t n);
+int trsv_chol_prepare(const float* L, int64_t n, void* work, cudaStream_t st);
+int trsv_chol_apply(const float* L, int64_t n, float* v, void* work, uint32_t epoch, cudaStream_t st);
+int trsv_chol_error(int64_t n, void* work, int* host_err, cudaStream_t st);
+
 namespace {
 
 constexpr int kMaxDevices = 64;
@@ -350,6 +356,7 @@ struct SolveWs {
   float* r32;     // n
   double* r;      // n
   double* acc;    // 16: iteration scalars and residual norms
+  void* trsv;     // SHIFT_MIXED: the triangular solves' diagonal-block inverses and flags
 };
 
 // The FP32 factorisation of SHIFT_MIXED runs with cuSOLVER's BF16x9 emulation of FP32
@@ -414,6 +421,7 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   const int64_t o_r32 = take(mixed ? n * 4 : 0);
   const int64_t o_r = take(mixed ? n * 8 : 0);
   const int64_t o_acc = take(mixed ? 16 * 8 : 0);
+  const int64_t o_trsv = take(mixed ? trsv_chol_workspace_bytes(n) : 0);
   *need = off;
   if (!base) return QGX_OK;
   if (bytes < off) return QGX_ERR_ARG;
@@ -432,6 +440,7 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   ws->r32 = reinterpret_cast<float*>(b + o_r32);
   ws->r = reinterpret_cast<double*>(b + o_r);
   ws->acc = reinterpret_cast<double*>(b + o_acc);
+  ws->trsv = b + o_trsv;
   if (hb > g_host_ws.size()) g_host_ws.resize(hb);
   return QGX_OK;
 }
@@ -516,11 +525,13 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     double* qv = ws.inv; // T p
     const unsigned gr = (unsigned)((n * 32 + 255) / 256);
     const unsigned gd = (unsigned)std::min<int64_t>((n + 255) / 256, kDotBlocks);
-    auto precondition = [&]() -> int {  // r32 <- M^-1 r32
-      if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.r32, n,
-                           ws.info + 1) != CUSOLVER_STATUS_SUCCESS)
-        return QGX_ERR_SOLVER;
-      return QGX_OK;
+    // r32 <- M^-1 r32 = L^-T L^-1 r32 with the decoupled block triangular solves (trsv.cu)
+    ++g_kernels;
+    if ((rc = trsv_chol_prepare(ws.t32, n, ws.trsv, st)) != QGX_OK) return rc;
+    uint32_t epoch = 0;
+    auto precondition = [&]() -> int {
+      g_kernels += 2;
+      return trsv_chol_apply(ws.t32, n, ws.r32, ws.trsv, ++epoch, st);
     };
     ++g_kernels;
     cg_init_kernel<<<gd, 256, 0, st>>>(ws.y, ws.r, ws.r32, b, n);
@@ -537,6 +548,7 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gd, scal, 0);
     if ((rc = launch_status()) != QGX_OK) return rc;
     double host[2];
+    int trsv_err = 0;
     for (int it = 0; it < kCgMaxIters; ++it) {
       ++g_kernels;
       symv_dot_kernel<<<gr, 256, 0, st>>>(T, n, pv, qv, ws.part);
@@ -547,7 +559,9 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
       ++g_kernels;
       reduce_step_kernel<<<1, 256, 0, st>>>(ws.part, (int)gd, scal, 2);
       QGX_CHECK_CUDA(cudaMemcpyAsync(host, scal + kScalRR, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      if ((rc = trsv_chol_error(n, ws.trsv, &trsv_err, st)) != QGX_OK) return rc;
       QGX_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (trsv_err) break;  // a triangular solve timed out: the residual check below fails
       if (!(host[0] > kCgTol * kCgTol * host[1])) break;  // converged (or NaN: caught by the check below)
       if ((rc = precondition()) != QGX_OK) return rc;
       ++g_kernels;
@@ -564,6 +578,10 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     residual_kernel<<<gr, 256, 0, st>>>(T, n, ws.y, b, ws.r, last);
     ++g_kernels;
     refine_check_kernel<<<1, 1, 0, st>>>(last, ws.info, dinfo, kRefineTol);
+    if (trsv_err) {  // a triangular solve timed out
+      ++g_kernels;
+      set_int_kernel<<<1, 1, 0, st>>>(dinfo, -1);
+    }
     return launch_status();
   }
   if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.w,

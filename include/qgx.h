@@ -110,6 +110,8 @@ int qgx_operator_diag(const qgx_operator_t* op, const uint32_t* spins, int64_t n
                       double* out, qgx_stream_t stream);
 
 /* ---- RBM_Dense (quantax/model/shallow_nets.py:35-126) ------------------------------- */
+/* Supported: n <= 1024 sites, m <= 1024 hidden units (padded internally to 128, 256, 384,
+ * 512 or 1024 with zero weights). */
 /* Number of floats of the per-parameter-set table used by every RBM kernel. */
 int64_t qgx_rbm_table_floats(int32_t n, int32_t m);
 /* Build the table from W (m x n row-major, eqx Linear layout), b (m) and the optional

@@ -33,7 +33,12 @@ struct RbmTable {
   const float* a;   // N (zeros without a visible bias)
 };
 
-__host__ __device__ inline int padded_m(int m) { return (m + 127) / 128 * 128; }
+// hidden units padded to a compiled width: 128, 256, 384, 512 or 1024 (padded units have
+// zero weights and bias, so cosh = 1, sinh = 0 and they leave every ratio unchanged)
+__host__ __device__ inline int padded_m(int m) {
+  const int p = (m + 127) / 128 * 128;
+  return (p > 512 && p <= 1024) ? 1024 : p;
+}
 
 // floats of the table, rounded to a multiple of 4 so staging can use 16-byte copies
 __host__ __device__ inline int64_t table_floats(int n, int m) {

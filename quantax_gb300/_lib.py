@@ -124,7 +124,7 @@ def _kernels(name, args):
     if name in ("qgx_minsr_solve", "qgx_sr_solve"):
         return int(lib().qgx_last_solve_kernels())
     if name == "qgx_resconv_sweep":
-        return 1 + 3 * int(args[10])
+        return 2 + 3 * int(args[10])  # step base, forward, then propose / forward / accept per step
     return KERNELS_PER_CALL.get(name, 0)
 
 

@@ -15,6 +15,9 @@
 // one (sample, site) pair, so every weight load is a warp-wide broadcast.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "qgx_common.cuh"
 #include "qgx_resconv.cuh"
@@ -195,10 +198,12 @@ __global__ void __launch_bounds__(kFwdThreads)
 // proposal of chain c at draw t: site i uniform among the hopping spins, j uniform in the
 // padded neighbour row of i (-1: no move); writes the swapped configuration and changed flag
 __global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* __restrict__ prop,
-                                  int8_t* __restrict__ changed, int64_t ns, int n, uint64_t seed, uint64_t step,
-                                  const int32_t* __restrict__ nbr, int z, int hop) {
+                                  int8_t* __restrict__ changed, int64_t ns, int n, uint64_t seed,
+                                  const uint64_t* __restrict__ step_base, int t, const int32_t* __restrict__ nbr, int z,
+                                  int hop) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ns) return;
+  const uint64_t step = *step_base + (uint64_t)t;
   const int nw = words_for(n);
   uint32_t w[8];
   for (int k = 0; k < nw; ++k) w[k] = spins[c * nw + k];
@@ -211,9 +216,10 @@ __global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* 
 __global__ void rc_accept_kernel(uint32_t* __restrict__ spins, float2* __restrict__ lp,
                                  const uint32_t* __restrict__ prop, const float2* __restrict__ lp_prop,
                                  const int8_t* __restrict__ changed, int32_t* __restrict__ accepts, int64_t ns, int n,
-                                 uint64_t seed, uint64_t step, float reweight) {
+                                 uint64_t seed, const uint64_t* __restrict__ step_base, int t, float reweight) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ns) return;
+  const uint64_t step = *step_base + (uint64_t)t;
   const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
   const float rhs = log1pf(-unit_float(r.y));
   if (changed[c] && reweight * (lp_prop[c].x - lp[c].x) > rhs) {
@@ -297,6 +303,8 @@ __global__ void rc_conn_write_kernel(qgx_operator_t op, const uint32_t* __restri
 }
 
 // E_loc(s) = diag(s) + sum_k elem_k exp(log psi(s'_k) - log psi(s)), complex
+__global__ void rc_set_step_kernel(uint64_t* __restrict__ step_base, uint64_t step0) { *step_base = step0; }
+
 __global__ void rc_eloc_reduce_kernel(qgx_operator_t op, const uint32_t* __restrict__ spins, int64_t ns, int n,
                                       const float2* __restrict__ lp, const int64_t* __restrict__ offsets,
                                       const double* __restrict__ elem, const float2* __restrict__ lp_conn,
@@ -638,6 +646,32 @@ int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, 
   }
 }
 
+// ---- sweep graphs ----------------------------------------------------------------------
+// A sweep is 1 + 3 nsteps launches (forward, then propose / forward / accept per step). The
+// launch sequence is captured once per set of buffers and sizes into a CUDA graph (on a
+// private stream, relaxed capture mode) and replayed on the caller's stream; the Philox step
+// base lives in the workspace, so one graph serves every starting step.
+struct SweepKey {
+  const void *table, *spins, *lp, *acc, *nbr, *ws;
+  int64_t ns;
+  int nsteps, L, B, C, cplx, prec, z, hop, device;
+  uint64_t seed;
+  float reweight;
+  bool operator==(const SweepKey& o) const { return std::memcmp(this, &o, sizeof(SweepKey)) == 0; }
+};
+
+struct SweepGraph {
+  SweepKey key;
+  cudaGraphExec_t exec;
+  uint64_t last_use;
+};
+
+constexpr int kMaxSweepGraphs = 32;
+std::mutex g_graph_mutex;
+std::vector<SweepGraph> g_graphs;
+uint64_t g_graph_clock = 0;
+cudaStream_t g_capture_stream[64] = {};
+
 bool valid_net(int L, int B, int C, int cplx) {
   return L >= 3 && L * L <= kMaxSitesConv && B >= 1 && B <= 64 && (C == 4 || C == 8 || C == 12 || C == 16) &&
          (!cplx || C % 2 == 0);
@@ -686,7 +720,7 @@ int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t 
 int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns) {
   if (L < 1 || ns < 1) return 0;
   const int nw = words_for(L * L);
-  return al256(ns * nw * 4) + al256(ns * 8) + al256(ns);
+  return al256(ns * nw * 4) + al256(ns * 8) + al256(ns) + al256(8);  // + the Philox step base
 }
 
 int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
@@ -707,18 +741,79 @@ int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t ch
   uint32_t* prop = reinterpret_cast<uint32_t*>(ws);
   float2* lp_prop = reinterpret_cast<float2*>(ws + al256(ns * nw * 4));
   int8_t* changed = reinterpret_cast<int8_t*>(ws + al256(ns * nw * 4) + al256(ns * 8));
+  uint64_t* step_base = reinterpret_cast<uint64_t*>(ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns));
   float2* lp = reinterpret_cast<float2*>(log_psi);
-  int rc = launch_forward(table, net, spins, ns, nullptr, lp, st);
-  if (rc != QGX_OK) return rc;
-  if (accepts) QGX_CHECK_CUDA(cudaMemsetAsync(accepts, 0, ns * sizeof(int32_t), st));
   const unsigned g = (unsigned)((ns + 127) / 128);
-  for (int t = 0; t < nsteps; ++t) {
-    rc_propose_kernel<<<g, 128, 0, st>>>(spins, prop, changed, ns, net.N, seed, step0 + t, nbr, z, hop);
-    if ((rc = launch_forward(table, net, prop, ns, nullptr, lp_prop, st)) != QGX_OK) return rc;
-    rc_accept_kernel<<<g, 128, 0, st>>>(spins, lp, prop, lp_prop, changed, accepts, ns, net.N, seed, step0 + t,
-                                        reweight);
+  // the launch sequence of the sweep (recorded into the graph)
+  auto record = [&](cudaStream_t s) -> int {
+    int rc = launch_forward(table, net, spins, ns, nullptr, lp, s);
+    if (rc != QGX_OK) return rc;
+    if (accepts) QGX_CHECK_CUDA(cudaMemsetAsync(accepts, 0, ns * sizeof(int32_t), s));
+    for (int t = 0; t < nsteps; ++t) {
+      rc_propose_kernel<<<g, 128, 0, s>>>(spins, prop, changed, ns, net.N, seed, step_base, t, nbr, z, hop);
+      if ((rc = launch_forward(table, net, prop, ns, nullptr, lp_prop, s)) != QGX_OK) return rc;
+      rc_accept_kernel<<<g, 128, 0, s>>>(spins, lp, prop, lp_prop, changed, accepts, ns, net.N, seed, step_base, t,
+                                         reweight);
+    }
+    return launch_status();
+  };
+  int dev = 0;
+  QGX_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return QGX_ERR_UNSUPPORTED;
+  rc_set_step_kernel<<<1, 1, 0, st>>>(step_base, step0);
+  QGX_CHECK_CUDA(cudaGetLastError());
+  SweepKey key;
+  std::memset(&key, 0, sizeof(key));
+  key.table = table;
+  key.spins = spins;
+  key.lp = log_psi;
+  key.acc = accepts;
+  key.nbr = nbr;
+  key.ws = workspace;
+  key.ns = ns;
+  key.nsteps = nsteps;
+  key.L = L;
+  key.B = nblocks;
+  key.C = channels;
+  key.cplx = complex_out != 0;
+  key.prec = conv_precision;
+  key.z = z;
+  key.hop = hop;
+  key.device = dev;
+  key.seed = seed;
+  key.reweight = reweight;
+  std::lock_guard<std::mutex> lock(g_graph_mutex);
+  SweepGraph* hit = nullptr;
+  for (auto& e : g_graphs)
+    if (e.key == key) hit = &e;
+  if (!hit) {
+    if (!g_capture_stream[dev]) QGX_CHECK_CUDA(cudaStreamCreateWithFlags(&g_capture_stream[dev], cudaStreamNonBlocking));
+    cudaStream_t cs = g_capture_stream[dev];
+    QGX_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+    const int rc = record(cs);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+    if (rc != QGX_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    QGX_CHECK_CUDA(ce);
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    QGX_CHECK_CUDA(ie);
+    if ((int)g_graphs.size() >= kMaxSweepGraphs) {  // evict the least recently used
+      auto lru = std::min_element(g_graphs.begin(), g_graphs.end(),
+                                  [](const SweepGraph& a, const SweepGraph& b) { return a.last_use < b.last_use; });
+      cudaGraphExecDestroy(lru->exec);
+      g_graphs.erase(lru);
+    }
+    g_graphs.push_back(SweepGraph{key, exec, 0});
+    hit = &g_graphs.back();
   }
-  return launch_status();
+  hit->last_use = ++g_graph_clock;
+  QGX_CHECK_CUDA(cudaGraphLaunch(hit->exec, st));
+  return QGX_OK;
 }
 
 int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn) {

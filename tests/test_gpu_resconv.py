@@ -155,3 +155,32 @@ def test_resconv_sr_step_matches_oracle(cuda):
         state.update(torch.as_tensor(step).cuda() * 1e-2)
     finally:
         qtx.set_default_dtype(np.float64)
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_resconv_sweep_graph_replay_equals_one_sweep(cuda, prec):
+    """A sweep is captured once into a CUDA graph and replayed; the Philox step base is read
+    from the workspace, so two replays starting at steps 0 and 12 give exactly the 24-step
+    sweep (configurations, log psi and the accepts of each part)."""
+    from quantax_gb300 import _lib as Lb
+    L, B, Cc, ns = 4, 2, 8, 48
+    net = Net(L, B, Cc, True, seed=6, bias_std=0.3)
+    nbr = torch.as_tensor(lattice.neighbor_table((L, L), 1)).cuda()
+    s0 = _pack(metropolis.init_fixed_up(ns, 16, 8, 11))
+
+    def sweep(packed, nsteps, step0, ws):
+        lp = torch.empty((ns, 2), dtype=torch.float32, device="cuda")
+        acc = torch.empty(ns, dtype=torch.int32, device="cuda")
+        Lb.call("qgx_resconv_sweep", Lb.ptr(net.table), L, B, Cc, 1, prec, Lb.ptr(packed), Lb.ptr(lp), Lb.ptr(acc),
+                ns, nsteps, 5, step0, 2.0, Lb.ptr(nbr), nbr.shape[1], 1, Lb.ptr(ws), ws.numel(), Lb.stream_ptr())
+        return lp, acc
+
+    ws = torch.empty(Lb.lib().qgx_resconv_sweep_workspace_bytes(L, ns), dtype=torch.uint8, device="cuda")
+    one = s0.clone()
+    lp1, acc1 = sweep(one, 24, 0, ws)
+    two = s0.clone()
+    _, a = sweep(two, 12, 0, ws)
+    lp2, b = sweep(two, 12, 12, ws)  # same buffers and sizes: the same graph, another step base
+    assert torch.equal(one, two)
+    assert torch.equal(lp1, lp2)
+    assert torch.equal(acc1, a + b)

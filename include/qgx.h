@@ -244,6 +244,14 @@ int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const doub
                        double* omean, void* workspace, int64_t workspace_bytes,
                        qgx_stream_t stream);
 
+/* ---- momentum variants of SR (SPRING, MARCH, AdamSR: quantax/optimizer/sr.py:198-429) --- */
+/* y = A x for the FP32 Obar A (rows x cols, row stride lda floats), FP64 x and y. */
+int qgx_obar_matvec(const float* A, int64_t rows, int64_t cols, int64_t lda, const double* x,
+                    double* y, qgx_stream_t stream);
+/* A[:, j] *= s[j] in place (FP64 scale factors). */
+int qgx_scale_columns(float* A, int64_t rows, int64_t cols, int64_t lda, const double* s,
+                      qgx_stream_t stream);
+
 /* ---- Gram matrices (quantax/optimizer/solver.py:139, 157) ---------------------------- */
 /* T = A A^T for A (rows x k, row stride lda floats), written as FP64 rows x rows
  * (full symmetric matrix, row stride ldt). mode = QGX_GRAM_*. */

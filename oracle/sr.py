@@ -112,3 +112,38 @@ def update(params, step, dtype=np.float32):
         return params, False
     p = np.asarray(params, dtype=dtype)
     return (p - np.real(step).astype(dtype)).astype(np.float64), True
+
+
+# ---- momentum variants (quantax/optimizer/sr.py:198-429), on the stacked real A and b ----
+def spring_step(A, b, last, mu, solver):
+    b = b - mu * (A @ last)
+    step = solver(A, b) + mu * last
+    return step
+
+
+def march_step(A, b, last, V_state, t, mu, beta, solver, a_dtype=np.float32):
+    """One MARCH solve (t already incremented); A is scaled column by column and rounded to
+    a_dtype, as the device stores Obar. Returns (step, new V_state)."""
+    b = b - mu * (A @ last)
+    if np.allclose(V_state, 0):
+        V = np.ones_like(V_state)
+    else:
+        V = (V_state / (1 - beta ** t)) ** 0.25 + 1e-8
+    As = (A * (1.0 / V)[None, :]).astype(a_dtype).astype(np.float64)
+    step = solver(As, b) / V + mu * last
+    V_state = beta * V_state + (1 - beta) * np.abs(step - last) ** 2
+    return step, V_state
+
+
+def adamsr_step(A, b, m, v, t, mu, beta, solver, a_dtype=np.float32):
+    """One AdamSR step (t already incremented). Returns (step, m, v)."""
+    g = solver(A, b)
+    m = mu * m + (1 - mu) * g
+    v = beta * v + (1 - beta) * np.abs(g) ** 2
+    mh = m / (1 - mu ** t)
+    vh = v / (1 - beta ** t)
+    V = vh ** 0.25 + 1e-8
+    b = b - A @ mh
+    As = (A * (1.0 / V)[None, :]).astype(a_dtype).astype(np.float64)
+    step = solver(As, b) / V + mh
+    return step, m, v

@@ -274,11 +274,55 @@ __global__ void update_kernel(float* __restrict__ params, const double* __restri
 
 inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// y = A x: A FP32 (rows x cols, lda), x and y FP64; one warp per row, FP64 accumulation in a
+// fixed order (the momentum term Obar @ step of SPRING / MARCH / AdamSR, sr.py:244, 315, 415)
+__global__ void obar_matvec_kernel(const float* __restrict__ A, int64_t rows, int64_t cols, int64_t lda,
+                                   const double* __restrict__ x, double* __restrict__ y) {
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  const float* a = A + row * lda;
+  double s = 0.0;
+  for (int64_t j = lane; j < cols; j += 32) s = fma((double)a[j], x[j], s);
+  s = warp_sum(s);
+  if (lane == 0) y[row] = s;
+}
+
+// A[:, j] <- A[:, j] * s_j in place (MARCH / AdamSR divide Obar by V, sr.py:323, 418)
+__global__ void scale_columns_kernel(float* __restrict__ A, int64_t rows, int64_t cols, int64_t lda,
+                                     const double* __restrict__ s) {
+  const int64_t row = blockIdx.y;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cols; j += (int64_t)gridDim.x * blockDim.x)
+    A[row * lda + j] = (float)((double)A[row * lda + j] * s[j]);
+}
+
 }  // namespace qgx
 
 using namespace qgx;
 
 extern "C" {
+
+int qgx_obar_matvec(const float* A, int64_t rows, int64_t cols, int64_t lda, const double* x, double* y,
+                    qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows >= 0 && cols >= 0 && lda >= cols);
+  if (rows == 0) return QGX_OK;
+  QGX_CHECK_ARG(A && x && y);
+  obar_matvec_kernel<<<blocks_for(rows * 32, 256), 256, 0, as_cuda(stream)>>>(A, rows, cols, lda, x, y);
+  return launch_status();
+}
+
+int qgx_scale_columns(float* A, int64_t rows, int64_t cols, int64_t lda, const double* s, qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows >= 0 && cols >= 0 && lda >= cols);
+  if (rows == 0 || cols == 0) return QGX_OK;
+  QGX_CHECK_ARG(A && s);
+  cudaStream_t st = as_cuda(stream);
+  const unsigned gx = (unsigned)std::min<int64_t>((cols + 255) / 256, 64);
+  for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
+    const int64_t rr = std::min<int64_t>(65535, rows - r0);
+    scale_columns_kernel<<<dim3(gx, (unsigned)rr), 256, 0, st>>>(A + r0 * lda, rr, cols, lda, s);
+  }
+  return launch_status();
+}
 
 int qgx_abi_version(void) { return 1; }
 

@@ -241,4 +241,128 @@ class SR(QNGD):
         return ebar
 
 
+class _MomentumSR(SR):
+    """Shared pieces of the momentum variants: Obar @ x and the in-place column scaling run on
+    the device (qgx_obar_matvec / qgx_scale_columns); the O(Np) bookkeeping is elementwise."""
+
+    _saved: tuple = ()
+
+    def __init__(self, state, hamiltonian, imag_time, solver, gram, file):
+        super().__init__(state, hamiltonian, imag_time, solver, gram)
+        self._dev = state.params.device
+        if file is not None:
+            self.load(file)
+
+    def _zeros(self):
+        return torch.zeros(self._state.nparams, dtype=torch.float64, device=self._dev)
+
+    def _obar_dot(self, Obar: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+        rows, np_ = Obar.shape
+        y = torch.empty(rows, dtype=torch.float64, device=Obar.device)
+        _lib.call("qgx_obar_matvec", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(x.contiguous()), _lib.ptr(y),
+                  _lib.stream_ptr())
+        return y
+
+    def _scale_columns(self, Obar: torch.Tensor, s: torch.Tensor) -> None:
+        rows, np_ = Obar.shape
+        _lib.call("qgx_scale_columns", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(s.contiguous()),
+                  _lib.stream_ptr())
+
+    def save(self, file) -> None:
+        """The optimizer's internal quantities (numpy .npz)."""
+        import numpy as np
+        vals = {k: (getattr(self, k).cpu().numpy() if torch.is_tensor(getattr(self, k)) else getattr(self, k))
+                for k in self._saved}
+        np.savez(file, **vals)
+
+    def load(self, file) -> None:
+        import numpy as np
+        with np.load(file) as d:
+            for k in self._saved:
+                v = d[k]
+                setattr(self, k, torch.as_tensor(v, device=self._dev) if v.ndim else v.item())
+
+
+class SPRING(_MomentumSR):
+    """SPRING: SR with momentum (sr.py:198-262). Ebar -= mu Obar @ last_step before the solve,
+    step += mu last_step after it. Obar and Ebar are the stacked real matrix / vector of
+    QNGD.solve; for a real_to_complex state the correction is the same row by row."""
+
+    _saved = ("_mu", "_last_step")
+
+    def __init__(self, state, hamiltonian, imag_time: bool = True, solver: Optional[Solver] = None,
+                 mu: float = 0.9, file=None, gram: str = "fp32"):
+        self._mu = float(mu)
+        self._last_step = None
+        super().__init__(state, hamiltonian, imag_time, solver, gram, file)
+        if self._last_step is None:
+            self._last_step = self._zeros()
+
+    def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
+        Ebar = Ebar.to(torch.float64) - self._mu * self._obar_dot(Obar, self._last_step)
+        step = super().solve(Obar, Ebar)
+        step = step + self._mu * self._last_step
+        self._last_step = step
+        return step
+
+
+class MARCH(_MomentumSR):
+    """MARCH: SR with first and second order momentum (sr.py:265-351). Obar is divided by
+    V = (V_t / (1 - beta^t))^(1/4) + 1e-8 column by column, in place."""
+
+    _saved = ("_mu", "_beta", "_last_step", "_V", "_t")
+
+    def __init__(self, state, hamiltonian, imag_time: bool = True, solver: Optional[Solver] = None,
+                 mu: float = 0.95, beta: float = 0.995, file=None, gram: str = "fp32"):
+        self._mu, self._beta = float(mu), float(beta)
+        self._last_step = self._V = None
+        self._t = 0
+        super().__init__(state, hamiltonian, imag_time, solver, gram, file)
+        if self._last_step is None:
+            self._last_step, self._V = self._zeros(), self._zeros()
+
+    def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
+        self._t += 1
+        Ebar = Ebar.to(torch.float64) - self._mu * self._obar_dot(Obar, self._last_step)
+        if bool(torch.allclose(self._V, torch.zeros_like(self._V))):
+            V = torch.ones_like(self._V)
+        else:
+            V = (self._V / (1.0 - self._beta ** self._t)) ** 0.25 + 1e-8
+        self._scale_columns(Obar, 1.0 / V)
+        step = super().solve(Obar, Ebar)
+        step = step / V + self._mu * self._last_step
+        self._V = self._beta * self._V + (1.0 - self._beta) * (step - self._last_step) ** 2
+        self._last_step = step
+        return step
+
+
+class AdamSR(_MomentumSR):
+    """AdamSR: two SR solves per step with Adam-style moments (sr.py:354-429)."""
+
+    _saved = ("_mu", "_beta", "_m", "_v", "_t")
+
+    def __init__(self, state, hamiltonian, imag_time: bool = True, solver: Optional[Solver] = None,
+                 mu: float = 0.95, beta: float = 0.995, file=None, gram: str = "fp32"):
+        self._mu, self._beta = float(mu), float(beta)
+        self._m = self._v = None
+        self._t = 0
+        super().__init__(state, hamiltonian, imag_time, solver, gram, file)
+        if self._m is None:
+            self._m, self._v = self._zeros(), self._zeros()
+
+    def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
+        self._t += 1
+        Ebar = Ebar.to(torch.float64)
+        g = super().solve(Obar, Ebar)
+        self._m = self._mu * self._m + (1.0 - self._mu) * g
+        self._v = self._beta * self._v + (1.0 - self._beta) * g ** 2
+        m = self._m / (1.0 - self._mu ** self._t)
+        v = self._v / (1.0 - self._beta ** self._t)
+        V = v ** 0.25 + 1e-8
+        Ebar = Ebar - self._obar_dot(Obar, m)
+        self._scale_columns(Obar, 1.0 / V)
+        step = super().solve(Obar, Ebar)
+        return step / V + m
+
+
 MinSR = SR

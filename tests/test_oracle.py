@@ -127,3 +127,22 @@ def test_golden_oracle_fixture_stable():
     s, lp, st = metropolis.sweep(net.log_psi, np.array(c["s0"], np.int8), c["nsteps"], seed=c["seed"])
     assert s.tolist() == c["spins"]
     np.testing.assert_allclose(lp, c["log_psi"], rtol=1e-12)
+
+
+def test_momentum_sr_oracle_limits():
+    """The momentum restatements reduce to plain SR where the reference's algebra says so:
+    SPRING with mu = 0; MARCH's first step (V = 0 -> no scaling, no momentum yet); AdamSR's
+    first step is g + (correction solve) with m_hat = g, so Ebar - Obar m_hat is orthogonal to
+    the range used by the second minimum-norm solve and the step equals g for an exact solver."""
+    rng = np.random.default_rng(4)
+    A = rng.normal(size=(30, 80)) / 9.0
+    b = rng.normal(size=30)
+    solver = lambda M, v: sr.minnorm_shift(M, v, rshift=0.0, ashift=1e-12)
+    g = solver(A, b)
+    np.testing.assert_allclose(sr.spring_step(A, b, rng.normal(size=80), 0.0, solver), g, rtol=1e-12, atol=1e-12)
+    x, V = sr.march_step(A, b, np.zeros(80), np.zeros(80), 1, 0.95, 0.995, solver, a_dtype=np.float64)
+    np.testing.assert_allclose(x, g, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(V, 0.005 * g ** 2, rtol=1e-12)
+    x, m, v = sr.adamsr_step(A, b, np.zeros(80), np.zeros(80), 1, 0.95, 0.995, solver, a_dtype=np.float64)
+    np.testing.assert_allclose(m, 0.05 * g, rtol=1e-12)
+    np.testing.assert_allclose(x, g, rtol=1e-6, atol=1e-6 * np.abs(g).max())

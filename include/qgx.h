@@ -306,6 +306,19 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda,
                  double rtol, double atol, double tol_snr, double* x, int32_t* info,
                  void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
 
+/* Real-time evolution's S-path (quantax/optimizer/time_evol.py:55-134):
+ * y = A^T b (cols doubles), FP64 accumulation in a fixed order; workspace from
+ * qgx_obar_rmatvec_workspace_bytes. */
+int qgx_obar_rmatvec_workspace_bytes(int64_t rows, int64_t cols, int64_t* bytes);
+int qgx_obar_rmatvec(const float* A, int64_t rows, int64_t cols, int64_t lda, const double* b,
+                     double* y, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+/* x = S^-1 f for a symmetric S (n x n FP64, overwritten): PINV is pinvh_solve
+ * (solver.py:104-111, eigh with the soft inverse), SHIFT the shifted Cholesky solve.
+ * Workspace: qgx_solve_workspace_bytes(n, 1, method). */
+int qgx_sym_solve(double* S, int64_t n, const double* f, int32_t method, double rshift,
+                  double ashift, double rtol, double atol, double* x, int32_t* info,
+                  void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+
 /* ---- parameter update (quantax/state/variational.py:558-579) ------------------------- */
 /* params <- params - step when every step entry is finite; otherwise params are left
  * unchanged and *flag (device int) is set to 1 (else 0). */

@@ -97,13 +97,36 @@ def auto(A, b, kind="pinv", **kw):
     return minnorm_shift(A, b, **kw) if A.shape[0] < A.shape[1] else lstsq_shift(A, b, **kw)
 
 
-def solve(Obar, Ebar, solver, complex_out=False):
+def solve(Obar, Ebar, solver, complex_out=False, imag_time=True):
+    """QNGD.solve (quantax/optimizer/sr.py:90-113) for states with real parameters. Real time:
+    complex-output states solve with [-Im; Re] Ebar; real ones get Ebar * 1j, whose purely
+    imaginary solution casts to a zero real step."""
     if complex_out:
         A = np.concatenate([Obar.real, Obar.imag], axis=0)
-        b = np.concatenate([Ebar.real, Ebar.imag])
+        b = np.concatenate([Ebar.real, Ebar.imag]) if imag_time else np.concatenate([-Ebar.imag, Ebar.real])
     else:
+        if not imag_time:
+            return np.zeros(Obar.shape[1])
         A, b = np.real(Obar), np.real(Ebar)
     return solver(A, b)
+
+
+def pinvh(H, b, rtol=None, atol=0.0):
+    """pinvh_solve (quantax/optimizer/solver.py:104-111): U diag(soft inverse) U^H b."""
+    lam, U = np.linalg.eigh(H)
+    return U @ (eigs_inv(lam, rtol, atol) * (U.conj().T @ b))
+
+
+def time_evol_sf(Obar, Ebar):
+    """TimeEvol.get_SF one-shot form (quantax/optimizer/time_evol.py:63-68)."""
+    return Obar.conj().T @ Obar, Obar.conj().T @ Ebar
+
+
+def time_evol_step(S, F, complex_out=True, solver=pinvh):
+    """TimeEvol.solve (quantax/optimizer/time_evol.py:113-128), real parameters."""
+    if not complex_out:
+        return np.zeros(S.shape[0])
+    return solver(S.real, -F.imag)
 
 
 def update(params, step, dtype=np.float32):

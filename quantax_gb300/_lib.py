@@ -97,6 +97,9 @@ SIGNATURES = {
     "qgx_transpose": (C.c_int, [vp, i64, i64, i64, vp, i64, i32, vp]),
     "qgx_obar_matvec": (C.c_int, [vp, i64, i64, i64, vp, vp, vp]),
     "qgx_scale_columns": (C.c_int, [vp, i64, i64, i64, vp, vp]),
+    "qgx_obar_rmatvec_workspace_bytes": (C.c_int, [i64, i64, vp]),
+    "qgx_obar_rmatvec": (C.c_int, [vp, i64, i64, i64, vp, vp, vp, i64, vp]),
+    "qgx_sym_solve": (C.c_int, [vp, i64, vp, i32, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_sr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_apply_update": (C.c_int, [vp, vp, i64, vp, vp]),
 }
@@ -117,13 +120,13 @@ KERNELS_PER_CALL = {
     "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_resconv_prepare": 2,
     "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6,
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
-    "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_apply_update": 2,
+    "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_apply_update": 2,
 }
 launch_count = 0
 
 
 def _kernels(name, args):
-    if name in ("qgx_minsr_solve", "qgx_sr_solve"):
+    if name in ("qgx_minsr_solve", "qgx_sr_solve", "qgx_sym_solve"):
         return int(lib().qgx_last_solve_kernels())
     if name == "qgx_scale_columns":
         return 1 + (int(args[1]) - 1) // 65535 if int(args[1]) > 0 and int(args[2]) > 0 else 0

@@ -654,4 +654,41 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
   return QGX_OK;
 }
 
+// F = A^T b with the solve's deterministic two-pass projection (TimeEvol.get_SF,
+// quantax/optimizer/time_evol.py:63-68)
+int qgx_obar_rmatvec_workspace_bytes(int64_t rows, int64_t cols, int64_t* bytes) {
+  QGX_CHECK_ARG(rows >= 0 && cols >= 0 && bytes);
+  *bytes = al256(std::max<int64_t>(1, (rows + kProjRows - 1) / kProjRows) * std::max<int64_t>(cols, 1) * 8);
+  return QGX_OK;
+}
+
+int qgx_obar_rmatvec(const float* A, int64_t rows, int64_t cols, int64_t lda, const double* b, double* y,
+                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows > 0 && cols > 0 && lda >= cols && A && b && y && workspace);
+  int64_t need = 0;
+  qgx_obar_rmatvec_workspace_bytes(rows, cols, &need);
+  QGX_CHECK_ARG(workspace_bytes >= need);
+  return project(A, rows, cols, lda, b, static_cast<double*>(workspace), y, as_cuda(stream));
+}
+
+// x = S^-1 f for a given symmetric S (n x n FP64, overwritten): pinvh_solve
+// (quantax/optimizer/solver.py:104-111) or the shifted Cholesky solve
+int qgx_sym_solve(double* S, int64_t n, const double* f, int32_t method, double rshift, double ashift, double rtol,
+                  double atol, double* x, int32_t* info, void* workspace, int64_t workspace_bytes,
+                  qgx_stream_t stream) {
+  QGX_CHECK_ARG(n > 0 && S && f && x && workspace);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  std::lock_guard<std::mutex> lock(g_solver_mutex);
+  g_kernels = 0;
+  SolveWs ws;
+  int64_t need = 0;
+  int rc = workspace_layout(n, 1, method, workspace, workspace_bytes, &ws, &need);
+  if (rc != QGX_OK) return rc;
+  cudaStream_t st = as_cuda(stream);
+  if ((rc = solve_gram(S, n, f, method, rshift, ashift, rtol, atol, 0.0, ws, info, st)) != QGX_OK) return rc;
+  QGX_CHECK_CUDA(cudaMemcpyAsync(x, ws.y, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  return QGX_OK;
+}
+
 }  // extern "C"

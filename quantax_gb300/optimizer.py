@@ -81,8 +81,6 @@ class QNGD:
     """Quantum natural gradient descent: solve Obar theta_dot = Ebar (sr.py:17-128)."""
 
     def __init__(self, state, imag_time: bool = True, solver: Optional[Solver] = None, gram: str = "fp32"):
-        if not imag_time:
-            raise NotImplementedError("real-time evolution is not implemented in quantax_gb300")
         self._state = state
         self._imag_time = imag_time
         self._solver = auto_pinv_eig() if solver is None else solver
@@ -121,12 +119,42 @@ class QNGD:
         obar, self._Omean = self._state.obar(samples, out[:, :np_])
         return obar
 
+    @property
+    def imag_time(self) -> bool:
+        return self._imag_time
+
+    def _gram_s(self, A: torch.Tensor) -> torch.Tensor:
+        """S = A^T A (np x np FP64) in the Gram mode of this optimizer."""
+        ns, np_ = A.shape
+        st = _lib.stream_ptr()
+        S = self._buffer("gram", (np_, np_), torch.float64)
+        if self._gram == _lib.GRAM_FP32:
+            _lib.call("qgx_gram_t", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(S), np_, st)
+        else:
+            # S = A^T A as the tensor-core Gram of A^T (rows padded for 16-byte TMA strides)
+            bf16 = self._gram == _lib.GRAM_BF16
+            At = self._buffer("obar_t", (np_, _round8(ns)), torch.bfloat16 if bf16 else torch.float32)
+            _lib.call("qgx_transpose", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(At), At.stride(0), int(bf16), st)
+            if bf16:
+                _lib.call("qgx_gram_tc", _lib.ptr(At), 1, np_, ns, At.stride(0), _lib.ptr(S), np_, None, st)
+            else:
+                _lib.call("qgx_gram", _lib.ptr(At), np_, ns, At.stride(0), _lib.ptr(S), np_, self._gram, st)
+        self._mark("gram")
+        return S
+
     def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
         """step = solver(Obar, Ebar) in FP64 (sr.py:90-113)."""
         # real_to_complex states arrive stacked: Obar rows [Re; Im], Ebar [Re; Im] (sr.py:99-105)
         A = Obar
         b = Ebar.to(torch.float64).contiguous()
         ns, np_ = A.shape
+        if not self._imag_time:
+            if self.vs_type != VS_TYPE.real_to_complex:
+                # Ebar * 1j makes the solution purely imaginary, and its cast to the real
+                # parameters keeps the real part: zero (sr.py:98-100, 111)
+                return torch.zeros(np_, dtype=torch.float64, device=A.device)
+            h = ns // 2
+            b = torch.cat([-b[h:], b[:h]])  # [-Im; Re] (sr.py:105)
         sv = self._solver
         method = _lib.SOLVE_SHIFT if sv.kind == "shift" else _lib.SOLVE_PINV
         rshift = _OBAR_RTOL if sv.rshift is None else sv.rshift
@@ -167,19 +195,7 @@ class QNGD:
                               _lib.SOLVE_SHIFT, 0.0, 0.0, rtol, sv.atol, sv.tol_snr, _lib.ptr(x), _lib.ptr(info),
                               _lib.ptr(ws), ws.numel(), st)
         else:
-            S = self._buffer("gram", (np_, np_), torch.float64)
-            if self._gram == _lib.GRAM_FP32:
-                _lib.call("qgx_gram_t", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(S), np_, st)
-            else:
-                # S = A^T A as the tensor-core Gram of A^T (rows padded for 16-byte TMA strides)
-                bf16 = self._gram == _lib.GRAM_BF16
-                At = self._buffer("obar_t", (np_, _round8(ns)), torch.bfloat16 if bf16 else torch.float32)
-                _lib.call("qgx_transpose", _lib.ptr(A), ns, np_, A.stride(0), _lib.ptr(At), At.stride(0), int(bf16), st)
-                if bf16:
-                    _lib.call("qgx_gram_tc", _lib.ptr(At), 1, np_, ns, At.stride(0), _lib.ptr(S), np_, None, st)
-                else:
-                    _lib.call("qgx_gram", _lib.ptr(At), np_, ns, At.stride(0), _lib.ptr(S), np_, self._gram, st)
-            self._mark("gram")
+            S = self._gram_s(A)
             _lib.call("qgx_solve_workspace_bytes", np_, ns, method, C.byref(nbytes))
             ws = self._state.workspace("solve", nbytes.value)
             _lib.call("qgx_sr_solve", _lib.ptr(S), np_, _lib.ptr(A), ns, A.stride(0), _lib.ptr(b), method, rshift,
@@ -258,14 +274,16 @@ class _MomentumSR(SR):
 
     def _obar_dot(self, Obar: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
         rows, np_ = Obar.shape
+        x = x.contiguous()
         y = torch.empty(rows, dtype=torch.float64, device=Obar.device)
-        _lib.call("qgx_obar_matvec", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(x.contiguous()), _lib.ptr(y),
+        _lib.call("qgx_obar_matvec", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(x), _lib.ptr(y),
                   _lib.stream_ptr())
         return y
 
     def _scale_columns(self, Obar: torch.Tensor, s: torch.Tensor) -> None:
         rows, np_ = Obar.shape
-        _lib.call("qgx_scale_columns", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(s.contiguous()),
+        s = s.contiguous()
+        _lib.call("qgx_scale_columns", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(s),
                   _lib.stream_ptr())
 
     def save(self, file) -> None:
@@ -363,6 +381,88 @@ class AdamSR(_MomentumSR):
         self._scale_columns(Obar, 1.0 / V)
         step = super().solve(Obar, Ebar)
         return step / V + m
+
+
+def pinvh_solve(rtol: Optional[float] = None, atol: float = 0.0) -> Solver:
+    """solver.py:104-111: S x = F by eigh with the soft inverse (TimeEvol's default)."""
+    return Solver("pinv", "lstsq", rtol=rtol, atol=atol)
+
+
+class TimeEvol(SR):
+    """Real-time evolution on the S-path (time_evol.py:26-134): S = Obar^H Obar (np x np)
+    and F = Obar^H Ebar, then S x = -Im F for complex-output states.
+
+    The reference accumulates S and F over sample chunks when the samples exceed its backward
+    chunk (time_evol.py:70-111); here Obar stays resident in HBM and the Gram kernel reads it
+    once, so the one-shot form is the only one. The solver acts on S itself: a "pinv" solver is
+    pinvh_solve, a "shift" solver the shifted Cholesky solve of S."""
+
+    def __init__(self, state, hamiltonian, solver: Optional[Solver] = None, gram: str = "fp32"):
+        super().__init__(state, hamiltonian, imag_time=False, solver=pinvh_solve() if solver is None else solver,
+                         gram=gram)
+
+    def get_SF(self, samples):
+        """(S, F): S = Re(Obar^H Obar), FP64 np x np; F = Obar^H Ebar, complex128 for a
+        complex-output state (else FP64). Only Re S is formed: solve() reads nothing else for
+        states with real parameters (time_evol.py:119-121)."""
+        S, F = self._sf(samples)
+        return S.clone(), F
+
+    def _sf(self, samples):
+        Ebar = self.get_Ebar(samples).contiguous()
+        Obar = self.get_Obar(samples)
+        S = self._gram_s(Obar)
+        rows, np_ = Obar.shape
+        import ctypes as C
+        nb = C.c_int64(0)
+        _lib.call("qgx_obar_rmatvec_workspace_bytes", rows, np_, C.byref(nb))
+        ws = self._state.workspace("rmatvec", nb.value)
+
+        def rmatvec(b):
+            y = torch.empty(np_, dtype=torch.float64, device=Obar.device)
+            _lib.call("qgx_obar_rmatvec", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(b), _lib.ptr(y),
+                      _lib.ptr(ws), ws.numel(), _lib.stream_ptr())
+            return y
+
+        if self.vs_type != VS_TYPE.real_to_complex:
+            return S, rmatvec(Ebar)
+        h = rows // 2
+        # Obar^H Ebar with Obar = Ore + i Oim, Ebar = Ere + i Eim:
+        # Re = Ore^T Ere + Oim^T Eim, Im = Ore^T Eim - Oim^T Ere
+        Fre = rmatvec(Ebar)
+        Fim = rmatvec(torch.cat([Ebar[h:], -Ebar[:h]]))
+        return S, torch.complex(Fre, Fim)
+
+    def solve(self, Smat: torch.Tensor, Fvec: torch.Tensor) -> torch.Tensor:
+        """step = solver(S, 1j F) for real_or_holomorphic states (its real part, zero, for
+        real parameters), solver(Re S, -Im F) otherwise (time_evol.py:115-128)."""
+        return self._solve_sf(Smat.real.to(torch.float64).clone(), Fvec)
+
+    def _solve_sf(self, S: torch.Tensor, Fvec: torch.Tensor) -> torch.Tensor:
+        """solve() on an FP64 S that it may overwrite."""
+        np_ = S.shape[0]
+        if self.vs_type != VS_TYPE.real_to_complex:
+            return torch.zeros(np_, dtype=torch.float64, device=S.device)
+        import ctypes as C
+        F = (-Fvec.imag if Fvec.is_complex() else torch.zeros_like(Fvec)).to(torch.float64).contiguous()
+        sv = self._solver
+        method = _lib.SOLVE_SHIFT if sv.kind == "shift" else _lib.SOLVE_PINV
+        rshift = _OBAR_RTOL if sv.rshift is None else sv.rshift
+        rtol = _OBAR_RTOL if sv.rtol is None else sv.rtol
+        nbytes = C.c_int64(0)
+        _lib.call("qgx_solve_workspace_bytes", np_, 1, method, C.byref(nbytes))
+        ws = self._state.workspace("solve", nbytes.value)
+        x = torch.empty(np_, dtype=torch.float64, device=S.device)
+        _lib.call("qgx_sym_solve", _lib.ptr(S), np_, _lib.ptr(F), method, rshift, sv.ashift, rtol, sv.atol,
+                  _lib.ptr(x), None, _lib.ptr(ws), ws.numel(), _lib.stream_ptr())
+        return x
+
+    def get_step(self, samples) -> torch.Tensor:
+        r = samples.reweight_factor
+        if r is not None and not bool(torch.allclose(r, torch.ones_like(r))):
+            raise ValueError("TimeEvol is only for non-reweighted samples")
+        S, F = self._sf(samples)
+        return self._solve_sf(S, F)
 
 
 MinSR = SR

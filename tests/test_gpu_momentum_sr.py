@@ -109,12 +109,14 @@ def test_obar_matvec_and_scale_columns(cuda):
     A = buf[:, :cols]
     x = rng.normal(size=cols)
     y = torch.empty(rows, dtype=torch.float64, device="cuda")
-    L.call("qgx_obar_matvec", L.ptr(A), rows, cols, lda, L.ptr(torch.as_tensor(x).cuda()), L.ptr(y), L.stream_ptr())
+    xd = torch.as_tensor(x).cuda()
+    L.call("qgx_obar_matvec", L.ptr(A), rows, cols, lda, L.ptr(xd), L.ptr(y), L.stream_ptr())
     An = A.cpu().numpy().astype(np.float64)
     np.testing.assert_allclose(y.cpu().numpy(), An @ x, rtol=1e-12, atol=1e-12)
     s = rng.uniform(0.5, 2.0, size=cols)
     pad_before = buf[:, cols:].clone()
-    L.call("qgx_scale_columns", L.ptr(A), rows, cols, lda, L.ptr(torch.as_tensor(s).cuda()), L.stream_ptr())
+    sd = torch.as_tensor(s).cuda()
+    L.call("qgx_scale_columns", L.ptr(A), rows, cols, lda, L.ptr(sd), L.stream_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(A.cpu().numpy(), (An * s[None, :]).astype(np.float32))
     assert torch.equal(buf[:, cols:], pad_before)

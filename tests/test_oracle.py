@@ -146,3 +146,17 @@ def test_momentum_sr_oracle_limits():
     x, m, v = sr.adamsr_step(A, b, np.zeros(80), np.zeros(80), 1, 0.95, 0.995, solver, a_dtype=np.float64)
     np.testing.assert_allclose(m, 0.05 * g, rtol=1e-12)
     np.testing.assert_allclose(x, g, rtol=1e-6, atol=1e-6 * np.abs(g).max())
+
+
+def test_time_evol_oracle_equals_real_time_lstsq():
+    """TimeEvol's S-path step equals real-time SR through lstsq_pinv_eig (the same pinv of
+    S = Re(Obar^H Obar) applied to -Im(Obar^H Ebar)) on a complex-output state."""
+    rng = np.random.default_rng(12)
+    O = rng.normal(size=(90, 20)) + 1j * rng.normal(size=(90, 20))
+    E = rng.normal(size=90) + 1j * rng.normal(size=90)
+    Ob, (eb, _, _) = sr.obar(O), sr.ebar(E)
+    S, F = sr.time_evol_sf(Ob, eb)
+    x = sr.time_evol_step(S, F, solver=lambda H, b: sr.pinvh(H, b, rtol=1e-9))
+    y = sr.solve(Ob, eb, lambda A, b: sr.lstsq_pinv(A, b, rtol=1e-9), complex_out=True, imag_time=False)
+    np.testing.assert_allclose(x, y, rtol=1e-10, atol=1e-12)
+    assert not np.allclose(x, 0)

@@ -226,6 +226,49 @@ int qgx_resconv_jacobian(const float* table, int32_t L, int32_t nblocks, int32_t
                          float* O_im, int64_t ldo, void* workspace, int64_t workspace_bytes,
                          qgx_stream_t stream);
 
+/* ---- symmetry projection (Variational(symm=...), quantax/state/variational.py:261-266,
+ * quantax/symmetry/symmetry.py:325-392) --------------------------------------------------
+ * psi_symm(s) = sum_g w_g psi(T_g s) with w_g = chi_0 chi_g / |G|. T_g s for g < nperm puts
+ * s[perm[g * N + i]] at site i (Symmetry.get_symm_spins); with z2 != 0 the elements
+ * nperm .. 2 nperm - 1 are the same permutations of -s, weighted by z2 chi (Z2 inversion).
+ * weight: (re, im) of w_g for g < nsymm = nperm (z2 ? 2 : 1), device doubles.
+ * The forward evaluates every T_g s with the same kernels as the unsymmetrised entry points
+ * and combines the |G| values per configuration in log space; a configuration whose sum
+ * vanishes gets log |psi| = -inf. */
+typedef struct {
+  const int16_t* perm;   /* device, nperm x N */
+  const double* weight;  /* device, 2 * nsymm */
+  int32_t nperm;
+  int32_t z2;            /* 0, 1 or -1 (only its being non-zero is read here) */
+} qgx_symm_t;
+
+int64_t qgx_resconv_log_psi_symm_workspace_bytes(int32_t L, int64_t ns, int32_t nsymm);
+int qgx_resconv_log_psi_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                             int32_t complex_out, int32_t conv_precision, const qgx_symm_t* symm,
+                             const uint32_t* spins, int64_t ns, float* log_psi, void* workspace,
+                             int64_t workspace_bytes, qgx_stream_t stream);
+int64_t qgx_resconv_sweep_symm_workspace_bytes(int32_t L, int64_t ns, int32_t nsymm);
+/* qgx_resconv_sweep for the symmetrised state: log_psi holds log psi_symm. */
+int qgx_resconv_sweep_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                           int32_t complex_out, int32_t conv_precision, const qgx_symm_t* symm,
+                           uint32_t* spins, float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps,
+                           uint64_t seed, uint64_t step0, float reweight, const int32_t* nbr, int32_t z,
+                           int32_t hop, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+int64_t qgx_resconv_eloc_symm_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn, int32_t nsymm);
+int qgx_resconv_eloc_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                          int32_t complex_out, int32_t conv_precision, const qgx_symm_t* symm,
+                          const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re,
+                          double* eloc_im, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+int64_t qgx_resconv_jacobian_symm_workspace_bytes(int32_t L, int32_t nblocks, int32_t channels, int64_t ns,
+                                                  int32_t nsymm);
+/* d log psi_symm / d params = sum_g v_g d log psi(T_g s) / d params with v_g = w_g psi(T_g s) /
+ * psi_symm(s) (the cotangents of variational.py:441-477): one backward per group element,
+ * seeded with v_g, accumulated into the sample's row. v_g comes from an FP32 forward. */
+int qgx_resconv_jacobian_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels,
+                              int32_t complex_out, const qgx_symm_t* symm, const uint32_t* spins, int64_t ns,
+                              float* O_re, float* O_im, int64_t ldo, void* workspace,
+                              int64_t workspace_bytes, qgx_stream_t stream);
+
 /* ---- statistics and centring (quantax/optimizer/sr.py:76-88, 180-195) ----------------- */
 /* energy = Re mean(E r), VarE = mean(|E - energy|^2 r) with compensated FP64 sums;
  * ebar = (E - mean E) sqrt(r / ns). E_im / ebar_im may be NULL for real E.

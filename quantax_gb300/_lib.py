@@ -52,6 +52,11 @@ class Operator(C.Structure):
     ]
 
 
+class Symm(C.Structure):
+    """qgx_symm_t"""
+    _fields_ = [("perm", vp), ("weight", vp), ("nperm", i32), ("z2", i32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "qgx_abi_version": (C.c_int, []),
@@ -97,6 +102,17 @@ SIGNATURES = {
     "qgx_transpose": (C.c_int, [vp, i64, i64, i64, vp, i64, i32, vp]),
     "qgx_obar_matvec": (C.c_int, [vp, i64, i64, i64, vp, vp, vp]),
     "qgx_scale_columns": (C.c_int, [vp, i64, i64, i64, vp, vp]),
+    "qgx_resconv_log_psi_symm_workspace_bytes": (i64, [i32, i64, i32]),
+    "qgx_resconv_log_psi_symm": (C.c_int, [vp, i32, i32, i32, i32, i32, C.POINTER(Symm), vp, i64, vp, vp, i64, vp]),
+    "qgx_resconv_sweep_symm_workspace_bytes": (i64, [i32, i64, i32]),
+    "qgx_resconv_sweep_symm": (C.c_int, [vp, i32, i32, i32, i32, i32, C.POINTER(Symm), vp, vp, vp, i64, i32, u64, u64,
+                                         f32, vp, i32, i32, vp, i64, vp]),
+    "qgx_resconv_eloc_symm_workspace_bytes": (i64, [i32, i64, i32, i32]),
+    "qgx_resconv_eloc_symm": (C.c_int, [vp, i32, i32, i32, i32, i32, C.POINTER(Symm), C.POINTER(Operator), vp, i64,
+                                        vp, vp, vp, i64, vp]),
+    "qgx_resconv_jacobian_symm_workspace_bytes": (i64, [i32, i32, i32, i64, i32]),
+    "qgx_resconv_jacobian_symm": (C.c_int, [vp, i32, i32, i32, i32, C.POINTER(Symm), vp, i64, vp, vp, i64, vp, i64,
+                                            vp]),
     "qgx_obar_rmatvec_workspace_bytes": (C.c_int, [i64, i64, vp]),
     "qgx_obar_rmatvec": (C.c_int, [vp, i64, i64, i64, vp, vp, vp, i64, vp]),
     "qgx_sym_solve": (C.c_int, [vp, i64, vp, i32, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
@@ -118,7 +134,8 @@ KERNELS_PER_CALL = {
     "qgx_philox4x32_10": 1, "qgx_spins_init_uniform": 1, "qgx_spins_init_fixed_up": 1, "qgx_spins_unpack": 1,
     "qgx_spins_pack": 1, "qgx_operator_diag": 1, "qgx_rbm_prepare": 1, "qgx_rbm_log_psi": 1, "qgx_rbm_sweep": 1,
     "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_resconv_prepare": 2,
-    "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6,
+    "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6, "qgx_resconv_log_psi_symm": 3, "qgx_resconv_eloc_symm": 10,
+    "qgx_resconv_jacobian_symm": 4,
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
     "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_apply_update": 2,
 }
@@ -132,6 +149,8 @@ def _kernels(name, args):
         return 1 + (int(args[1]) - 1) // 65535 if int(args[1]) > 0 and int(args[2]) > 0 else 0
     if name == "qgx_resconv_sweep":
         return 2 + 3 * int(args[10])  # step base, forward, then propose / forward / accept per step
+    if name == "qgx_resconv_sweep_symm":
+        return 4 + 5 * int(args[11])  # each forward is expand / forward / combine
     return KERNELS_PER_CALL.get(name, 0)
 
 

@@ -329,6 +329,75 @@ __global__ void rc_eloc_reduce_kernel(qgx_operator_t op, const uint32_t* __restr
   if (ei) ei[c] = im;
 }
 
+// ---- symmetry projection (quantax/symmetry/symmetry.py:325-392) -----------------------------
+struct SymmDev {
+  const int16_t* perm;
+  const double* weight;
+  int nperm, nsymm;
+};
+
+// the symmetrised configurations of the jacobian: T_g s per (sample, g), log psi(T_g s),
+// log psi_symm(s) and the weights; cfg == nullptr means no symmetry
+struct SymmJac {
+  const uint32_t* cfg;
+  const float2* lp_g;
+  const float2* lp_sym;
+  const double* weight;
+  int nsymm;
+};
+
+// row c * nsymm + g of out = T_g s_c (bits past n stay 0); n_live_exp = live count x nsymm
+__global__ void rc_symm_expand_kernel(const uint32_t* __restrict__ cfg, int64_t ncfg, const int64_t* __restrict__ n_live,
+                                      int n, const int16_t* __restrict__ perm, int nperm, int nsymm,
+                                      uint32_t* __restrict__ out, int64_t* __restrict__ n_live_exp) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
+  if (idx == 0 && n_live_exp) *n_live_exp = total * nsymm;
+  const int64_t c = idx / nsymm;
+  const int g = (int)(idx - c * nsymm);
+  if (c >= total) return;
+  const int nw = words_for(n);
+  const uint32_t* src = cfg + c * nw;
+  const int16_t* p = perm + (int64_t)(g % nperm) * n;
+  const bool flip = g >= nperm;
+  uint32_t* dst = out + idx * nw;
+  for (int k = 0; k < nw; ++k) {
+    const int nb = min(32, n - 32 * k);
+    uint32_t w = 0;
+    for (int b = 0; b < nb; ++b) {
+      int j = p[32 * k + b];
+      j = j < 0 ? 0 : (j >= n ? n - 1 : j);  // a malformed table stays inside the row
+      w |= ((src[j >> 5] >> (j & 31)) & 1u) << b;
+    }
+    if (flip) w ^= nb == 32 ? 0xffffffffu : ((1u << nb) - 1u);
+    dst[k] = w;
+  }
+}
+
+// log psi_symm(s_c) = log sum_g w_g exp(log psi(T_g s_c)), stable in the largest |psi(T_g s)|
+__global__ void rc_symm_combine_kernel(const float2* __restrict__ lp_g, int64_t ncfg, const int64_t* __restrict__ n_live,
+                                       int nsymm, const double* __restrict__ weight, float2* __restrict__ out) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
+  if (c >= total) return;
+  const float2* l = lp_g + c * nsymm;
+  float m = -INFINITY;
+  for (int g = 0; g < nsymm; ++g) m = fmaxf(m, l[g].x);
+  if (m == -INFINITY) {
+    out[c] = make_float2(-INFINITY, 0.0f);
+    return;
+  }
+  double zr = 0.0, zi = 0.0;
+  for (int g = 0; g < nsymm; ++g) {
+    const double e = exp((double)l[g].x - (double)m);
+    const double ar = e * cos((double)l[g].y), ai = e * sin((double)l[g].y);
+    const double wr = weight[2 * g], wi = weight[2 * g + 1];
+    zr += wr * ar - wi * ai;
+    zi += wr * ai + wi * ar;
+  }
+  out[c] = make_float2((float)((double)m + 0.5 * log(zr * zr + zi * zi)), (float)atan2(zi, zr));
+}
+
 // ---- per-sample log-derivatives (Variational.jacobian, quantax/state/variational.py:424-511) ----
 __device__ inline float gelu_tanh_grad(float x) {
   const float k0 = 0.7978845608028654f;
@@ -346,7 +415,7 @@ constexpr int kJacThreads = 256;
 template <int C>
 __device__ inline void weight_grads(const float* __restrict__ g /*[2][C][N]*/, const float* __restrict__ in /*[cin][N]*/,
                                     int cin, const int16_t* __restrict__ nbr, int N, bool has_bias,
-                                    float* __restrict__ o_re, float* __restrict__ o_im) {
+                                    float* __restrict__ o_re, float* __restrict__ o_im, bool accumulate) {
   constexpr int G = C / 4;
   const int items = 2 * G * cin * 2;  // cotangent x o-group x input channel x half
   // every lane of a warp runs the same iterations (blockDim is a multiple of 32), so the
@@ -395,8 +464,14 @@ __device__ inline void weight_grads(const float* __restrict__ g /*[2][C][N]*/, c
         for (int q = 0; q < 4; ++q) {
           const int o = 4 * og + q;
 #pragma unroll
-          for (int t = 0; t < 9; ++t) row[((int64_t)o * cin + i) * 9 + t] = acc[q][t];
-          if (has_bias && i == 0) row[(int64_t)C * cin * 9 + o] = bacc[q];
+          for (int t = 0; t < 9; ++t) {
+            float* dst = row + ((int64_t)o * cin + i) * 9 + t;
+            *dst = accumulate ? *dst + acc[q][t] : acc[q][t];
+          }
+          if (has_bias && i == 0) {
+            float* dst = row + (int64_t)C * cin * 9 + o;
+            *dst = accumulate ? *dst + bacc[q] : bacc[q];
+          }
         }
       }
     }
@@ -449,7 +524,8 @@ __device__ inline void stage_layer(const float* table, int l, float* W, float* W
 template <int C>
 __global__ void __launch_bounds__(kJacThreads)
     rc_jacobian_kernel(const float* __restrict__ table, ConvNet net, const uint32_t* __restrict__ spins, int64_t ns,
-                       float* __restrict__ o_re, float* __restrict__ o_im, int64_t ldo, float* __restrict__ scratch) {
+                       float* __restrict__ o_re, float* __restrict__ o_im, int64_t ldo, float* __restrict__ scratch,
+                       SymmJac sj) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int N = net.N, B = net.B, nw = words_for(N);
@@ -469,10 +545,24 @@ __global__ void __launch_bounds__(kJacThreads)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float fs = rsqrtf((float)(B + 1));
   const int cp = net.cplx ? C / 2 : C;
+  const int ng = sj.cfg ? sj.nsymm : 1;
   for (int64_t smp = blockIdx.x; smp < ns; smp += gridDim.x) {
+   for (int g = 0; g < ng; ++g) {
+    // v = d log psi_symm / d log psi(T_g s) = w_g psi(T_g s) / psi_symm(s); 1 without symmetry
+    float vr = 1.0f, vi = 0.0f;
+    const uint32_t* src = spins + smp * nw;
+    if (sj.cfg) {
+      const int64_t k = smp * sj.nsymm + g;
+      src = sj.cfg + k * nw;
+      const float2 lg = sj.lp_g[k], ls = sj.lp_sym[smp];
+      const double mag = exp((double)lg.x - (double)ls.x), ph = (double)lg.y - (double)ls.y;
+      const double ar = mag * cos(ph), ai = mag * sin(ph), wr = sj.weight[2 * g], wi = sj.weight[2 * g + 1];
+      vr = (float)(wr * ar - wi * ai);
+      vi = (float)(wr * ai + wi * ar);
+    }
     __syncthreads();
     for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      const float v = ((spins[smp * nw + (e >> 5)] >> (e & 31)) & 1u) ? 1.0f : -1.0f;
+      const float v = ((src[e >> 5] >> (e & 31)) & 1u) ? 1.0f : -1.0f;
       for (int c = 0; c < C; ++c) X[c * N + e] = v;
     }
     // ---- forward, saving X_b and A_b
@@ -540,7 +630,8 @@ __global__ void __launch_bounds__(kJacThreads)
       float sn = 0.0f, cs = 1.0f;
       if (net.cplx) sincosf(X[cp * N + e] * fs, &sn, &cs);
       const float ar = ex * cs, ai = ex * sn;
-      const float wr = ar * ir - ai * ii, wi = ar * ii + ai * ir;  // w = exp(z) / sum
+      const float ur = ar * ir - ai * ii, ui = ar * ii + ai * ir;  // exp(z) / sum
+      const float wr = vr * ur - vi * ui, wi = vr * ui + vi * ur;  // times v
       if (net.cplx) {
         G[e] = wr * fs;               // d Re / d y_c
         G[cp * N + e] = -wi * fs;     // d Re / d y_{c+C/2}
@@ -573,13 +664,13 @@ __global__ void __launch_bounds__(kJacThreads)
       stage_layer<C>(table, 2 * b + 1, W, WT);
       __syncthreads();
       // conv2: grads of W2, b2 and of Q (into GA)
-      weight_grads<C>(G, Qa, C, nbr, N, !last, row_re + poff + n1, row_im ? row_im + poff + n1 : nullptr);
+      weight_grads<C>(G, Qa, C, nbr, N, !last, row_re + poff + n1, row_im ? row_im + poff + n1 : nullptr, g > 0);
       input_grads<C>(G, WT, C, nbr, N, GA);
       __syncthreads();
       for (int e = threadIdx.x; e < 2 * CN; e += blockDim.x) GA[e] *= gelu_tanh_grad(xs[CN + (e % CN)]);
       stage_layer<C>(table, 2 * b, W, WT);
       __syncthreads();
-      weight_grads<C>(GA, P, cin, nbr, N, true, row_re + poff, row_im ? row_im + poff : nullptr);
+      weight_grads<C>(GA, P, cin, nbr, N, true, row_re + poff, row_im ? row_im + poff : nullptr, g > 0);
       if (b > 0) {
         input_grads<C>(GA, WT, cin, nbr, N, GP);
         __syncthreads();
@@ -589,12 +680,14 @@ __global__ void __launch_bounds__(kJacThreads)
         }
       }
     }
+   }
   }
 }
 
 template <int C>
 int launch_jacobian_c(const float* table, const ConvNet& net, const uint32_t* spins, int64_t ns, float* o_re,
-                      float* o_im, int64_t ldo, float* scratch, int64_t scratch_floats, cudaStream_t st) {
+                      float* o_im, int64_t ldo, float* scratch, int64_t scratch_floats, const SymmJac& sj,
+                      cudaStream_t st) {
   const int CN = C * net.N;
   const int64_t sf = 3LL * CN + 6LL * CN + C * 9 * C + C + 9 * C * C;
   const int smem = (int)(sf * 4 + net.N * 9 * 2 + 16);
@@ -607,7 +700,7 @@ int launch_jacobian_c(const float* table, const ConvNet& net, const uint32_t* sp
   int64_t grid = std::min<int64_t>((int64_t)device_sm_count() * per_sm, ns);
   grid = std::min<int64_t>(grid, scratch_floats / per_cta);
   if (grid < 1) return QGX_ERR_ARG;
-  k<<<(unsigned)grid, kJacThreads, smem, st>>>(table, net, spins, ns, o_re, o_im, ldo, scratch);
+  k<<<(unsigned)grid, kJacThreads, smem, st>>>(table, net, spins, ns, o_re, o_im, ldo, scratch, sj);
   return launch_status();
 }
 
@@ -646,13 +739,42 @@ int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, 
   }
 }
 
+inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
+
+// scratch of one symmetrised forward over ncfg configurations
+int64_t symm_scratch_bytes(int64_t ncfg, int nw, int nsymm) {
+  return al256(ncfg * nsymm * nw * 4) + al256(ncfg * nsymm * 8) + al256(8);
+}
+
+// log psi (or log psi_symm with sym) of ncfg configurations, n_live as in launch_forward
+int symm_forward(const float* table, const ConvNet& net, const SymmDev* sym, const uint32_t* cfg, int64_t ncfg,
+                 const int64_t* n_live, float2* out, char* scratch, cudaStream_t st, float2** lp_g_out = nullptr,
+                 const uint32_t** cfg_out = nullptr) {
+  if (!sym) return launch_forward(table, net, cfg, ncfg, n_live, out, st);
+  const int nw = words_for(net.N);
+  const int64_t ne = ncfg * sym->nsymm;
+  uint32_t* cg = reinterpret_cast<uint32_t*>(scratch);
+  float2* lg = reinterpret_cast<float2*>(scratch + al256(ne * nw * 4));
+  int64_t* nle = reinterpret_cast<int64_t*>(scratch + al256(ne * nw * 4) + al256(ne * 8));
+  rc_symm_expand_kernel<<<(unsigned)((ne + 127) / 128), 128, 0, st>>>(cfg, ncfg, n_live, net.N, sym->perm, sym->nperm,
+                                                                       sym->nsymm, cg, n_live ? nle : nullptr);
+  int rc = launch_forward(table, net, cg, ne, n_live ? nle : nullptr, lg, st);
+  if (rc != QGX_OK) return rc;
+  rc_symm_combine_kernel<<<(unsigned)((ncfg + 127) / 128), 128, 0, st>>>(lg, ncfg, n_live, sym->nsymm, sym->weight,
+                                                                         out);
+  if (lp_g_out) *lp_g_out = lg;
+  if (cfg_out) *cfg_out = cg;
+  return launch_status();
+}
+
 // ---- sweep graphs ----------------------------------------------------------------------
 // A sweep is 1 + 3 nsteps launches (forward, then propose / forward / accept per step). The
 // launch sequence is captured once per set of buffers and sizes into a CUDA graph (on a
 // private stream, relaxed capture mode) and replayed on the caller's stream; the Philox step
 // base lives in the workspace, so one graph serves every starting step.
 struct SweepKey {
-  const void *table, *spins, *lp, *acc, *nbr, *ws;
+  const void *table, *spins, *lp, *acc, *nbr, *ws, *perm, *weight;
+  int64_t nperm_nsymm;
   int64_t ns;
   int nsteps, L, B, C, cplx, prec, z, hop, device;
   uint64_t seed;
@@ -679,7 +801,17 @@ bool valid_net(int L, int B, int C, int cplx) {
 
 bool valid_prec(int p) { return p == QGX_CONV_FP32 || p == QGX_CONV_TF32 || p == QGX_CONV_BF16; }
 
-inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
+constexpr int kMaxSymm = 1024;
+
+// the public descriptor checked and made internal; false on a malformed one
+bool to_symm(const qgx_symm_t* s, SymmDev* d) {
+  if (!s || !s->perm || !s->weight || s->nperm < 1) return false;
+  d->perm = s->perm;
+  d->weight = s->weight;
+  d->nperm = s->nperm;
+  d->nsymm = s->nperm * (s->z2 != 0 ? 2 : 1);
+  return d->nsymm <= kMaxSymm;
+}
 
 }  // namespace
 }  // namespace qgx
@@ -723,18 +855,15 @@ int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns) {
   return al256(ns * nw * 4) + al256(ns * 8) + al256(ns) + al256(8);  // + the Philox step base
 }
 
-int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-                      int32_t conv_precision, uint32_t* spins, float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed,
-                      uint64_t step0, float reweight, const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
-                      int64_t workspace_bytes, qgx_stream_t stream) {
-  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0 &&
-                nsteps >= 0);
-  QGX_CHECK_ARG(nbr && z > 0 && (hop == 1 || hop == -1));
-  if (ns == 0) return QGX_OK;
-  QGX_CHECK_ARG(table && spins && log_psi && workspace);
-  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_workspace_bytes(L, ns));
-  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  cudaStream_t st = as_cuda(stream);
+}  // extern "C"
+
+namespace qgx {
+namespace {
+
+int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+               int32_t conv_precision, const SymmDev* sym, uint32_t* spins, float* log_psi, int32_t* accepts,
+               int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0, float reweight, const int32_t* nbr, int32_t z,
+               int32_t hop, void* workspace, cudaStream_t st) {
   ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
   const int nw = words_for(net.N);
   char* ws = static_cast<char*>(workspace);
@@ -742,16 +871,17 @@ int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t ch
   float2* lp_prop = reinterpret_cast<float2*>(ws + al256(ns * nw * 4));
   int8_t* changed = reinterpret_cast<int8_t*>(ws + al256(ns * nw * 4) + al256(ns * 8));
   uint64_t* step_base = reinterpret_cast<uint64_t*>(ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns));
+  char* sscratch = ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns) + al256(8);
   float2* lp = reinterpret_cast<float2*>(log_psi);
   const unsigned g = (unsigned)((ns + 127) / 128);
   // the launch sequence of the sweep (recorded into the graph)
   auto record = [&](cudaStream_t s) -> int {
-    int rc = launch_forward(table, net, spins, ns, nullptr, lp, s);
+    int rc = symm_forward(table, net, sym, spins, ns, nullptr, lp, sscratch, s);
     if (rc != QGX_OK) return rc;
     if (accepts) QGX_CHECK_CUDA(cudaMemsetAsync(accepts, 0, ns * sizeof(int32_t), s));
     for (int t = 0; t < nsteps; ++t) {
       rc_propose_kernel<<<g, 128, 0, s>>>(spins, prop, changed, ns, net.N, seed, step_base, t, nbr, z, hop);
-      if ((rc = launch_forward(table, net, prop, ns, nullptr, lp_prop, s)) != QGX_OK) return rc;
+      if ((rc = symm_forward(table, net, sym, prop, ns, nullptr, lp_prop, sscratch, s)) != QGX_OK) return rc;
       rc_accept_kernel<<<g, 128, 0, s>>>(spins, lp, prop, lp_prop, changed, accepts, ns, net.N, seed, step_base, t,
                                          reweight);
     }
@@ -770,6 +900,11 @@ int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t ch
   key.acc = accepts;
   key.nbr = nbr;
   key.ws = workspace;
+  if (sym) {
+    key.perm = sym->perm;
+    key.weight = sym->weight;
+    key.nperm_nsymm = ((int64_t)sym->nperm << 32) | sym->nsymm;
+  }
   key.ns = ns;
   key.nsteps = nsteps;
   key.L = L;
@@ -816,6 +951,49 @@ int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t ch
   return QGX_OK;
 }
 
+}  // namespace
+}  // namespace qgx
+
+extern "C" {
+
+int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                      int32_t conv_precision, uint32_t* spins, float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed,
+                      uint64_t step0, float reweight, const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
+                      int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0 &&
+                nsteps >= 0);
+  QGX_CHECK_ARG(nbr && z > 0 && (hop == 1 || hop == -1));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_workspace_bytes(L, ns));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return sweep_impl(table, L, nblocks, channels, complex_out, conv_precision, nullptr, spins, log_psi, accepts, ns,
+                    nsteps, seed, step0, reweight, nbr, z, hop, workspace, as_cuda(stream));
+}
+
+int64_t qgx_resconv_sweep_symm_workspace_bytes(int32_t L, int64_t ns, int32_t nsymm) {
+  if (L < 1 || ns < 1 || nsymm < 1) return 0;
+  return qgx_resconv_sweep_workspace_bytes(L, ns) + symm_scratch_bytes(ns, words_for(L * L), nsymm);
+}
+
+int qgx_resconv_sweep_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                           int32_t conv_precision, const qgx_symm_t* symm, uint32_t* spins, float* log_psi,
+                           int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0, float reweight,
+                           const int32_t* nbr, int32_t z, int32_t hop, void* workspace, int64_t workspace_bytes,
+                           qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0 &&
+                nsteps >= 0);
+  QGX_CHECK_ARG(nbr && z > 0 && (hop == 1 || hop == -1));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_symm_workspace_bytes(L, ns, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return sweep_impl(table, L, nblocks, channels, complex_out, conv_precision, &sym, spins, log_psi, accepts, ns,
+                    nsteps, seed, step0, reweight, nbr, z, hop, workspace, as_cuda(stream));
+}
+
 int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn) {
   if (L < 1 || ns < 1 || max_conn < 0) return 0;
   const int nw = words_for(L * L);
@@ -823,16 +1001,15 @@ int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn
   return al256(ns * 8) + al256((ns + 1) * 8) + al256(nc * nw * 4) + al256(nc * 8) + al256(nc * 8) + al256(ns * 8);
 }
 
-int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-                     int32_t conv_precision, const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im,
-                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
-  QGX_CHECK_ARG(op && valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
-  if (ns == 0) return QGX_OK;
-  QGX_CHECK_ARG(table && spins && eloc_re && workspace);
+}  // extern "C"
+
+namespace qgx {
+namespace {
+
+int eloc_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+              int32_t conv_precision, const SymmDev* sym, const qgx_operator_t* op, const uint32_t* spins, int64_t ns,
+              double* eloc_re, double* eloc_im, void* workspace, cudaStream_t st) {
   const int max_conn = op->n_f1 + op->n_f2;
-  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_workspace_bytes(L, ns, max_conn));
-  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  cudaStream_t st = as_cuda(stream);
   ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
   const int nw = words_for(net.N);
   const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
@@ -849,15 +1026,105 @@ int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t cha
   double* elem = reinterpret_cast<double*>(take(nc * 8));
   float2* lp_conn = reinterpret_cast<float2*>(take(nc * 8));
   float2* lp = reinterpret_cast<float2*>(take(ns * 8));
+  char* sscratch = sym ? take(symm_scratch_bytes(nc, nw, sym->nsymm)) : nullptr;
   const unsigned g = (unsigned)((ns + 127) / 128);
   rc_conn_count_kernel<<<g, 128, 0, st>>>(*op, spins, ns, net.N, counts);
   rc_scan_kernel<<<1, 1024, 0, st>>>(counts, ns, offsets);
   rc_conn_write_kernel<<<g, 128, 0, st>>>(*op, spins, ns, net.N, offsets, conn, elem);
-  int rc = launch_forward(table, net, spins, ns, nullptr, lp, st);
+  int rc = symm_forward(table, net, sym, spins, ns, nullptr, lp, sscratch, st);
   if (rc != QGX_OK) return rc;
-  if ((rc = launch_forward(table, net, conn, nc, offsets + ns, lp_conn, st)) != QGX_OK) return rc;
+  if ((rc = symm_forward(table, net, sym, conn, nc, offsets + ns, lp_conn, sscratch, st)) != QGX_OK) return rc;
   rc_eloc_reduce_kernel<<<g, 128, 0, st>>>(*op, spins, ns, net.N, lp, offsets, elem, lp_conn, eloc_re, eloc_im);
   return launch_status();
+}
+
+int jacobian_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                  const SymmDev* sym, const uint32_t* spins, int64_t ns, float* O_re, float* O_im, int64_t ldo,
+                  void* workspace, int64_t workspace_bytes, cudaStream_t st) {
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, QGX_CONV_FP32};
+  char* ws = static_cast<char*>(workspace);
+  int64_t scratch_bytes = workspace_bytes;
+  SymmJac sj{nullptr, nullptr, nullptr, nullptr, 1};
+  if (sym) {
+    // log psi(T_g s) and log psi_symm(s) by the FP32 forward, then one backward per element
+    const int nw = words_for(net.N);
+    const int64_t sb = symm_scratch_bytes(ns, nw, sym->nsymm);
+    float2* lp_sym = reinterpret_cast<float2*>(ws + sb);
+    float2* lp_g = nullptr;
+    const uint32_t* cfg = nullptr;
+    int rc = symm_forward(table, net, sym, spins, ns, nullptr, lp_sym, ws, st, &lp_g, &cfg);
+    if (rc != QGX_OK) return rc;
+    sj = SymmJac{cfg, lp_g, lp_sym, sym->weight, sym->nsymm};
+    ws += sb + al256(ns * 8);
+    scratch_bytes -= sb + al256(ns * 8);
+  }
+  float* scratch = reinterpret_cast<float*>(ws);
+  const int64_t sf = scratch_bytes / 4;
+  switch (channels) {
+    case 4: return launch_jacobian_c<4>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, sj, st);
+    case 8: return launch_jacobian_c<8>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, sj, st);
+    case 12: return launch_jacobian_c<12>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, sj, st);
+    case 16: return launch_jacobian_c<16>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, sj, st);
+    default: return QGX_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace
+}  // namespace qgx
+
+extern "C" {
+
+int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                     int32_t conv_precision, const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im,
+                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(op && valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && eloc_re && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_workspace_bytes(L, ns, op->n_f1 + op->n_f2));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return eloc_impl(table, L, nblocks, channels, complex_out, conv_precision, nullptr, op, spins, ns, eloc_re, eloc_im,
+                   workspace, as_cuda(stream));
+}
+
+int64_t qgx_resconv_eloc_symm_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn, int32_t nsymm) {
+  if (L < 1 || ns < 1 || max_conn < 0 || nsymm < 1) return 0;
+  const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
+  return qgx_resconv_eloc_workspace_bytes(L, ns, max_conn) + symm_scratch_bytes(nc, words_for(L * L), nsymm);
+}
+
+int qgx_resconv_eloc_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                          int32_t conv_precision, const qgx_symm_t* symm, const qgx_operator_t* op,
+                          const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im, void* workspace,
+                          int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(op && valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && eloc_re && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_symm_workspace_bytes(L, ns, op->n_f1 + op->n_f2, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return eloc_impl(table, L, nblocks, channels, complex_out, conv_precision, &sym, op, spins, ns, eloc_re, eloc_im,
+                   workspace, as_cuda(stream));
+}
+
+int64_t qgx_resconv_log_psi_symm_workspace_bytes(int32_t L, int64_t ns, int32_t nsymm) {
+  if (L < 1 || ns < 1 || nsymm < 1) return 0;
+  return symm_scratch_bytes(ns, words_for(L * L), nsymm);
+}
+
+int qgx_resconv_log_psi_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                             int32_t conv_precision, const qgx_symm_t* symm, const uint32_t* spins, int64_t ns,
+                             float* log_psi, void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_log_psi_symm_workspace_bytes(L, ns, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
+  return symm_forward(table, net, &sym, spins, ns, nullptr, reinterpret_cast<float2*>(log_psi),
+                      static_cast<char*>(workspace), as_cuda(stream));
 }
 
 int64_t qgx_resconv_jacobian_workspace_bytes(int32_t L, int32_t nblocks, int32_t channels) {
@@ -874,17 +1141,31 @@ int qgx_resconv_jacobian(const float* table, int32_t L, int32_t nblocks, int32_t
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && O_re && workspace && workspace_bytes > 0);
   QGX_CHECK_ARG(!complex_out || O_im);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, QGX_CONV_FP32};
-  float* scratch = static_cast<float*>(workspace);
-  const int64_t sf = workspace_bytes / 4;
-  cudaStream_t st = as_cuda(stream);
-  switch (channels) {
-    case 4: return launch_jacobian_c<4>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
-    case 8: return launch_jacobian_c<8>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
-    case 12: return launch_jacobian_c<12>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
-    case 16: return launch_jacobian_c<16>(table, net, spins, ns, O_re, O_im, ldo, scratch, sf, st);
-    default: return QGX_ERR_UNSUPPORTED;
-  }
+  return jacobian_impl(table, L, nblocks, channels, complex_out, nullptr, spins, ns, O_re, O_im, ldo, workspace,
+                       workspace_bytes, as_cuda(stream));
+}
+
+int64_t qgx_resconv_jacobian_symm_workspace_bytes(int32_t L, int32_t nblocks, int32_t channels, int64_t ns,
+                                                  int32_t nsymm) {
+  if (L < 1 || nblocks < 1 || channels < 1 || ns < 1 || nsymm < 1) return 0;
+  return symm_scratch_bytes(ns, words_for(L * L), nsymm) + al256(ns * 8) +
+         qgx_resconv_jacobian_workspace_bytes(L, nblocks, channels);
+}
+
+int qgx_resconv_jacobian_symm(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
+                              const qgx_symm_t* symm, const uint32_t* spins, int64_t ns, float* O_re, float* O_im,
+                              int64_t ldo, void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && ns >= 0);
+  QGX_CHECK_ARG(ldo >= qgx_resconv_nparams(nblocks, channels));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && O_re && workspace);
+  QGX_CHECK_ARG(!complex_out || O_im);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_jacobian_symm_workspace_bytes(L, nblocks, channels, ns, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return jacobian_impl(table, L, nblocks, channels, complex_out, &sym, spins, ns, O_re, O_im, ldo, workspace,
+                       workspace_bytes, as_cuda(stream));
 }
 
 }  // extern "C"

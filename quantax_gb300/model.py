@@ -196,34 +196,60 @@ class ResConv:
     def _fwd_args(self):
         return self._args() + (self._conv_code,)
 
-    def log_psi(self, table, packed, out):
-        """out: (ns, 2) float32 (re, im)."""
-        _lib.call("qgx_resconv_log_psi", _lib.ptr(table), *self._fwd_args(), _lib.ptr(packed), packed.shape[0],
-                  _lib.ptr(out), _lib.stream_ptr())
+    # symm: a non-identity quantax_gb300.symmetry.Symmetry, or None
+    def log_psi_workspace_bytes(self, ns, symm=None):
+        return 0 if symm is None else int(_lib.lib().qgx_resconv_log_psi_symm_workspace_bytes(self.L, ns, symm.nsymm))
 
-    def sweep_workspace_bytes(self, ns):
-        return int(_lib.lib().qgx_resconv_sweep_workspace_bytes(self.L, ns))
+    def log_psi(self, table, packed, out, symm=None, workspace=None):
+        """out: (ns, 2) float32 (re, im)."""
+        if symm is None:
+            _lib.call("qgx_resconv_log_psi", _lib.ptr(table), *self._fwd_args(), _lib.ptr(packed), packed.shape[0],
+                      _lib.ptr(out), _lib.stream_ptr())
+            return
+        _lib.call("qgx_resconv_log_psi_symm", _lib.ptr(table), *self._fwd_args(), C.byref(symm.device_struct()),
+                  _lib.ptr(packed), packed.shape[0], _lib.ptr(out), _lib.ptr(workspace), workspace.numel(),
+                  _lib.stream_ptr())
+
+    def sweep_workspace_bytes(self, ns, symm=None):
+        if symm is None:
+            return int(_lib.lib().qgx_resconv_sweep_workspace_bytes(self.L, ns))
+        return int(_lib.lib().qgx_resconv_sweep_symm_workspace_bytes(self.L, ns, symm.nsymm))
 
     def sweep(self, table, packed, log_psi, accepts, nsteps, seed, step0, reweight, proposal, nbr, z, hop,
-              workspace):
+              workspace, symm=None):
         if proposal != _lib.PROPOSAL_SPIN_EXCHANGE:
             raise NotImplementedError("the ResConv sampler implements SpinExchange proposals")
-        _lib.call("qgx_resconv_sweep", _lib.ptr(table), *self._fwd_args(), _lib.ptr(packed), _lib.ptr(log_psi),
-                  _lib.ptr(accepts), packed.shape[0], int(nsteps), int(seed), int(step0), float(reweight),
-                  _lib.ptr(nbr), int(z), int(hop), _lib.ptr(workspace), workspace.numel(), _lib.stream_ptr())
+        head = (_lib.ptr(table), *self._fwd_args())
+        if symm is not None:
+            head = head + (C.byref(symm.device_struct()),)
+        _lib.call("qgx_resconv_sweep" if symm is None else "qgx_resconv_sweep_symm", *head, _lib.ptr(packed),
+                  _lib.ptr(log_psi), _lib.ptr(accepts), packed.shape[0], int(nsteps), int(seed), int(step0),
+                  float(reweight), _lib.ptr(nbr), int(z), int(hop), _lib.ptr(workspace), workspace.numel(),
+                  _lib.stream_ptr())
 
-    def eloc_workspace_bytes(self, ns, max_conn):
-        return int(_lib.lib().qgx_resconv_eloc_workspace_bytes(self.L, ns, max_conn))
+    def eloc_workspace_bytes(self, ns, max_conn, symm=None):
+        if symm is None:
+            return int(_lib.lib().qgx_resconv_eloc_workspace_bytes(self.L, ns, max_conn))
+        return int(_lib.lib().qgx_resconv_eloc_symm_workspace_bytes(self.L, ns, max_conn, symm.nsymm))
 
-    def eloc(self, table, compiled_op, packed, out_re, out_im, workspace):
-        _lib.call("qgx_resconv_eloc", _lib.ptr(table), *self._fwd_args(), C.byref(compiled_op.struct),
+    def eloc(self, table, compiled_op, packed, out_re, out_im, workspace, symm=None):
+        head = (_lib.ptr(table), *self._fwd_args())
+        if symm is not None:
+            head = head + (C.byref(symm.device_struct()),)
+        _lib.call("qgx_resconv_eloc" if symm is None else "qgx_resconv_eloc_symm", *head, C.byref(compiled_op.struct),
                   _lib.ptr(packed), packed.shape[0], _lib.ptr(out_re), _lib.ptr(out_im), _lib.ptr(workspace),
                   workspace.numel(), _lib.stream_ptr())
 
-    def jacobian_workspace_bytes(self):
-        return int(_lib.lib().qgx_resconv_jacobian_workspace_bytes(self.L, self.nblocks, self.channels))
+    def jacobian_workspace_bytes(self, ns=1, symm=None):
+        if symm is None:
+            return int(_lib.lib().qgx_resconv_jacobian_workspace_bytes(self.L, self.nblocks, self.channels))
+        return int(_lib.lib().qgx_resconv_jacobian_symm_workspace_bytes(self.L, self.nblocks, self.channels, ns,
+                                                                          symm.nsymm))
 
-    def jacobian(self, table, packed, o_re, o_im, ldo, workspace):
-        _lib.call("qgx_resconv_jacobian", _lib.ptr(table), *self._args(), _lib.ptr(packed), packed.shape[0],
-                  _lib.ptr(o_re), _lib.ptr(o_im), int(ldo), _lib.ptr(workspace), workspace.numel(),
+    def jacobian(self, table, packed, o_re, o_im, ldo, workspace, symm=None):
+        head = (_lib.ptr(table), *self._args())
+        if symm is not None:
+            head = head + (C.byref(symm.device_struct()),)
+        _lib.call("qgx_resconv_jacobian" if symm is None else "qgx_resconv_jacobian_symm", *head, _lib.ptr(packed),
+                  packed.shape[0], _lib.ptr(o_re), _lib.ptr(o_im), int(ldo), _lib.ptr(workspace), workspace.numel(),
                   _lib.stream_ptr())

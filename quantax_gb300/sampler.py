@@ -132,9 +132,9 @@ class Metropolis:
         n = self._sweep_steps if nsweeps is None else int(nsweeps)
         st = self._state
         if self._resconv:
-            ws = st.workspace("sweep", st.model.sweep_workspace_bytes(self._nsamples))
+            ws = st.workspace("sweep", st.model.sweep_workspace_bytes(self._nsamples, st.symm_dev))
             st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, n, self._seed, self._step,
-                           self._reweight, self.proposal, self._nbr, self._z, self._hop, ws)
+                           self._reweight, self.proposal, self._nbr, self._z, self._hop, ws, st.symm_dev)
             lp_real = self._log_psi[:, 0].contiguous()
             lp = torch.view_as_complex(self._log_psi.clone()) if st.is_complex else lp_real
         else:

@@ -152,6 +152,10 @@ class Lattice(Sites):
         return len(self._shape) - 1
 
     @property
+    def basis_vectors(self) -> np.ndarray:
+        return self._basis_vectors
+
+    @property
     def ncells(self) -> int:
         return int(np.prod(self._shape[1:]))
 

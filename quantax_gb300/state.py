@@ -47,8 +47,13 @@ class Variational:
     """Variational state wrapping a model with device kernels."""
 
     def __init__(self, model, param_file=None, symm=None, max_parallel=None, use_ref: bool = True):
-        if symm is not None:
-            raise NotImplementedError("symmetry projection is not implemented in quantax_gb300")
+        from .symmetry import Identity
+        self._symm = Identity() if symm is None else symm
+        if self._symm.Nmodes != get_sites().Nmodes:
+            raise ValueError("the symmetry was built for another lattice")
+        self._sym = None if self._symm.is_identity else self._symm
+        if self._sym is not None and model.kind != "resconv":
+            raise NotImplementedError("symmetry projection is built for the ResConv model")
         self._model = model
         self._dev = device()
         self._sites = get_sites()  # the lattice this state was built on (kept, not re-read)
@@ -96,6 +101,16 @@ class Variational:
         return self._vs_type
 
     @property
+    def symm(self):
+        """The symmetry the wavefunction is projected on (Identity by default)."""
+        return self._symm
+
+    @property
+    def symm_dev(self):
+        """The symmetry the kernels evaluate: None for the identity."""
+        return self._sym
+
+    @property
     def use_ref(self) -> bool:
         return self._use_ref
 
@@ -131,8 +146,15 @@ class Variational:
             self._model.log_psi(self._table, packed, out)
             return out
         out = torch.empty((packed.shape[0], 2), dtype=torch.float32, device=self._dev)
-        self._model.log_psi(self._table, packed, out)
-        return torch.view_as_complex(out) if self.is_complex else out[:, 0].contiguous()
+        if self._sym is None:
+            self._model.log_psi(self._table, packed, out)
+        else:
+            ws = self.workspace("fwd_symm", self._model.log_psi_workspace_bytes(packed.shape[0], self._sym))
+            self._model.log_psi(self._table, packed, out, self._sym, ws)
+        # a projected real state can be negative: its phase (0 or pi) carries the sign
+        if self.is_complex or self._sym is not None:
+            return torch.view_as_complex(out)
+        return out[:, 0].contiguous()
 
     def log_psi(self, s) -> torch.Tensor:
         return self.log_psi_packed(pack_spins(s, self.Nmodes))
@@ -140,7 +162,8 @@ class Variational:
     def __call__(self, s) -> torch.Tensor:
         """psi(s) as float64 / complex128 (variational.py:325-347); use log_psi for large systems."""
         lp = self.log_psi(s)
-        return torch.exp(lp.to(torch.complex128 if lp.is_complex() else torch.float64))
+        psi = torch.exp(lp.to(torch.complex128 if lp.is_complex() else torch.float64))
+        return psi if self.is_complex or not psi.is_complex() else psi.real
 
     def init_internal(self, s):
         return None
@@ -158,8 +181,8 @@ class Variational:
             return out
         out_im = torch.empty(ns, dtype=torch.float64, device=self._dev) if self.is_complex else None
         max_conn = len(comp.host["f1"]) + len(comp.host["f2"])
-        ws = self.workspace("eloc", self._model.eloc_workspace_bytes(ns, max_conn))
-        self._model.eloc(self._table, comp, samples.packed, out, out_im, ws)
+        ws = self.workspace("eloc", self._model.eloc_workspace_bytes(ns, max_conn, self._sym))
+        self._model.eloc(self._table, comp, samples.packed, out, out_im, ws, self._sym)
         return torch.complex(out, out_im) if out_im is not None else out
 
     def jacobian(self, s) -> torch.Tensor:
@@ -173,8 +196,9 @@ class Variational:
             return out
         rows = 2 * ns if self.is_complex else ns
         out = torch.empty((rows, self.nparams), dtype=torch.float32, device=self._dev)
-        ws = self.workspace("jac", self._model.jacobian_workspace_bytes())
-        self._model.jacobian(self._table, packed, out[:ns], out[ns:] if self.is_complex else None, self.nparams, ws)
+        ws = self.workspace("jac", self._model.jacobian_workspace_bytes(ns, self._sym))
+        self._model.jacobian(self._table, packed, out[:ns], out[ns:] if self.is_complex else None, self.nparams, ws,
+                             self._sym)
         return torch.complex(out[:ns], out[ns:]) if self.is_complex else out
 
     def obar_rows(self, ns: int) -> int:
@@ -192,10 +216,10 @@ class Variational:
             ws = self.workspace("obar", self._model.obar_workspace_bytes(ns))
             self._model.obar(self._table, samples.packed, samples.reweight_factor, out, omean, ws)
             return out, omean
-        ws = self.workspace("jac", self._model.jacobian_workspace_bytes())
+        ws = self.workspace("jac", self._model.jacobian_workspace_bytes(ns, self._sym))
         cplx = self.is_complex
         ld = out.stride(0)
-        self._model.jacobian(self._table, samples.packed, out[:ns], out[ns:] if cplx else None, ld, ws)
+        self._model.jacobian(self._table, samples.packed, out[:ns], out[ns:] if cplx else None, ld, ws, self._sym)
         cws = self.workspace("center", _lib.lib().qgx_center_columns_workspace_bytes(ns, self.nparams))
         halves = [out[:ns], out[ns:]] if cplx else [out]
         means = []

@@ -358,6 +358,94 @@ def run_trajectory(args, rank):
                           "chains": args.chains, "steps": args.steps, "forms": out}), flush=True)
 
 
+# ED ground energy of the 4x4 Heisenberg model (MSR) and the reference's trained, projected
+# ResConv(2 blocks, 8 channels) on it (tutorials/J1J2.ipynb:90, :331)
+HEIS4_ED_E0 = -44.91393283371544
+HEIS4_REFERENCE = {"energy": -44.91365075323898, "rel_err": 6.280467076974902e-06, "fidelity": 0.9999925315217684}
+
+
+def exact_energy(qtx, state, H):
+    """<psi|H|psi> / <psi|psi> summed over every Sz = 0 configuration of the 4x4 lattice:
+    psi and E_loc from the device kernels, weights |psi|^2 (no sampling)."""
+    import numpy as np
+    import torch
+    from quantax_gb300.sampler import Samples
+    from quantax_gb300.state import pack_spins
+    n = state.Nmodes
+    codes = np.arange(1 << n, dtype=np.int64)
+    pop = np.zeros_like(codes)
+    for i in range(n):
+        pop += (codes >> i) & 1
+    codes = codes[pop == n // 2]
+    spins = (((codes[:, None] >> np.arange(n)) & 1) * 2 - 1).astype(np.int8)
+    packed = pack_spins(spins, n)
+    lp = state.log_psi_packed(packed)
+    lpr = lp.real if lp.is_complex() else lp
+    samples = Samples(packed, lp, n, None)
+    E = H.Oloc(state, samples)
+    E = E.real if E.is_complex() else E
+    w = torch.exp(2.0 * (lpr.double() - lpr.max().double()))
+    live = (w > 0) & torch.isfinite(E)
+    return float((w[live] * E[live]).sum() / w[live].sum()), int(codes.size)
+
+
+def run_tutorial(args, rank):
+    """The reference's 4x4 Heisenberg notebook (tutorials/J1J2.ipynb cells 1-19): ResConv(2
+    blocks, 8 channels) trained 200 SR steps (lr 0.01, 1024 SpinExchange samples, default
+    pinv solver) without symmetry, then projected on Rotation(pi/2) @ Flip() @ SpinInverse();
+    and 200 more steps of the projected state. Energies are exact sums over the 12870-state
+    sector; times are CUDA events around each phase."""
+    import numpy as np
+    import torch
+    import quantax_gb300 as qtx
+    from quantax_gb300.symmetry import Flip, Rotation, SpinInverse
+    qtx.set_random_seed(args.seed)
+    qtx.set_default_dtype(np.float64)
+    qtx.sites.Square(4, Nparticles=(8, 8))
+    H = qtx.operator.Heisenberg(msr=True)
+    model = qtx.model.ResConv(2, 8)
+    out = {}
+
+    def train(state, steps):
+        sampler = qtx.sampler.SpinExchange(state, 1024)
+        opt = qtx.optimizer.SR(state, H)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        energies = []
+        for _ in range(steps):
+            samples = sampler.sweep()
+            step = opt.get_step(samples)
+            state.update(step * 0.01)
+            energies.append(opt.stats)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0, [float(x[0]) for x in energies]
+
+    state = qtx.state.Variational(model)
+    t1, en1 = train(state, args.tutorial_steps)
+    e_plain, dim = exact_energy(qtx, state, H)
+    symm = Rotation(np.pi / 2) @ Flip() @ SpinInverse()
+    symm_state = qtx.state.Variational(model, symm=symm)
+    symm_state.set_params(state.params.cpu())
+    e_proj, _ = exact_energy(qtx, symm_state, H)
+    t2, en2 = train(symm_state, args.tutorial_steps)
+    e_proj2, _ = exact_energy(qtx, symm_state, H)
+    rel = lambda e: abs((e - HEIS4_ED_E0) / HEIS4_ED_E0)
+    line = {
+        "metric": "relative energy error of the projected state", "workload": "heisenberg_square4_resconv2x8_tutorial",
+        "ed_energy": HEIS4_ED_E0, "sector_dim": dim, "seed": args.seed, "steps_per_phase": args.tutorial_steps,
+        "unsymmetrised_training": {"steps_per_s": args.tutorial_steps / t1, "exact_energy": e_plain,
+                                   "rel_err": rel(e_plain), "mc_energy_last10": float(np.mean(en1[-10:]))},
+        "projected_after_unsymmetrised_training": {"exact_energy": e_proj, "rel_err": rel(e_proj),
+                                                   "reference": HEIS4_REFERENCE, "nsymm": symm.nsymm},
+        "projected_training": {"steps_per_s": args.tutorial_steps / t2, "exact_energy": e_proj2,
+                               "rel_err": rel(e_proj2), "mc_energy_last10": float(np.mean(en2[-10:]))},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def percentile(lat, q):
     s = sorted(lat)
     return s[min(len(s) - 1, int(round(q * (len(s) - 1))))]
@@ -375,7 +463,10 @@ def main():
     ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
-    ap.add_argument("--workload", default="rbm", choices=["rbm", "resconv", "serving", "trajectory"],
+    ap.add_argument("--tutorial-steps", type=int, default=200, help="heisenberg_tutorial: SR steps per phase")
+    ap.add_argument("--seed", type=int, default=0, help="heisenberg_tutorial: random seed")
+    ap.add_argument("--workload", default="rbm",
+                    choices=["rbm", "resconv", "serving", "trajectory", "heisenberg_tutorial"],
                     help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv); "
                          "serving: a Poisson stream of config-5 jobs through quantax_gb300.serving")
     ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
@@ -407,6 +498,9 @@ def main():
         return
     if args.workload == "trajectory":
         run_trajectory(args, rank)
+        return
+    if args.workload == "heisenberg_tutorial":
+        run_tutorial(args, rank)
         return
 
     plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)

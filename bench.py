@@ -358,10 +358,20 @@ def run_trajectory(args, rank):
                           "chains": args.chains, "steps": args.steps, "forms": out}), flush=True)
 
 
-# ED ground energy of the 4x4 Heisenberg model (MSR) and the reference's trained, projected
-# ResConv(2 blocks, 8 channels) on it (tutorials/J1J2.ipynb:90, :331)
-HEIS4_ED_E0 = -44.91393283371544
-HEIS4_REFERENCE = {"energy": -44.91365075323898, "rel_err": 6.280467076974902e-06, "fidelity": 0.9999925315217684}
+# ED ground energies of the 4x4 Heisenberg and J1-J2 (J2 = 0.5) models (MSR) and the reference's
+# trained, projected ResConv(2 blocks, 8 channels) on them (tutorials/J1J2.ipynb:90, :331,
+# :374, :562). The Heisenberg figure is the projection of the unsymmetrised 200-step model
+# (the notebook's second loop updates the unprojected state); the J1-J2 one follows 200
+# steps of the projected state.
+TUTORIALS = {
+    "heisenberg_tutorial": dict(J=[1.0], n_neighbor=[1], sinhp1=False, ed=-44.91393283371544,
+                                reference={"energy": -44.91365075323898, "rel_err": 6.280467076974902e-06,
+                                           "fidelity": 0.9999925315217684,
+                                           "state": "projected_after_unsymmetrised_training"}),
+    "j1j2_tutorial": dict(J=[1.0, 0.5], n_neighbor=[1, 2], sinhp1=True, ed=-33.831693405579394,
+                          reference={"energy": -33.782434819834265, "rel_err": 0.001455989363423509,
+                                     "fidelity": 0.9971699670582732, "state": "projected_training"}),
+}
 
 
 def exact_energy(qtx, state, H):
@@ -390,21 +400,22 @@ def exact_energy(qtx, state, H):
 
 
 def run_tutorial(args, rank):
-    """The reference's 4x4 Heisenberg notebook (tutorials/J1J2.ipynb cells 1-19): ResConv(2
-    blocks, 8 channels) trained 200 SR steps (lr 0.01, 1024 SpinExchange samples, default
-    pinv solver) without symmetry, then projected on Rotation(pi/2) @ Flip() @ SpinInverse();
-    and 200 more steps of the projected state. Energies are exact sums over the 12870-state
-    sector; times are CUDA events around each phase."""
+    """The reference's 4x4 notebook (tutorials/J1J2.ipynb: cells 1-19 Heisenberg with
+    exp_by_scale, cells 21-30 J1-J2 with sinhp1_by_scale): ResConv(2 blocks, 8 channels)
+    trained 200 SR steps (lr 0.01, 1024 SpinExchange samples, default pinv solver) without
+    symmetry, then projected on Rotation(pi/2) @ Flip() @ SpinInverse(); and 200 more steps of
+    the projected state. Energies are exact sums over the 12870-state sector; times are CUDA
+    events around each phase."""
     import numpy as np
     import torch
     import quantax_gb300 as qtx
     from quantax_gb300.symmetry import Flip, Rotation, SpinInverse
+    tut = TUTORIALS[args.workload]
     qtx.set_random_seed(args.seed)
     qtx.set_default_dtype(np.float64)
     qtx.sites.Square(4, Nparticles=(8, 8))
-    H = qtx.operator.Heisenberg(msr=True)
-    model = qtx.model.ResConv(2, 8)
-    out = {}
+    H = qtx.operator.Heisenberg(J=tut["J"], n_neighbor=tut["n_neighbor"], msr=True)
+    model = qtx.model.ResConv(2, 8, final_activation=qtx.nn.sinhp1_by_scale if tut["sinhp1"] else None)
 
     def train(state, steps):
         sampler = qtx.sampler.SpinExchange(state, 1024)
@@ -431,14 +442,18 @@ def run_tutorial(args, rank):
     e_proj, _ = exact_energy(qtx, symm_state, H)
     t2, en2 = train(symm_state, args.tutorial_steps)
     e_proj2, _ = exact_energy(qtx, symm_state, H)
-    rel = lambda e: abs((e - HEIS4_ED_E0) / HEIS4_ED_E0)
+    ed = tut["ed"]
+    rel = lambda e: abs((e - ed) / ed)
     line = {
-        "metric": "relative energy error of the projected state", "workload": "heisenberg_square4_resconv2x8_tutorial",
-        "ed_energy": HEIS4_ED_E0, "sector_dim": dim, "seed": args.seed, "steps_per_phase": args.tutorial_steps,
+        "metric": "relative energy error of the projected state",
+        "workload": args.workload.replace("_tutorial", "") + "_square4_resconv2x8_tutorial",
+        "final_activation": "sinhp1_by_scale" if tut["sinhp1"] else "exp_by_scale",
+        "ed_energy": ed, "sector_dim": dim, "seed": args.seed, "steps_per_phase": args.tutorial_steps,
+        "reference": tut["reference"],
         "unsymmetrised_training": {"steps_per_s": args.tutorial_steps / t1, "exact_energy": e_plain,
                                    "rel_err": rel(e_plain), "mc_energy_last10": float(np.mean(en1[-10:]))},
         "projected_after_unsymmetrised_training": {"exact_energy": e_proj, "rel_err": rel(e_proj),
-                                                   "reference": HEIS4_REFERENCE, "nsymm": symm.nsymm},
+                                                   "nsymm": symm.nsymm},
         "projected_training": {"steps_per_s": args.tutorial_steps / t2, "exact_energy": e_proj2,
                                "rel_err": rel(e_proj2), "mc_energy_last10": float(np.mean(en2[-10:]))},
     }
@@ -463,10 +478,10 @@ def main():
     ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
-    ap.add_argument("--tutorial-steps", type=int, default=200, help="heisenberg_tutorial: SR steps per phase")
-    ap.add_argument("--seed", type=int, default=0, help="heisenberg_tutorial: random seed")
+    ap.add_argument("--tutorial-steps", type=int, default=200, help="*_tutorial: SR steps per phase")
+    ap.add_argument("--seed", type=int, default=0, help="*_tutorial: random seed")
     ap.add_argument("--workload", default="rbm",
-                    choices=["rbm", "resconv", "serving", "trajectory", "heisenberg_tutorial"],
+                    choices=["rbm", "resconv", "serving", "trajectory", "heisenberg_tutorial", "j1j2_tutorial"],
                     help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv); "
                          "serving: a Poisson stream of config-5 jobs through quantax_gb300.serving")
     ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
@@ -499,7 +514,7 @@ def main():
     if args.workload == "trajectory":
         run_trajectory(args, rank)
         return
-    if args.workload == "heisenberg_tutorial":
+    if args.workload in TUTORIALS:
         run_tutorial(args, rank)
         return
 

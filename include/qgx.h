@@ -174,7 +174,14 @@ int qgx_rbm_obar_noalloc(const float* table, int32_t n, int32_t m, int32_t has_v
 /* ---- ResConv (quantax/model/conv_nets.py:26-183) ----------------------------------- */
 /* Parameters in the reference's ravel order: per block conv1.weight (C, Cin, 3, 3),
  * conv1.bias (C), conv2.weight (C, C, 3, 3), conv2.bias (C, absent in the last block);
- * Cin = 1 in block 0. Supported: L x L periodic lattices with L*L <= 256, C in {4,8,12,16}. */
+ * Cin = 1 in block 0. Supported: L x L periodic lattices with L*L <= 256, C in {4,8,12,16}.
+ * The complex_out argument of every ResConv entry point holds flags: QGX_RESCONV_COMPLEX,
+ * complex output (pair_cpl: the first C/2 channels are the real part), and QGX_RESCONV_SINHP1,
+ * the final activation sinhp1_by_scale, psi = mean (sinh z + 1), instead of exp_by_scale,
+ * psi = mean exp z (nn/activation.py:7-32). A real sinhp1 state can be negative: its log psi
+ * carries the sign as the phase 0 or pi. */
+#define QGX_RESCONV_COMPLEX 1
+#define QGX_RESCONV_SINHP1 2
 int64_t qgx_resconv_nparams(int32_t nblocks, int32_t channels);
 int64_t qgx_resconv_table_floats(int32_t nblocks, int32_t channels);
 /* Convolution arithmetic of the forward pass (log_psi, sweep, eloc). FP32: CUDA-core FMA

@@ -93,7 +93,9 @@ def features(p, spins, L, nblocks, channels):
     return x / math.sqrt(nblocks + 1)
 
 
-def log_psi_torch(p, spins, L, nblocks, channels, complex_out=True):
+def log_psi_torch(p, spins, L, nblocks, channels, complex_out=True, sinhp1=False):
+    """log of the mean final activation: exp_by_scale, or sinhp1_by_scale (sinh z + 1) when
+    sinhp1 (quantax/nn/activation.py:7-32); complex for sinhp1 (a real psi can be negative)."""
     x = features(p, spins, L, nblocks, channels)
     ns = x.shape[0]
     if complex_out:
@@ -101,21 +103,27 @@ def log_psi_torch(p, spins, L, nblocks, channels, complex_out=True):
         z = torch.complex(x[:, :c2], x[:, c2:]).reshape(ns, -1)
     else:
         z = x.reshape(ns, -1)
+    if sinhp1:
+        z = z.to(torch.complex128)
+        m = z.real.abs().max(dim=1, keepdim=True).values
+        sig = 0.5 * (torch.exp(z - m) - torch.exp(-z - m)) + torch.exp(-m)
+        return m.squeeze(1) + torch.log(sig.sum(dim=1)) - math.log(z.shape[1])
     m = z.real.max(dim=1, keepdim=True).values
     lse = m.squeeze(1) + torch.log(torch.exp(z - m).sum(dim=1))
     return lse - math.log(z.shape[1])
 
 
 class ResConv:
-    def __init__(self, params, L, nblocks, channels, complex_out=True):
+    def __init__(self, params, L, nblocks, channels, complex_out=True, sinhp1=False):
         self.p = np.asarray(params, dtype=np.float64)
         self.L, self.nblocks, self.channels, self.complex_out = L, nblocks, channels, complex_out
+        self.sinhp1 = sinhp1
 
     def log_psi(self, s):
         s = torch.as_tensor(np.atleast_2d(s), dtype=torch.float64)
         p = torch.as_tensor(self.p)
         with torch.no_grad():
-            lp = log_psi_torch(p, s, self.L, self.nblocks, self.channels, self.complex_out)
+            lp = log_psi_torch(p, s, self.L, self.nblocks, self.channels, self.complex_out, self.sinhp1)
         return lp.numpy()
 
     def jacobian(self, s):
@@ -124,12 +132,14 @@ class ResConv:
         rows = []
         for a in range(s.shape[0]):
             p = torch.as_tensor(self.p).clone().requires_grad_(True)
-            lp = log_psi_torch(p, s[a:a + 1], self.L, self.nblocks, self.channels, self.complex_out)[0]
+            lp = log_psi_torch(p, s[a:a + 1], self.L, self.nblocks, self.channels, self.complex_out,
+                               self.sinhp1)[0]
             if self.complex_out:
                 gr, = torch.autograd.grad(lp.real, p, retain_graph=True)
                 gi, = torch.autograd.grad(lp.imag, p)
                 rows.append((gr + 1j * gi).numpy())
             else:
-                g, = torch.autograd.grad(lp, p)
+                # real output: d log |psi| (a sinhp1 psi carries its sign in the phase)
+                g, = torch.autograd.grad(lp.real, p)
                 rows.append(g.numpy())
         return np.stack(rows)

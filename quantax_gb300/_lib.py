@@ -32,6 +32,8 @@ GRAM_3XTF32 = 3
 CONV_FP32 = 0
 CONV_TF32 = 1
 CONV_BF16 = 2
+RESCONV_COMPLEX = 1
+RESCONV_SINHP1 = 2
 
 vp = C.c_void_p
 i32 = C.c_int32

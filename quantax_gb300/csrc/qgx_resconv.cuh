@@ -91,13 +91,56 @@ __device__ inline bool propose_exchange(uint32_t (&w)[8], int n, int nw, const u
   return true;
 }
 
+// sinhp1_by_scale (nn/activation.py:7-15) on one final feature z = a + i b, shifted by e^-m:
+// f = (sinh z + 1) e^-m and g = f'(z) e^-m = cosh z e^-m, as (re, im) pairs
+__device__ inline void sinhp1_shifted(float a, float b, float m, bool cplx, float* fr, float* fi, float* gr, float* gi) {
+  float sn = 0.0f, cs = 1.0f;
+  if (cplx) sincosf(b, &sn, &cs);
+  const float ep = expf(a - m), em = expf(-a - m);
+  const float sh = 0.5f * (ep - em), ch = 0.5f * (ep + em);
+  *fr = fmaf(sh, cs, expf(-m));
+  *fi = ch * sn;
+  *gr = ch * cs;
+  *gi = sh * sn;
+}
+
+// log psi = log mean_e f(z_e) of one configuration, one warp: z_e = scale * za[e] for
+// e < cpN (real parts), imaginary parts at za[cpN + e] when cplx. exp_by_scale
+// (nn/activation.py:26-32) shifts by max Re z, sinhp1_by_scale by max |Re z|. (re, im) of log psi.
+__device__ inline float2 rc_warp_log_psi(const float* za, int cpN, float scale, bool cplx, bool sinhp1, int lane) {
+  float m = -INFINITY;
+  for (int e = lane; e < cpN; e += 32) {
+    const float a = za[e] * scale;
+    m = fmaxf(m, sinhp1 ? fabsf(a) : a);
+  }
+  m = warp_max(m);
+  float sr = 0.0f, si = 0.0f;
+  for (int e = lane; e < cpN; e += 32) {
+    if (sinhp1) {
+      float fr, fi, gr, gi;
+      sinhp1_shifted(za[e] * scale, cplx ? za[cpN + e] * scale : 0.0f, m, cplx, &fr, &fi, &gr, &gi);
+      sr += fr;
+      si += fi;
+    } else {
+      const float ex = expf(za[e] * scale - m);
+      float sn = 0.0f, cs = 1.0f;
+      if (cplx) sincosf(za[cpN + e] * scale, &sn, &cs);
+      sr = fmaf(ex, cs, sr);
+      si = fmaf(ex, sn, si);
+    }
+  }
+  sr = warp_sum(sr);
+  si = warp_sum(si);
+  return make_float2(m + 0.5f * logf(sr * sr + si * si) - logf((float)cpN), atan2f(si, sr));
+}
+
 }  // namespace
 
 // writes both tensor-core weight images from the FP32 part of the table (resconv_tc.cu)
 int rc_prepare_tc_images(float* table, int B, int C, cudaStream_t st);
 
 // tensor-core forward (resconv_tc.cu); kind 0: TF32 operands, 1: BF16 operands
-int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,
-                         const int64_t* n_live, float2* out, int kind, cudaStream_t st);
+int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg,
+                         int64_t ncfg, const int64_t* n_live, float2* out, int kind, cudaStream_t st);
 
 }  // namespace qgx

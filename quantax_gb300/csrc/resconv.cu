@@ -31,8 +31,14 @@ constexpr int kMaxSitesConv = 256;  // L <= 16
 struct ConvNet {
   int L, N, B, C;
   bool cplx;
-  int prec;  // QGX_CONV_*: arithmetic of the forward convolutions
+  int prec;     // QGX_CONV_*: arithmetic of the forward convolutions
+  bool sinhp1;  // final activation sinhp1_by_scale instead of exp_by_scale
 };
+
+// the complex_out argument of the entry points: QGX_RESCONV_COMPLEX | QGX_RESCONV_SINHP1
+inline ConvNet make_net(int L, int B, int C, int out_flags, int prec) {
+  return ConvNet{L, L * L, B, C, (out_flags & QGX_RESCONV_COMPLEX) != 0, prec, (out_flags & QGX_RESCONV_SINHP1) != 0};
+}
 
 __host__ __device__ inline int64_t nparams_rc(int B, int C) {
   // reference ravel order: per block conv1.weight, conv1.bias, conv2.weight, conv2.bias (not in the last block)
@@ -166,30 +172,12 @@ __global__ void __launch_bounds__(kFwdThreads)
       conv_layer<C>(Q, C, X, Wl, nbr, N, S, 1);
     }
     __syncthreads();
-    // log sum exp over (channel, site) per sample, one warp per sample
+    // log of the mean final activation over (channel, site) per sample, one warp per sample
     const float fs = rsqrtf((float)(net.B + 1));
     const int cp = net.cplx ? C / 2 : C;
     for (int a = warp; a < s_here; a += kFwdThreads / 32) {
-      const float* xa = X + (int64_t)a * C * N;
-      float m = -INFINITY;
-      for (int e = lane; e < cp * N; e += 32) m = fmaxf(m, xa[e] * fs);
-      m = warp_max(m);
-      float sr = 0.0f, si = 0.0f;
-      for (int e = lane; e < cp * N; e += 32) {
-        const float re = xa[e] * fs - m;
-        const float im = net.cplx ? xa[cp * N + e] * fs : 0.0f;
-        const float ex = expf(re);
-        float sn, cs;
-        sincosf(im, &sn, &cs);
-        sr = fmaf(ex, cs, sr);
-        si = fmaf(ex, sn, si);
-      }
-      sr = warp_sum(sr);
-      si = warp_sum(si);
-      if (lane == 0) {
-        const float lr = m + 0.5f * logf(sr * sr + si * si) - logf((float)(cp * N));
-        out[base + a] = make_float2(lr, atan2f(si, sr));
-      }
+      const float2 lp = rc_warp_log_psi(X + (int64_t)a * C * N, cp * N, fs, net.cplx, net.sinhp1, lane);
+      if (lane == 0) out[base + a] = lp;
     }
   }
 }
@@ -592,9 +580,9 @@ __global__ void __launch_bounds__(kJacThreads)
       conv_layer<C>(Qa, C, X, W, nbr, N, 1, 1);
     }
     __syncthreads();
-    // ---- output cotangents: w = exp(z - logsumexp z)
+    // ---- output cotangents: w_e = f'(z_e) / sum f, f = exp (exp_by_scale) or sinh + 1
     float m = -INFINITY;
-    for (int e = threadIdx.x; e < cp * N; e += blockDim.x) m = fmaxf(m, X[e] * fs);
+    for (int e = threadIdx.x; e < cp * N; e += blockDim.x) m = fmaxf(m, net.sinhp1 ? fabsf(X[e] * fs) : X[e] * fs);
     m = warp_max(m);
     if (lane == 0) red[0][warp] = m;
     __syncthreads();
@@ -603,6 +591,13 @@ __global__ void __launch_bounds__(kJacThreads)
     __syncthreads();
     float sr = 0.0f, si = 0.0f;
     for (int e = threadIdx.x; e < cp * N; e += blockDim.x) {
+      if (net.sinhp1) {
+        float fr, fi, gr, gi;
+        sinhp1_shifted(X[e] * fs, net.cplx ? X[cp * N + e] * fs : 0.0f, m, net.cplx, &fr, &fi, &gr, &gi);
+        sr += fr;
+        si += fi;
+        continue;
+      }
       const float ex = expf(X[e] * fs - m);
       float sn = 0.0f, cs = 1.0f;
       if (net.cplx) sincosf(X[cp * N + e] * fs, &sn, &cs);
@@ -626,11 +621,18 @@ __global__ void __launch_bounds__(kJacThreads)
     const float den = sr * sr + si * si;
     const float ir = sr / den, ii = -si / den;
     for (int e = threadIdx.x; e < cp * N; e += blockDim.x) {
-      const float ex = expf(X[e] * fs - m);
-      float sn = 0.0f, cs = 1.0f;
-      if (net.cplx) sincosf(X[cp * N + e] * fs, &sn, &cs);
-      const float ar = ex * cs, ai = ex * sn;
-      const float ur = ar * ir - ai * ii, ui = ar * ii + ai * ir;  // exp(z) / sum
+      float ar, ai;
+      if (net.sinhp1) {
+        float fr, fi;
+        sinhp1_shifted(X[e] * fs, net.cplx ? X[cp * N + e] * fs : 0.0f, m, net.cplx, &fr, &fi, &ar, &ai);
+      } else {
+        const float ex = expf(X[e] * fs - m);
+        float sn = 0.0f, cs = 1.0f;
+        if (net.cplx) sincosf(X[cp * N + e] * fs, &sn, &cs);
+        ar = ex * cs;
+        ai = ex * sn;
+      }
+      const float ur = ar * ir - ai * ii, ui = ar * ii + ai * ir;  // f'(z) / sum f
       const float wr = vr * ur - vi * ui, wi = vr * ui + vi * ur;  // times v
       if (net.cplx) {
         G[e] = wr * fs;               // d Re / d y_c
@@ -728,7 +730,7 @@ int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg
 int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                    float2* out, cudaStream_t st) {
   if (net.prec != QGX_CONV_FP32)
-    return rc_launch_forward_tc(table, net.L, net.B, net.C, net.cplx, cfg, ncfg, n_live, out,
+    return rc_launch_forward_tc(table, net.L, net.B, net.C, net.cplx, net.sinhp1, cfg, ncfg, n_live, out,
                                 net.prec == QGX_CONV_BF16 ? 1 : 0, st);
   switch (net.C) {
     case 4: return launch_forward_c<4>(table, net, cfg, ncfg, n_live, out, st);
@@ -794,9 +796,10 @@ std::vector<SweepGraph> g_graphs;
 uint64_t g_graph_clock = 0;
 cudaStream_t g_capture_stream[64] = {};
 
-bool valid_net(int L, int B, int C, int cplx) {
+bool valid_net(int L, int B, int C, int out_flags) {
   return L >= 3 && L * L <= kMaxSitesConv && B >= 1 && B <= 64 && (C == 4 || C == 8 || C == 12 || C == 16) &&
-         (!cplx || C % 2 == 0);
+         (out_flags & ~(QGX_RESCONV_COMPLEX | QGX_RESCONV_SINHP1)) == 0 &&
+         (!(out_flags & QGX_RESCONV_COMPLEX) || C % 2 == 0);
 }
 
 bool valid_prec(int p) { return p == QGX_CONV_FP32 || p == QGX_CONV_TF32 || p == QGX_CONV_BF16; }
@@ -845,7 +848,7 @@ int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t 
   QGX_CHECK_ARG(valid_net(L, nblocks, channels, complex_out) && valid_prec(conv_precision) && ns >= 0);
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && log_psi);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
+  const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
   return launch_forward(table, net, spins, ns, nullptr, reinterpret_cast<float2*>(log_psi), as_cuda(stream));
 }
 
@@ -864,7 +867,7 @@ int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels,
                int32_t conv_precision, const SymmDev* sym, uint32_t* spins, float* log_psi, int32_t* accepts,
                int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0, float reweight, const int32_t* nbr, int32_t z,
                int32_t hop, void* workspace, cudaStream_t st) {
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
+  const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
   const int nw = words_for(net.N);
   char* ws = static_cast<char*>(workspace);
   uint32_t* prop = reinterpret_cast<uint32_t*>(ws);
@@ -910,7 +913,7 @@ int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels,
   key.L = L;
   key.B = nblocks;
   key.C = channels;
-  key.cplx = complex_out != 0;
+  key.cplx = complex_out;  // the output flags
   key.prec = conv_precision;
   key.z = z;
   key.hop = hop;
@@ -1010,7 +1013,7 @@ int eloc_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, 
               int32_t conv_precision, const SymmDev* sym, const qgx_operator_t* op, const uint32_t* spins, int64_t ns,
               double* eloc_re, double* eloc_im, void* workspace, cudaStream_t st) {
   const int max_conn = op->n_f1 + op->n_f2;
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
+  const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
   const int nw = words_for(net.N);
   const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
   char* ws = static_cast<char*>(workspace);
@@ -1041,7 +1044,7 @@ int eloc_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, 
 int jacobian_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
                   const SymmDev* sym, const uint32_t* spins, int64_t ns, float* O_re, float* O_im, int64_t ldo,
                   void* workspace, int64_t workspace_bytes, cudaStream_t st) {
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, QGX_CONV_FP32};
+  const ConvNet net = make_net(L, nblocks, channels, complex_out, QGX_CONV_FP32);
   char* ws = static_cast<char*>(workspace);
   int64_t scratch_bytes = workspace_bytes;
   SymmJac sj{nullptr, nullptr, nullptr, nullptr, 1};
@@ -1122,7 +1125,7 @@ int qgx_resconv_log_psi_symm(const float* table, int32_t L, int32_t nblocks, int
   QGX_CHECK_ARG(table && spins && log_psi && workspace);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_log_psi_symm_workspace_bytes(L, ns, sym.nsymm));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  ConvNet net{L, L * L, nblocks, channels, complex_out != 0, conv_precision};
+  const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
   return symm_forward(table, net, &sym, spins, ns, nullptr, reinterpret_cast<float2*>(log_psi),
                       static_cast<char*>(workspace), as_cuda(stream));
 }
@@ -1140,7 +1143,7 @@ int qgx_resconv_jacobian(const float* table, int32_t L, int32_t nblocks, int32_t
   QGX_CHECK_ARG(ldo >= qgx_resconv_nparams(nblocks, channels));
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && O_re && workspace && workspace_bytes > 0);
-  QGX_CHECK_ARG(!complex_out || O_im);
+  QGX_CHECK_ARG(!(complex_out & QGX_RESCONV_COMPLEX) || O_im);
   return jacobian_impl(table, L, nblocks, channels, complex_out, nullptr, spins, ns, O_re, O_im, ldo, workspace,
                        workspace_bytes, as_cuda(stream));
 }
@@ -1161,7 +1164,7 @@ int qgx_resconv_jacobian_symm(const float* table, int32_t L, int32_t nblocks, in
   QGX_CHECK_ARG(ldo >= qgx_resconv_nparams(nblocks, channels));
   if (ns == 0) return QGX_OK;
   QGX_CHECK_ARG(table && spins && O_re && workspace);
-  QGX_CHECK_ARG(!complex_out || O_im);
+  QGX_CHECK_ARG(!(complex_out & QGX_RESCONV_COMPLEX) || O_im);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_jacobian_symm_workspace_bytes(L, nblocks, channels, ns, sym.nsymm));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   return jacobian_impl(table, L, nblocks, channels, complex_out, &sym, spins, ns, O_re, O_im, ldo, workspace,

@@ -60,7 +60,7 @@ struct TcCfg {
 
 struct TcShape {
   int L, N, Lp, NP, B, C, S, ntiles, rows_tot;
-  bool cplx;
+  bool cplx, sinhp1;
   int oP, oQ, oW, oBar;  // byte offsets in shared memory
   int wbuf;              // bytes between the two weight buffers
   int smem;
@@ -79,6 +79,7 @@ inline TcShape tc_shape(int L, int B, int C, bool cplx, int esz, int S) {
   s.B = B;
   s.C = C;
   s.cplx = cplx;
+  s.sinhp1 = false;
   s.S = S;
   s.ntiles = (S * s.NP + 127) / 128;
   s.rows_tot = kGuard + s.ntiles * 128 + kGuard;
@@ -413,21 +414,8 @@ struct TcForward {
     __syncthreads();
     const int cp = sh.cplx ? sh.C / 2 : sh.C;
     for (int a = warp; a < s_here; a += kThreads / 32) {
-      const float* za = Z + a * sh.C * N;
-      float mx = -INFINITY;
-      for (int e = lane; e < cp * N; e += 32) mx = fmaxf(mx, za[e]);
-      mx = warp_max(mx);
-      float sr = 0.0f, si = 0.0f;
-      for (int e = lane; e < cp * N; e += 32) {
-        const float ex = expf(za[e] - mx);
-        float sn = 0.0f, cs = 1.0f;
-        if (sh.cplx) sincosf(za[cp * N + e], &sn, &cs);
-        sr = fmaf(ex, cs, sr);
-        si = fmaf(ex, sn, si);
-      }
-      sr = warp_sum(sr);
-      si = warp_sum(si);
-      if (lane == 0) out[a] = make_float2(mx + 0.5f * logf(sr * sr + si * si) - logf((float)(cp * N)), atan2f(si, sr));
+      const float2 lp = rc_warp_log_psi(Z + a * sh.C * N, cp * N, 1.0f, sh.cplx, sh.sinhp1, lane);
+      if (lane == 0) out[a] = lp;
     }
     __syncthreads();  // Z is overwritten by the next forward's P; out may be read next
     return true;
@@ -549,11 +537,12 @@ int tc_smem_request(const TcShape& sh) {
 }
 
 template <int KIND>
-int launch_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,
+int launch_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg, int64_t ncfg,
               const int64_t* n_live, float2* out, cudaStream_t st) {
   using T = TcLaunch<KIND>;
   TcShape sh;
   if (!tc_launch_shape<KIND>(L, B, C, cplx, &sh)) return QGX_ERR_UNSUPPORTED;
+  sh.sinhp1 = sinhp1;
   const uint8_t* wimg = reinterpret_cast<const uint8_t*>(table) + tc_image_offset(B, C, KIND);
   auto k = rc_forward_tc_kernel<KIND, T::WG, T::RPT, T::CTAS>;
   const int smem = tc_smem_request<KIND>(sh);
@@ -566,11 +555,11 @@ int launch_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t
 
 }  // namespace
 
-int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, const uint32_t* cfg, int64_t ncfg,
-                         const int64_t* n_live, float2* out, int kind, cudaStream_t st) {
+int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg,
+                         int64_t ncfg, const int64_t* n_live, float2* out, int kind, cudaStream_t st) {
   if (C < 1 || C > kCh || L < 3 || L + 3 > kGuard) return QGX_ERR_UNSUPPORTED;
-  if (kind == 1) return launch_tc<1>(table, L, B, C, cplx, cfg, ncfg, n_live, out, st);
-  return launch_tc<0>(table, L, B, C, cplx, cfg, ncfg, n_live, out, st);
+  if (kind == 1) return launch_tc<1>(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, st);
+  return launch_tc<0>(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, st);
 }
 
 }  // namespace qgx

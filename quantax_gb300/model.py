@@ -141,10 +141,14 @@ class ResConv:
         """conv_precision: arithmetic of the forward convolutions used by sampling and local
         energies -- "fp32" (CUDA cores), "tf32" or "bf16" (tensor-core operands, FP32
         accumulation). The log-derivatives are always computed in FP32."""
+        from . import nn
         from .global_defs import get_lattice
-        if kernel_size != 3 or final_activation is not None or trans_symm is not None:
-            raise NotImplementedError("quantax_gb300 ResConv: 3x3 kernels, exp_by_scale output and the default "
-                                      "translation symmetrisation only")
+        if kernel_size != 3 or trans_symm is not None:
+            raise NotImplementedError("quantax_gb300 ResConv: 3x3 kernels and the default translation "
+                                      "symmetrisation only")
+        if final_activation not in (None, nn.exp_by_scale, nn.sinhp1_by_scale):
+            raise NotImplementedError("ResConv final_activation: quantax_gb300.nn.exp_by_scale or sinhp1_by_scale")
+        self.sinhp1 = final_activation is nn.sinhp1_by_scale
         if np.dtype(dtype) != np.float32:
             raise NotImplementedError("ResConv runs with float32 parameters")
         lat = get_lattice()
@@ -190,8 +194,14 @@ class ResConv:
         self._conv_precision = p
         self._conv_code = codes[p]
 
+    @property
+    def signed_output(self) -> bool:
+        """A real output that can be negative (sinhp1): log psi carries the sign as its phase."""
+        return self.sinhp1 and not self.complex_output
+
     def _args(self):
-        return (self.L, self.nblocks, self.channels, int(self.complex_output))
+        flags = (_lib.RESCONV_COMPLEX if self.complex_output else 0) | (_lib.RESCONV_SINHP1 if self.sinhp1 else 0)
+        return (self.L, self.nblocks, self.channels, flags)
 
     def _fwd_args(self):
         return self._args() + (self._conv_code,)

@@ -151,8 +151,8 @@ class Variational:
         else:
             ws = self.workspace("fwd_symm", self._model.log_psi_workspace_bytes(packed.shape[0], self._sym))
             self._model.log_psi(self._table, packed, out, self._sym, ws)
-        # a projected real state can be negative: its phase (0 or pi) carries the sign
-        if self.is_complex or self._sym is not None:
+        # a projected or sinhp1 real state can be negative: its phase (0 or pi) carries the sign
+        if self.is_complex or self._sym is not None or getattr(self._model, "signed_output", False):
             return torch.view_as_complex(out)
         return out[:, 0].contiguous()
 

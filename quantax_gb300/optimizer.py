@@ -286,19 +286,36 @@ class _MomentumSR(SR):
         _lib.call("qgx_scale_columns", _lib.ptr(Obar), rows, np_, Obar.stride(0), _lib.ptr(s),
                   _lib.stream_ptr())
 
+    # the momentum vectors holding steps are stored in the default dtype, as the reference's
+    # solve returns them (sr.py:111); the squared ones stay real (sr.py:300-301, 382-383)
+    _step_like = ("_last_step", "_m")
+
     def save(self, file) -> None:
-        """The optimizer's internal quantities (numpy .npz)."""
+        """The optimizer's internal quantities, in the reference's file format (its leaf
+        order, sr.py:258-262, 344-349, 424-429): one .npy record per quantity."""
         import numpy as np
-        vals = {k: (getattr(self, k).cpu().numpy() if torch.is_tensor(getattr(self, k)) else getattr(self, k))
-                for k in self._saved}
-        np.savez(file, **vals)
+        from .checkpoint import write_leaves
+        from .global_defs import is_default_cpl
+        leaves = []
+        for k in self._saved:
+            v = getattr(self, k)
+            if torch.is_tensor(v):
+                v = v.cpu().numpy().astype(np.float64)
+                if k in self._step_like and is_default_cpl():
+                    v = v.astype(np.complex128)
+            leaves.append(v)
+        write_leaves(file, leaves)
 
     def load(self, file) -> None:
-        import numpy as np
-        with np.load(file) as d:
-            for k in self._saved:
-                v = d[k]
-                setattr(self, k, torch.as_tensor(v, device=self._dev) if v.ndim else v.item())
+        """Quantities saved by save() or by the reference's optimizer."""
+        from .checkpoint import read_leaves
+        for k, v in zip(self._saved, read_leaves(file, len(self._saved))):
+            if v.ndim:
+                if v.shape != (self._state.nparams,):
+                    raise ValueError(f"{k}: {v.shape[0]} entries in the file, the state has {self._state.nparams}")
+                setattr(self, k, torch.as_tensor(v.real, dtype=torch.float64, device=self._dev))
+            else:
+                setattr(self, k, v.item())
 
 
 class SPRING(_MomentumSR):

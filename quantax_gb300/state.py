@@ -59,9 +59,9 @@ class Variational:
         self._sites = get_sites()  # the lattice this state was built on (kept, not re-read)
         params = model.init_params
         if param_file is not None:
-            params = np.load(param_file).astype(np.float32).reshape(-1)
-            if params.size != model.nparams:
-                raise ValueError(f"{param_file} holds {params.size} parameters, the model has {model.nparams}")
+            # the reference's checkpoint (equinox leaf records) or a flat .npy of the parameters
+            from .checkpoint import load_model
+            params = load_model(param_file, model)
         self._params = torch.as_tensor(params, dtype=torch.float32, device=self._dev).contiguous()
         self._table = torch.empty(max(model.table_floats(), 4), dtype=torch.float32, device=self._dev)
         self._flag = torch.zeros(1, dtype=torch.int32, device=self._dev)
@@ -271,4 +271,7 @@ class Variational:
         self._refresh()
 
     def save(self, file) -> None:
-        np.save(file, self._params.cpu().numpy())
+        """The parameters in the reference's checkpoint format (variational.py:581-587):
+        quantax loads the file with Variational(model, file), and so does this class."""
+        from .checkpoint import save_model
+        save_model(file, self._model, self._params.cpu().numpy())

@@ -91,7 +91,7 @@ def test_momentum_sr_save_load(cuda, kind, tmp_path):
     rng = np.random.default_rng(7)
     for _ in range(2):
         _dev_step(opt, *_inputs(rng, 64, np_))
-    f = tmp_path / f"{kind}.npz"
+    f = tmp_path / f"{kind}.eqx"
     opt.save(f)
     A, b = _inputs(rng, 64, np_)
     restored = _make(kind, file=f)

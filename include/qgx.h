@@ -53,6 +53,9 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
 #define QGX_GRAM_TF32 1    /* tcgen05 kind::tf32, FP32 accumulation in TMEM */
 #define QGX_GRAM_BF16 2    /* tcgen05 kind::f16 with bf16 operands, FP32 accumulation */
 #define QGX_GRAM_3XTF32 3  /* tcgen05 split-TF32 (hi*hi + hi*lo + lo*hi), FP32 accuracy */
+#define QGX_GRAM_FP64 4    /* FP64 SIMT products and accumulation: the exact Gram of the FP32
+                            * operand up to FP64 rounding (for solves that keep eigenvalues
+                            * below FP32 resolution, e.g. lstsq_pinv_eig(rtol=1e-9)) */
 
 /* ---- library ----------------------------------------------------------------- */
 int qgx_abi_version(void);
@@ -170,6 +173,21 @@ int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias,
 int qgx_rbm_obar_noalloc(const float* table, int32_t n, int32_t m, int32_t has_vbias,
                          const uint32_t* spins, const double* r, int64_t ns, float* Obar,
                          int64_t ldo, double* omean, qgx_stream_t stream);
+
+/* ---- RBM_Conv (quantax/model/shallow_nets.py:129-190) ---------------------------------
+ * psi = prod_{c,x} cosh(theta_{c,x}), theta_{c,x} = b_c + sum_k W_c[(k - x + lo) mod L] s_k on an
+ * L0 x L1 periodic lattice (L1 = 1 for a chain; lo = (L - 1) / 2 per axis, the circular SAME
+ * convolution with a lattice-sized kernel). Parameters: W (channels x L0 x L1, row-major), then
+ * b (channels). It is the dense RBM with n = L0 L1 visible and m = channels L0 L1 <= 2048
+ * hidden units: qgx_rbm_log_psi / qgx_rbm_sweep / qgx_rbm_eloc run on its table with those
+ * n and m. */
+int64_t qgx_rbm_conv_table_floats(int32_t L0, int32_t L1, int32_t channels);
+int qgx_rbm_conv_prepare(const float* params, int32_t L0, int32_t L1, int32_t channels, float* table,
+                         qgx_stream_t stream);
+/* Per-sample log-derivatives of the shared weights and biases (ns x (channels L0 L1 +
+ * channels), row stride ldo floats, the parameter order above). */
+int qgx_rbm_conv_jacobian(const float* table, int32_t L0, int32_t L1, int32_t channels,
+                          const uint32_t* spins, int64_t ns, float* O, int64_t ldo, qgx_stream_t stream);
 
 /* ---- ResConv (quantax/model/conv_nets.py:26-183) ----------------------------------- */
 /* Parameters in the reference's ravel order: per block conv1.weight (C, Cin, 3, 3),

@@ -79,3 +79,45 @@ def init_normal(N, M, std=0.01, seed=0, visible_bias=False):
     b = rng.normal(0.0, std, M).astype(np.float32)
     a = rng.normal(0.0, std, N).astype(np.float32) if visible_bias else None
     return W, b, a
+
+
+class RBMConv:
+    """RBM_Conv (quantax/model/shallow_nets.py:129-190): theta[c, x] = b_c + sum_d W[c, d]
+    s[x + d - lo] over the periodic lattice (lo = (L - 1) // 2 per axis: the circular SAME
+    convolution with a lattice-sized kernel, cross-correlation as lax.conv computes it),
+    log psi = sum_{c,x} log cosh theta[c, x]. Written with lattice rolls, independently of the
+    device's dense expansion. W: (C, L0, L1), b: (C,); a chain is L1 = 1."""
+
+    def __init__(self, W, b):
+        self.W = np.asarray(W, dtype=np.float64)
+        self.b = np.asarray(b, dtype=np.float64)
+        self.C, self.L0, self.L1 = self.W.shape
+        self.lo = ((self.L0 - 1) // 2, (self.L1 - 1) // 2)
+
+    def _shifted(self, s):
+        """(ns, L0, L1, L0, L1): [..., d0, d1] = s[x + d - lo] as a lattice over x."""
+        s = np.asarray(s, dtype=np.float64).reshape(-1, self.L0, self.L1)
+        out = np.empty(s.shape + (self.L0, self.L1))
+        for d0 in range(self.L0):
+            for d1 in range(self.L1):
+                out[..., d0, d1] = np.roll(s, (self.lo[0] - d0, self.lo[1] - d1), axis=(1, 2))
+        return out
+
+    def theta(self, s):
+        sh = self._shifted(s)  # (ns, x0, x1, d0, d1)
+        return np.einsum("cde,nxyde->ncxy", self.W, sh) + self.b[None, :, None, None]
+
+    def log_psi(self, s):
+        th = self.theta(np.atleast_2d(s))
+        return logcosh(th).reshape(th.shape[0], -1).sum(axis=1)
+
+    def jacobian(self, s):
+        s = np.atleast_2d(s)
+        t = np.tanh(self.theta(s))  # (ns, C, x0, x1)
+        sh = self._shifted(s)
+        gW = np.einsum("ncxy,nxyde->ncde", t, sh).reshape(s.shape[0], -1)
+        gb = t.reshape(t.shape[0], self.C, -1).sum(axis=2)
+        return np.concatenate([gW, gb], axis=1)
+
+    def params(self):
+        return np.concatenate([self.W.ravel(), self.b])

@@ -11,6 +11,8 @@ The leaf order of the two models follows from their dataclass fields:
 
   RBM_Dense = SingleDense (quantax/model/shallow_nets.py:35-78): layers = (Linear, Lambda,
     prod_by_log), holomorphic  ->  Linear.weight (M, N), Linear.bias (M,) [use_bias], holomorphic.
+  RBM_Conv = SingleConv (shallow_nets.py:129-170): layers = (ReshapeConv, Conv, Lambda,
+    prod_by_log), holomorphic  ->  Conv.weight (C, 1, *lattice), Conv.bias (C, 1[, 1]), holomorphic.
   ResConv (quantax/model/conv_nets.py:95-183): fields layers, holomorphic (from Sequential,
     quantax/nn/modules.py:9-37), then nblocks, channels, kernel_size, final_activation,
     trans_symm, dtype, out_dtype; layers = (ReshapeConv, _ConvBlock..., final layer,
@@ -34,6 +36,13 @@ PathOrFile = Union[str, "os.PathLike", BinaryIO]
 def model_layout(model) -> Tuple[List[Tuple[str, tuple]], List[Tuple[str, object]]]:
     """(array leaves as (name, shape), number leaves as (name, value)) of a model."""
     kind = getattr(model, "kind", None)
+    if kind == "rbm" and getattr(model, "conv", False):
+        # SingleConv: layers = (ReshapeConv, Conv, Lambda, prod_by_log), holomorphic
+        dims = (model.L0,) if model.L1 == 1 else (model.L0, model.L1)
+        arrays = [("layers[1].weight", (model.channels, 1) + dims)]
+        if model.use_bias:
+            arrays.append(("layers[1].bias", (model.channels,) + (1,) * len(dims)))
+        return arrays, [("holomorphic", False)]
     if kind == "rbm":
         if getattr(model, "visible_bias", False):
             raise ValueError("the reference's RBM_Dense has no visible bias: no checkpoint layout")
@@ -98,7 +107,8 @@ def save_model(file: PathOrFile, model, params: np.ndarray) -> None:
         leaves.append(p[off:off + n].reshape(shape))
         off += n
     if model.kind == "rbm" and not model.use_bias:
-        off += model.M  # the bias entries kept at zero here are not leaves of the reference model
+        # the bias entries kept at zero here are not leaves of the reference model
+        off += model.channels if getattr(model, "conv", False) else model.M
     if off != p.size:
         raise ValueError(f"{p.size} parameters, the layout holds {off}")
     leaves += [v for _, v in numbers]
@@ -126,7 +136,7 @@ def load_model(file: PathOrFile, model) -> np.ndarray:
             raise ValueError(f"{name}: complex parameters are not supported")
         parts.append(np.asarray(r, dtype=np.float32).reshape(-1))
     if model.kind == "rbm" and not model.use_bias:
-        parts.append(np.zeros(model.M, dtype=np.float32))
+        parts.append(np.zeros(model.channels if getattr(model, "conv", False) else model.M, dtype=np.float32))
     for (name, want), r in zip(numbers, recs[len(arrays):]):
         got = r.item()
         if got != want:

@@ -1,7 +1,9 @@
 // Gram matrices of the SR / MinSR solve (quantax/optimizer/solver.py:139 T = A A^T and
-// :157 S = A^T A), FP32 operands and FP32 accumulation, written as FP64 for the solver.
+// :157 S = A^T A), FP32 operands, written as FP64 for the solver.
 //
-// This file holds the FP32 SIMT path (QGX_GRAM_FP32): 128 x 128 output tiles, 256
+// This file holds the SIMT paths: QGX_GRAM_FP32 (FP32 accumulation) and QGX_GRAM_FP64 (FP64
+// products and accumulation: a product of two FP32 numbers is exact in FP64, so the result is
+// the Gram of the FP32 matrix up to FP64 rounding). 128 x 128 output tiles, 256
 // threads with 8 x 8 register micro-tiles, K staged through shared memory in chunks of
 // 16 with a register prefetch of the next chunk. Only tiles on or below the diagonal
 // are computed; each off-diagonal tile is written twice (itself and its mirror). The
@@ -30,7 +32,7 @@ __device__ inline float load_elem(const float* __restrict__ A, int64_t lda, int6
   return TRANS ? __ldg(A + kk * lda + vec) : __ldg(A + vec * lda + kk);
 }
 
-template <bool TRANS>
+template <bool TRANS, typename ACC>
 __global__ void __launch_bounds__(NT, 1)
     gram_simt_kernel(const float* __restrict__ A, int64_t nvec, int64_t klen, int64_t lda, double* __restrict__ T,
                      int64_t ldt) {
@@ -83,11 +85,11 @@ __global__ void __launch_bounds__(NT, 1)
     }
   };
 
-  float acc[8][8];
+  ACC acc[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    for (int j = 0; j < 8; ++j) acc[i][j] = ACC(0);
 
   const int64_t nk = (klen + BK - 1) / BK;
   gload(0);
@@ -110,7 +112,7 @@ __global__ void __launch_bounds__(NT, 1)
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 8; ++j) acc[i][j] = fma((ACC)a[i], (ACC)b[j], acc[i][j]);
     }
     if (kc + 1 < nk) sstore(buf ^ 1);
     __syncthreads();
@@ -131,12 +133,12 @@ __global__ void __launch_bounds__(NT, 1)
   }
 }
 
-template <bool TRANS>
+template <bool TRANS, typename ACC = float>
 int launch_gram_simt(const float* A, int64_t nvec, int64_t klen, int64_t lda, double* T, int64_t ldt, cudaStream_t st) {
   const int64_t nb = (nvec + BM - 1) / BM;
   const int64_t tiles = nb * (nb + 1) / 2;
   if (tiles > 0x7fffffff) return QGX_ERR_UNSUPPORTED;
-  gram_simt_kernel<TRANS><<<(unsigned)tiles, NT, 0, st>>>(A, nvec, klen, lda, T, ldt);
+  gram_simt_kernel<TRANS, ACC><<<(unsigned)tiles, NT, 0, st>>>(A, nvec, klen, lda, T, ldt);
   return launch_status();
 }
 
@@ -153,6 +155,7 @@ int qgx_gram(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, in
   if (rows == 0) return QGX_OK;
   QGX_CHECK_ARG(A && T);
   if (mode == QGX_GRAM_FP32) return launch_gram_simt<false>(A, rows, k, lda, T, ldt, as_cuda(stream));
+  if (mode == QGX_GRAM_FP64) return launch_gram_simt<false, double>(A, rows, k, lda, T, ldt, as_cuda(stream));
   if (mode == QGX_GRAM_TF32 || mode == QGX_GRAM_BF16 || mode == QGX_GRAM_3XTF32)
     return gram_tc(A, rows, k, lda, T, ldt, mode, as_cuda(stream));
   return QGX_ERR_ARG;

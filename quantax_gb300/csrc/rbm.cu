@@ -33,11 +33,11 @@ struct RbmTable {
   const float* a;   // N (zeros without a visible bias)
 };
 
-// hidden units padded to a compiled width: 128, 256, 384, 512 or 1024 (padded units have
+// hidden units padded to a compiled width: 128, 256, 384, 512, 1024 or 2048 (padded units have
 // zero weights and bias, so cosh = 1, sinh = 0 and they leave every ratio unchanged)
 __host__ __device__ inline int padded_m(int m) {
   const int p = (m + 127) / 128 * 128;
-  return (p > 512 && p <= 1024) ? 1024 : p;
+  return p > 1024 ? 2048 : ((p > 512) ? 1024 : p);
 }
 
 // floats of the table, rounded to a multiple of 4 so staging can use 16-byte copies
@@ -553,6 +553,95 @@ __global__ void __launch_bounds__(NT)
 }
 
 // ---------------------------------------------------------------------------------------
+// RBM_Conv (quantax/model/shallow_nets.py:129-190): one circular convolution over the whole
+// lattice, theta_{c,x} = b_c + sum_k W_c[(k - x + lo) mod L] s_k per lattice axis (lo =
+// (L - 1) / 2, SAME padding), psi = prod_{c,x} cosh theta_{c,x}. It is the dense RBM with
+// m = C N hidden units (c, x) whose weights are translated copies of W_c: the conv table is
+// that dense table, followed by the conv parameters (W_c row-major over the lattice, then b).
+struct ConvGeom {
+  int L0, L1, lo0, lo1, N, C;
+};
+
+// index into W_c of the weight joining site k to output x
+__host__ __device__ inline int conv_tap(const ConvGeom& g, int k, int x) {
+  const int k0 = k / g.L1, k1 = k % g.L1, x0 = x / g.L1, x1 = x % g.L1;
+  const int d0 = ((k0 - x0 + g.lo0) % g.L0 + g.L0) % g.L0;
+  const int d1 = ((k1 - x1 + g.lo1) % g.L1 + g.L1) % g.L1;
+  return d0 * g.L1 + d1;
+}
+
+// the site whose weight to output x is W_c[d]: inverse of conv_tap in k
+__device__ inline int conv_site(const ConvGeom& g, int x, int d) {
+  const int x0 = x / g.L1, x1 = x % g.L1, d0 = d / g.L1, d1 = d % g.L1;
+  const int k0 = ((x0 + d0 - g.lo0) % g.L0 + g.L0) % g.L0;
+  const int k1 = ((x1 + d1 - g.lo1) % g.L1 + g.L1) % g.L1;
+  return k0 * g.L1 + k1;
+}
+
+__host__ __device__ inline int64_t conv_param_floats(int N, int C) { return (int64_t)C * N + C; }
+
+__global__ void conv_prepare_kernel(const float* __restrict__ params, ConvGeom g, int mp, float* __restrict__ out) {
+  const int n = g.N, m = g.C * g.N;
+  const int64_t nm = (int64_t)n * mp;
+  const int64_t tot = table_floats(n, m), np = conv_param_floats(g.N, g.C);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot + np; e += (int64_t)gridDim.x * blockDim.x) {
+    if (e >= tot) {
+      out[e] = params[e - tot];
+    } else if (e < nm) {
+      const int k = (int)(e / mp), i = (int)(e % mp);
+      const float w = i < m ? params[(int64_t)(i / n) * n + conv_tap(g, k, i % n)] : 0.0f;
+      out[e] = w;
+      out[nm + e] = coshf(2.0f * w);
+      out[2 * nm + e] = sinhf(2.0f * w);
+    } else if (e >= 3 * nm) {
+      const int64_t r = e - 3 * nm;  // b (mp), then the visible bias (zero)
+      out[e] = (r < m) ? params[(int64_t)g.C * n + r / n] : 0.0f;
+    }
+  }
+}
+
+// O[s][c N + d] = sum_x t_{c,x} s_{site(x, d)}, O[s][C N + c] = sum_x t_{c,x}, t = tanh theta:
+// the log-derivatives of the shared weights and biases (variational.py:424-511). One CTA per
+// sample; theta is summed over k in the dense forward's order.
+__global__ void __launch_bounds__(256) conv_jacobian_kernel(const float* __restrict__ cparams, ConvGeom g,
+                                                            const uint32_t* __restrict__ spins, int64_t ns,
+                                                            float* __restrict__ O, int64_t ldo) {
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int N = g.N, CN = g.C * g.N, nw = (N + 31) / 32;
+  float* s = sm;          // N
+  float* W = s + N;       // C N
+  float* t = W + CN;      // C N
+  for (int e = threadIdx.x; e < CN; e += blockDim.x) W[e] = cparams[e];
+  const float* b = cparams + CN;
+  for (int64_t smp = blockIdx.x; smp < ns; smp += gridDim.x) {
+    __syncthreads();
+    const uint32_t* sp = spins + smp * nw;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) s[k] = spin_at(sp, k);
+    __syncthreads();
+    for (int i = threadIdx.x; i < CN; i += blockDim.x) {
+      const int c = i / N, x = i % N;
+      float th = b[c];
+      for (int k = 0; k < N; ++k) th = fmaf(s[k], W[c * N + conv_tap(g, k, x)], th);
+      t[i] = tanhf(th);
+    }
+    __syncthreads();
+    float* row = O + smp * ldo;
+    for (int i = threadIdx.x; i < CN + g.C; i += blockDim.x) {
+      float acc = 0.0f;
+      if (i < CN) {
+        const int c = i / N, d = i % N;
+        for (int x = 0; x < N; ++x) acc = fmaf(t[c * N + x], s[conv_site(g, x, d)], acc);
+      } else {
+        const int c = i - CN;
+        for (int x = 0; x < N; ++x) acc += t[c * N + x];
+      }
+      row[i] = acc;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // launch helpers
 template <int JT>
 constexpr int threads_for() {
@@ -694,6 +783,7 @@ int launch_jacobian(const float* table, int n, int m, int mp, int has_vbias, con
     case 3: return CALL(3);                \
     case 4: return CALL(4);                \
     case 8: return CALL(8);                \
+    case 16: return CALL(16);              \
     default: return QGX_ERR_UNSUPPORTED;   \
   }
 
@@ -701,7 +791,7 @@ constexpr int kMaxSites = 1024;  // 32 packed words per configuration
 
 inline bool mp_supported(int mp) {
   const int jt = mp / 128;
-  return jt == 1 || jt == 2 || jt == 3 || jt == 4 || jt == 8;
+  return jt == 1 || jt == 2 || jt == 3 || jt == 4 || jt == 8 || jt == 16;
 }
 
 }  // namespace
@@ -725,6 +815,47 @@ int qgx_rbm_prepare(const float* W, const float* b, const float* a, int32_t n, i
   const int64_t tot = table_floats(n, m);
   const unsigned g = (unsigned)std::min<int64_t>((tot + 255) / 256, 4096);
   prepare_kernel<<<g, 256, 0, as_cuda(stream)>>>(W, b, a, n, m, mp, table);
+  return launch_status();
+}
+
+static bool conv_geom(int32_t L0, int32_t L1, int32_t channels, ConvGeom* g) {
+  if (L0 < 1 || L1 < 1 || channels < 1) return false;
+  const int64_t N = (int64_t)L0 * L1;
+  if (N > kMaxSites || channels * N > 2048) return false;
+  *g = ConvGeom{L0, L1, (L0 - 1) / 2, (L1 - 1) / 2, (int)N, channels};
+  return true;
+}
+
+int64_t qgx_rbm_conv_table_floats(int32_t L0, int32_t L1, int32_t channels) {
+  ConvGeom g;
+  if (!conv_geom(L0, L1, channels, &g)) return 0;
+  return table_floats(g.N, g.C * g.N) + (conv_param_floats(g.N, g.C) + 3) / 4 * 4;
+}
+
+int qgx_rbm_conv_prepare(const float* params, int32_t L0, int32_t L1, int32_t channels, float* table,
+                         qgx_stream_t stream) {
+  ConvGeom g;
+  QGX_CHECK_ARG(conv_geom(L0, L1, channels, &g) && params && table);
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(table) & 15) == 0);
+  const int mp = padded_m(g.C * g.N);
+  const int64_t tot = table_floats(g.N, g.C * g.N) + conv_param_floats(g.N, g.C);
+  const unsigned blocks = (unsigned)std::min<int64_t>((tot + 255) / 256, 4096);
+  conv_prepare_kernel<<<blocks, 256, 0, as_cuda(stream)>>>(params, g, mp, table);
+  return launch_status();
+}
+
+int qgx_rbm_conv_jacobian(const float* table, int32_t L0, int32_t L1, int32_t channels, const uint32_t* spins,
+                          int64_t ns, float* O, int64_t ldo, qgx_stream_t stream) {
+  ConvGeom g;
+  QGX_CHECK_ARG(conv_geom(L0, L1, channels, &g) && ns >= 0 && ldo >= conv_param_floats(g.N, g.C));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && O);
+  const float* cparams = table + table_floats(g.N, g.C * g.N);
+  const size_t smem = (size_t)(g.N + 2 * g.C * g.N) * sizeof(float);
+  if (smem > 48 * 1024)
+    QGX_CHECK_CUDA(cudaFuncSetAttribute(conv_jacobian_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned grid = (unsigned)std::min<int64_t>(ns, (int64_t)device_sm_count() * 8);
+  conv_jacobian_kernel<<<grid, 256, smem, as_cuda(stream)>>>(cparams, g, spins, ns, O, ldo);
   return launch_status();
 }
 
@@ -815,6 +946,7 @@ int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias, co
     case 3: rc = CALL(3); break;
     case 4: rc = CALL(4); break;
     case 8: rc = CALL(8); break;
+    case 16: rc = CALL(16); break;
     default: return QGX_ERR_UNSUPPORTED;
   }
 #undef CALL

@@ -130,6 +130,69 @@ class RBM_Dense:
                   workspace.numel(), _lib.stream_ptr())
 
 
+class RBM_Conv(RBM_Dense):
+    """Restricted Boltzmann machine with one convolutional layer (quantax/model/shallow_nets.py:
+    129-190): psi = prod cosh(Conv(s)), a circular convolution whose kernel covers the whole
+    (periodic) lattice. Parameters in the reference's ravel order: the kernel (channels x
+    lattice shape, row-major), then the biases. The device evaluates it as the dense RBM with
+    channels x Nsites hidden units that the kernel's translated copies make."""
+
+    conv = True
+
+    def __init__(self, channels: int, use_bias: bool = True, dtype=np.float32, init_std: Optional[float] = None,
+                 seed: Optional[int] = None):
+        from .global_defs import get_lattice
+        if np.dtype(dtype) != np.float32:
+            raise NotImplementedError("RBM_Conv runs with float32 parameters")
+        lat = get_lattice()
+        if lat.ndim > 2 or lat.shape[0] != 1:
+            raise NotImplementedError("RBM_Conv: 1D and 2D lattices with one site per cell")
+        dims = tuple(lat.shape[1:]) + ((1,) if lat.ndim == 1 else ())
+        self.L0, self.L1 = int(dims[0]), int(dims[1])
+        self.channels = int(channels)
+        self.N = self.L0 * self.L1
+        self.M = self.channels * self.N  # hidden units of the equivalent dense RBM
+        if self.M > 2048:
+            raise NotImplementedError("RBM_Conv: channels x Nsites <= 2048")
+        self.use_bias = use_bias
+        self.visible_bias = False
+        rng = np.random.default_rng(get_subkeys() if seed is None else seed)
+        shape = (self.channels, self.N)
+        if init_std is not None:
+            W = rng.normal(0.0, init_std, shape)
+            b = rng.normal(0.0, init_std, self.channels) if use_bias else np.zeros(self.channels)
+        else:
+            # lecun normal (fan-in = the kernel's size), then the cosh output scale of
+            # shallow_nets.py:17-32 over channels x cells features (:174-176); zero biases
+            W = _truncated_normal(rng, shape, 1.0 / np.sqrt(self.N)) * _cosh_scale(self.M, self.N, rng)
+            b = np.zeros(self.channels)
+        self.init_params = np.concatenate([W.ravel(), b]).astype(np.float32)
+
+    @property
+    def nparams(self) -> int:
+        return self.channels * self.N + self.channels
+
+    def table_floats(self) -> int:
+        return int(_lib.lib().qgx_rbm_conv_table_floats(self.L0, self.L1, self.channels))
+
+    def prepare(self, params: torch.Tensor, table: torch.Tensor) -> None:
+        _lib.call("qgx_rbm_conv_prepare", _lib.ptr(params), self.L0, self.L1, self.channels, _lib.ptr(table),
+                  _lib.stream_ptr())
+
+    def jacobian(self, table, packed, out):
+        _lib.call("qgx_rbm_conv_jacobian", _lib.ptr(table), self.L0, self.L1, self.channels, _lib.ptr(packed),
+                  packed.shape[0], _lib.ptr(out), out.stride(0), _lib.stream_ptr())
+
+    def obar_workspace_bytes(self, ns: int) -> int:
+        return int(_lib.lib().qgx_center_columns_workspace_bytes(ns, self.nparams))
+
+    def obar(self, table, packed, r, out, omean, workspace):
+        """Obar = (O - <O>) sqrt(r / Ns): the log-derivatives, then the column centring."""
+        self.jacobian(table, packed, out)
+        _lib.call("qgx_center_columns", _lib.ptr(out), packed.shape[0], self.nparams, out.stride(0), _lib.ptr(r),
+                  _lib.ptr(omean), _lib.ptr(workspace), workspace.numel(), _lib.stream_ptr())
+
+
 class ResConv:
     """Deep convolutional residual network (conv_nets.py:95-183) on a periodic L x L lattice."""
 

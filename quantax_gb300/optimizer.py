@@ -19,7 +19,8 @@ def _round8(n: int) -> int:
     return (n + 7) // 8 * 8
 
 
-_GRAM_MODES = {"fp32": _lib.GRAM_FP32, "tf32": _lib.GRAM_TF32, "bf16": _lib.GRAM_BF16, "3xtf32": _lib.GRAM_3XTF32}
+_GRAM_MODES = {"fp32": _lib.GRAM_FP32, "tf32": _lib.GRAM_TF32, "bf16": _lib.GRAM_BF16, "3xtf32": _lib.GRAM_3XTF32,
+               "fp64": _lib.GRAM_FP64}
 
 
 @dataclass(frozen=True)

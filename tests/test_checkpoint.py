@@ -126,3 +126,22 @@ def test_optimizer_leaf_records():
     assert (mu.item(), beta.item(), t.item()) == (0.95, 0.995, 7)
     assert mu.dtype == np.float64 and t.dtype.kind == "i"
     np.testing.assert_array_equal(m, np.arange(5.0))
+
+
+def test_rbm_conv_record_sequence():
+    """RBM_Conv on a 10 x 10 lattice: Conv.weight (C, 1, 10, 10), Conv.bias (C, 1, 1), holomorphic;
+    on a chain Conv.bias is (C, 1)."""
+    import quantax_gb300 as qtx
+    qtx.set_default_dtype(np.float64)
+    qtx.sites.Square(10)
+    model = qtx.model.RBM_Conv(16, seed=1)
+    buf = io.BytesIO()
+    ck.save_model(buf, model, model.init_params)
+    assert [r.shape for r in _records(buf)] == [(16, 1, 10, 10), (16, 1, 1), ()]
+    buf.seek(0)
+    np.testing.assert_array_equal(ck.load_model(buf, model), model.init_params)
+    qtx.sites.Chain(12)
+    chain = qtx.model.RBM_Conv(2, seed=1)
+    buf = io.BytesIO()
+    ck.save_model(buf, chain, chain.init_params)
+    assert [r.shape for r in _records(buf)] == [(2, 1, 12), (2, 1), ()]

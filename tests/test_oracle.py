@@ -160,3 +160,34 @@ def test_time_evol_oracle_equals_real_time_lstsq():
     y = sr.solve(Ob, eb, lambda A, b: sr.lstsq_pinv(A, b, rtol=1e-9), complex_out=True, imag_time=False)
     np.testing.assert_allclose(x, y, rtol=1e-10, atol=1e-12)
     assert not np.allclose(x, 0)
+
+
+def test_rbm_conv_is_the_translated_dense_rbm():
+    """The roll-based RBM_Conv equals the dense RBM whose unit (c, x) has the weights
+    W_c[(k - x + lo) mod L] (2D 6x4 and a chain of 10), and its log-derivatives match finite
+    differences."""
+    rng = np.random.default_rng(3)
+    for L0, L1 in ((6, 4), (10, 1)):
+        C, N = 3, L0 * L1
+        W = rng.normal(size=(C, L0, L1)) * 0.3
+        b = rng.normal(size=C) * 0.1
+        conv = rbm.RBMConv(W, b)
+        lo0, lo1 = (L0 - 1) // 2, (L1 - 1) // 2
+        Wd = np.zeros((C * N, N))
+        for c in range(C):
+            for x in range(N):
+                for k in range(N):
+                    d0 = (k // L1 - x // L1 + lo0) % L0
+                    d1 = (k % L1 - x % L1 + lo1) % L1
+                    Wd[c * N + x, k] = W[c, d0, d1]
+        dense = rbm.RBM(Wd, np.repeat(b, N))
+        s = rng.choice([-1.0, 1.0], size=(5, N))
+        np.testing.assert_allclose(conv.log_psi(s), dense.log_psi(s), rtol=1e-12)
+        J = conv.jacobian(s)
+        p = conv.params()
+        for k in (0, 7, p.size - 1):
+            e = np.zeros_like(p)
+            e[k] = 1e-6
+            up = rbm.RBMConv((p + e)[:C * N].reshape(C, L0, L1), (p + e)[C * N:])
+            dn = rbm.RBMConv((p - e)[:C * N].reshape(C, L0, L1), (p - e)[C * N:])
+            np.testing.assert_allclose((up.log_psi(s) - dn.log_psi(s)) / 2e-6, J[:, k], rtol=1e-6, atol=1e-8)

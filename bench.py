@@ -461,6 +461,53 @@ def run_tutorial(args, rank):
         print(json.dumps(line), flush=True)
 
 
+# examples/RBM.ipynb: 10 x 10 Heisenberg (MSR), QMC energy and the reference's relative error of
+# the mean of its last 100 SR steps (cells 3-5)
+RBM_EXAMPLE_E_QMC = -268.62107
+RBM_EXAMPLE_REFERENCE_REL_ERR = 0.0009721019350138251
+
+
+def run_rbm_example(args, rank):
+    """The reference's examples/RBM.ipynb: RBM_Conv(16) on the 10 x 10 Heisenberg model (MSR),
+    8192 SpinExchange samples, SR with lstsq_pinv_eig(rtol=1e-9) (FP64 Gram, the cut-off lies
+    below FP32 resolution), lr 2e-3; the energy is the mean of the last 100 steps' MC energies,
+    against the QMC value. Times are CUDA events around the training loop."""
+    import numpy as np
+    import torch
+    import quantax_gb300 as qtx
+    qtx.set_random_seed(args.seed)
+    qtx.set_default_dtype(np.float64)
+    qtx.sites.Square(10, Nparticles=(50, 50))
+    H = qtx.operator.Heisenberg(msr=True)
+    state = qtx.state.Variational(qtx.model.RBM_Conv(16))
+    sampler = qtx.sampler.SpinExchange(state, 8192)
+    opt = qtx.optimizer.SR(state, H, solver=qtx.optimizer.lstsq_pinv_eig(rtol=1e-9), gram="fp64")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    stats = []
+    for _ in range(args.example_steps):
+        samples = sampler.sweep()
+        step = opt.get_step(samples)
+        state.update(step * 2e-3)
+        stats.append(opt.stats.clone())
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0
+    energies = np.array([float(x[0]) for x in stats])
+    tail = energies[-min(100, len(energies)):]
+    E = float(tail.mean())
+    line = {"metric": "relative energy error vs QMC", "workload": "heisenberg_square10_rbm_conv16_example",
+            "seed": args.seed, "steps": args.example_steps, "steps_per_s": args.example_steps / t,
+            "ms_per_step": 1000.0 * t / args.example_steps, "energy_last100_mean": E,
+            "rel_err": (E - RBM_EXAMPLE_E_QMC) / abs(RBM_EXAMPLE_E_QMC), "e_qmc": RBM_EXAMPLE_E_QMC,
+            "reference_rel_err": RBM_EXAMPLE_REFERENCE_REL_ERR,
+            "energy_every_100": [float(energies[i]) for i in range(0, len(energies), 100)],
+            "solve_fallbacks": opt.solve_fallbacks}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def percentile(lat, q):
     s = sorted(lat)
     return s[min(len(s) - 1, int(round(q * (len(s) - 1))))]
@@ -479,9 +526,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
     ap.add_argument("--tutorial-steps", type=int, default=200, help="*_tutorial: SR steps per phase")
-    ap.add_argument("--seed", type=int, default=0, help="*_tutorial: random seed")
+    ap.add_argument("--seed", type=int, default=0, help="*_tutorial, rbm_example: random seed")
+    ap.add_argument("--example-steps", type=int, default=1000, help="rbm_example: SR steps")
     ap.add_argument("--workload", default="rbm",
-                    choices=["rbm", "resconv", "serving", "trajectory", "heisenberg_tutorial", "j1j2_tutorial"],
+                    choices=["rbm", "resconv", "serving", "trajectory", "heisenberg_tutorial", "j1j2_tutorial",
+                             "rbm_example"],
                     help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv); "
                          "serving: a Poisson stream of config-5 jobs through quantax_gb300.serving")
     ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
@@ -516,6 +565,9 @@ def main():
         return
     if args.workload in TUTORIALS:
         run_tutorial(args, rank)
+        return
+    if args.workload == "rbm_example":
+        run_rbm_example(args, rank)
         return
 
     plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)

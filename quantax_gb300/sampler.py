@@ -127,19 +127,32 @@ class Metropolis:
         if self._thermal_steps > 0:
             self.sweep(self._thermal_steps)
 
+    def _device_sweep(self, nsteps: int, step0: int, proposal, nbr, z: int, hop: int) -> None:
+        """nsteps proposals of one kind for every chain, Philox steps step0 .. step0 + nsteps - 1."""
+        st = self._state
+        if self._resconv:
+            ws = st.workspace("sweep", st.model.sweep_workspace_bytes(self._nsamples, st.symm_dev))
+            st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, nsteps, self._seed, step0,
+                           self._reweight, proposal, nbr, z, hop, ws, st.symm_dev)
+        else:
+            st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, nsteps, self._seed, step0,
+                           self._reweight, proposal, nbr, z, hop)
+
+    def _run_proposals(self, n: int) -> None:
+        self._device_sweep(n, self._step, self.proposal, self._nbr, self._z, self._hop)
+
     def sweep(self, nsweeps: Optional[int] = None) -> Samples:
         """nsweeps proposals per chain (metropolis.py:171-215); default sweep_steps."""
         n = self._sweep_steps if nsweeps is None else int(nsweeps)
         st = self._state
+        self._run_proposals(n)
         if self._resconv:
-            ws = st.workspace("sweep", st.model.sweep_workspace_bytes(self._nsamples, st.symm_dev))
-            st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, n, self._seed, self._step,
-                           self._reweight, self.proposal, self._nbr, self._z, self._hop, ws, st.symm_dev)
             lp_real = self._log_psi[:, 0].contiguous()
-            lp = torch.view_as_complex(self._log_psi.clone()) if st.is_complex else lp_real
+            # complex output, or a real state that can be negative (symmetry projection,
+            # sinhp1): the phase carries the sign
+            signed = st.symm_dev is not None or getattr(st.model, "signed_output", False)
+            lp = torch.view_as_complex(self._log_psi.clone()) if st.is_complex or signed else lp_real
         else:
-            st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, n, self._seed, self._step,
-                           self._reweight, self.proposal, self._nbr, self._z, self._hop)
             lp_real = self._log_psi
             lp = self._log_psi.clone()
         self._step += n
@@ -190,3 +203,64 @@ class SpinExchange(Metropolis):
 
 
 NeighborExchange = SpinExchange
+
+
+class MixSampler(Metropolis):
+    """A mixture of Metropolis samplers (metropolis.py:325-428): every proposal step draws one
+    component with probability proportional to its nsamples, and all chains propose with that
+    component's move. The chains start from the components' chains, concatenated.
+
+    Components are the built-in samplers (LocalFlip, SpinExchange with any n_neighbor); their
+    moves run inside the device sweep kernels, so a Python-level propose() cannot take part.
+    The component index of each step comes from a host generator seeded by (seed, step); a run
+    of equal indices is one kernel sweep."""
+
+    def __init__(self, samplers: Sequence[Metropolis], reweight: float = 2.0, thermal_steps: Optional[int] = None,
+                 sweep_steps: Optional[int] = None, initial_spins=None):
+        samplers = tuple(samplers)
+        state = samplers[0].state
+        for smp in samplers[1:]:
+            if smp.state is not state:
+                raise ValueError("The states of component samplers should be the same in `MixSampler`.")
+        for smp in samplers:
+            if type(smp).proposal is None:
+                raise NotImplementedError(f"{type(smp).__name__}: only built-in proposals run in the device sweep")
+            if state.model.kind == "resconv" and smp.proposal != _lib.PROPOSAL_SPIN_EXCHANGE:
+                raise NotImplementedError("the ResConv sweep implements SpinExchange proposals")
+        self._samplers = samplers
+        counts = np.array([smp.nsamples for smp in samplers], dtype=np.float64)
+        self._ratio = counts / counts.sum()
+        super().__init__(state, int(counts.sum()), reweight, thermal_steps, sweep_steps, initial_spins)
+
+    @property
+    def samplers(self):
+        return self._samplers
+
+    @property
+    def nflips(self) -> Optional[int]:
+        nf = [smp.nflips for smp in self._samplers]
+        return None if None in nf else max(nf)
+
+    def _initial(self) -> torch.Tensor:
+        if self._initial_spins is not None:
+            return super()._initial()
+        return torch.cat([smp._packed for smp in self._samplers], dim=0)
+
+    def component_sequence(self, n: int, step0: int) -> np.ndarray:
+        """The component drawn at each of the steps step0 .. step0 + n - 1."""
+        rng = np.random.default_rng([int(self._seed), int(step0)])
+        return rng.choice(len(self._samplers), size=n, p=self._ratio)
+
+    def _run_proposals(self, n: int) -> None:
+        idx = self.component_sequence(n, self._step)
+        total = torch.zeros_like(self._accepts)  # each kernel sweep restarts the per-chain counts
+        i = 0
+        while i < n:
+            j = i
+            while j < n and idx[j] == idx[i]:
+                j += 1
+            c = self._samplers[idx[i]]
+            self._device_sweep(j - i, self._step + i, c.proposal, c._nbr, c._z, c._hop)
+            total += self._accepts
+            i = j
+        self._accepts.copy_(total)

@@ -148,12 +148,18 @@ def test_sweep_in_two_launches_equals_one(cuda):
     assert torch.equal(p1, p2)
 
 
-def test_spin_exchange_sweep_bit_exact(cuda):
+@pytest.mark.parametrize("shells", [1, [1, 2]])
+def test_spin_exchange_sweep_bit_exact(cuda, shells):
+    """SpinExchange with nearest neighbours, and with the first two shells
+    (SpinExchange(state, n, n_neighbor=[1, 2]) of tutorials/neural_jastrow.ipynb): the
+    neighbour rows are padded to the longest, the draws are the same."""
     L = 4
     N = L * L
     W, b, a = rbm.init_normal(N, 32, 0.2, seed=4, visible_bias=True)
     net = rbm.RBM(W, b, a)
-    nbr = lattice.neighbor_table((L, L), 1)
+    nbr = lattice.neighbor_table((L, L), shells)
+    if shells != 1:
+        assert nbr.shape[1] == 8
     s0 = metropolis.init_fixed_up(64, N, N // 2, 3)
     want, want_lp, stats = metropolis.sweep(net.log_psi, s0, 80, 99, 0, proposal="exchange", nbr_table=nbr, hop=1)
     assert stats["min_margin"] > 1e-5

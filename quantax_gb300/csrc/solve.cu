@@ -67,40 +67,66 @@ __global__ void shift_diag_kernel(double* __restrict__ T, int64_t n, int64_t ldt
   }
 }
 
-// partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s] in FP64 (the reference forms
-// x = A^T y in float64, solver.py:58-61, 144-146); four columns per thread, 16-byte loads
+// partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s] to about 48 bits (the reference
+// forms x = A^T y in float64, solver.py:58-61, 144-146). FP64 arithmetic runs at a small
+// fraction of the FP32 rate on this GPU, so the sum is kept as an unevaluated pair of floats:
+// y = yh + yl (two floats), a*yh exactly as p + e (TwoProd by FMA), a*yl added to e, and
+// (sh, sl) += (p, e) by TwoSum. Four columns per thread, 16-byte loads; the chunk's y split
+// once into shared memory.
+struct DSum {
+  float h = 0.0f, l = 0.0f;
+  // the _rn intrinsics are never contracted into FMAs, which would void the error terms
+  __device__ inline void add_prod(float a, float yh, float yl) {
+    const float p = __fmul_rn(a, yh);
+    float e = fmaf(a, yh, -p);
+    e = fmaf(a, yl, e);
+    const float t = __fadd_rn(h, p);
+    const float z = __fsub_rn(t, h);
+    l = __fadd_rn(l, __fadd_rn(__fadd_rn(__fsub_rn(h, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+    h = t;
+  }
+  __device__ inline double value() const { return (double)h + (double)l; }
+};
+
 __global__ void project_partial_kernel(const float* __restrict__ A, int64_t nrow, int64_t ncol, int64_t lda,
                                        const double* __restrict__ y, double* __restrict__ part, bool vec4) {
-  const int64_t c0 = 4 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  __shared__ float2 ys[kProjRows];
   const int64_t r0 = (int64_t)blockIdx.y * kProjRows;
   const int64_t r1 = min(nrow, r0 + kProjRows);
+  for (int64_t s = r0 + threadIdx.x; s < r1; s += blockDim.x) {
+    const double v = y[s];
+    const float hi = (float)v;
+    ys[s - r0] = make_float2(hi, (float)(v - (double)hi));
+  }
+  __syncthreads();
+  const int64_t c0 = 4 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
   if (c0 >= ncol) return;
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  DSum a0, a1, a2, a3;
   if (vec4 && c0 + 3 < ncol) {
 #pragma unroll 4
     for (int64_t s = r0; s < r1; ++s) {
-      const double ys = y[s];
+      const float2 yv = ys[s - r0];
       const float4 v = __ldg(reinterpret_cast<const float4*>(A + s * lda + c0));
-      a0 = fma((double)v.x, ys, a0);
-      a1 = fma((double)v.y, ys, a1);
-      a2 = fma((double)v.z, ys, a2);
-      a3 = fma((double)v.w, ys, a3);
+      a0.add_prod(v.x, yv.x, yv.y);
+      a1.add_prod(v.y, yv.x, yv.y);
+      a2.add_prod(v.z, yv.x, yv.y);
+      a3.add_prod(v.w, yv.x, yv.y);
     }
   } else {
     for (int64_t s = r0; s < r1; ++s) {
-      const double ys = y[s];
+      const float2 yv = ys[s - r0];
       const float* row = A + s * lda;
-      a0 = fma((double)__ldg(row + c0), ys, a0);
-      if (c0 + 1 < ncol) a1 = fma((double)__ldg(row + c0 + 1), ys, a1);
-      if (c0 + 2 < ncol) a2 = fma((double)__ldg(row + c0 + 2), ys, a2);
-      if (c0 + 3 < ncol) a3 = fma((double)__ldg(row + c0 + 3), ys, a3);
+      a0.add_prod(__ldg(row + c0), yv.x, yv.y);
+      if (c0 + 1 < ncol) a1.add_prod(__ldg(row + c0 + 1), yv.x, yv.y);
+      if (c0 + 2 < ncol) a2.add_prod(__ldg(row + c0 + 2), yv.x, yv.y);
+      if (c0 + 3 < ncol) a3.add_prod(__ldg(row + c0 + 3), yv.x, yv.y);
     }
   }
   double* p = part + blockIdx.y * ncol + c0;
-  p[0] = a0;
-  if (c0 + 1 < ncol) p[1] = a1;
-  if (c0 + 2 < ncol) p[2] = a2;
-  if (c0 + 3 < ncol) p[3] = a3;
+  p[0] = a0.value();
+  if (c0 + 1 < ncol) p[1] = a1.value();
+  if (c0 + 2 < ncol) p[2] = a2.value();
+  if (c0 + 3 < ncol) p[3] = a3.value();
 }
 
 __global__ void sum_partials_kernel(const double* __restrict__ part, int64_t nchunk, int64_t ncol,

@@ -2,13 +2,15 @@
 // SR solve: v <- L^-1 v, then v <- L^-T v, for L lower triangular, n x n, column-major (as
 // cuSOLVER's Xpotrf leaves it; the other triangle is not read).
 //
-// Decoupled block substitution: 64-row blocks; a CTA takes block b in ticket order (an
+// Decoupled block substitution: 128-row blocks; a CTA takes block b in ticket order (an
 // atomic counter, so block b's CTA started after the CTAs of every block it waits on) and
 // folds in each earlier block k's contribution L_bk y_k as soon as block k's flag is
 // published, then applies the precomputed inverse of its diagonal block and publishes y_b.
-// The backward pass runs the blocks in reverse order with L^T. Every wait on a flag is bounded
-// (2 s of the global timer); a wait that runs out sets the error word and the CTA goes on
-// with what it has, so the caller sees a wrong residual and falls back.
+// The backward pass runs the blocks in reverse order with L^T. The chain of publications is
+// the critical path, so the L tile of block k is loaded before its flag is awaited (it does
+// not depend on the flag) and only the 128 published values are read after it. Every wait on
+// a flag is bounded (2 s of the global timer); a wait that runs out sets the error word and
+// the CTA goes on with what it has, so the caller sees a wrong residual and falls back.
 #include <algorithm>
 
 #include "qgx_common.cuh"
@@ -22,12 +24,14 @@ int trsv_chol_error(int64_t n, void* work, int* host_err, cudaStream_t st);
 
 namespace {
 
-constexpr int kNB = 64;            // rows per block
-constexpr int kTrsvThreads = 256;  // 4 column groups x 64 rows
+constexpr int kNB = 128;                 // rows per block
+constexpr int kGroups = 4;               // column groups of the off-diagonal products
+constexpr int kTrsvThreads = kNB * kGroups;  // 512
+constexpr int kDPitch = kNB + 1;         // padded row of a diagonal block's inverse in shared memory
 constexpr unsigned long long kFlagWaitNs = 2000000000ull;
 
 struct TrsvWork {
-  float* dinv;   // nblk x 64 x 64: inverses of the diagonal blocks, row-major per block
+  float* dinv;   // nblk x 128 x 128: inverses of the diagonal blocks, row-major per block
   int* flags;    // 2 x nblk: forward / backward publication epochs
   int* tickets;  // 2
   int* err;      // 1
@@ -35,6 +39,7 @@ struct TrsvWork {
 
 inline int64_t nblocks(int64_t n) { return (n + kNB - 1) / kNB; }
 inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
+inline size_t trsv_smem_bytes() { return (size_t)kNB * kDPitch * 4 + (size_t)(kGroups + 1) * kNB * 4; }
 
 TrsvWork layout(int64_t n, void* base) {
   char* b = static_cast<char*>(base);
@@ -78,10 +83,18 @@ __device__ inline bool wait_flag(const int* flag, int epoch, int* err) {
   return true;
 }
 
+// every warp's lane 0 waits, then the warp proceeds
+__device__ inline void warp_wait_flag(const int* flag, int epoch, int* err) {
+  if ((threadIdx.x & 31) == 0) wait_flag(flag, epoch, err);
+  __syncwarp();
+}
+
 // inverse of every diagonal block (one CTA per block): thread c solves L_bb x = e_c by forward
-// substitution; dinv[b][i][c] = x_i (rows past n: identity)
-__global__ void dinv_kernel(const float* __restrict__ L, int64_t n, float* __restrict__ dinv) {
-  __shared__ float D[kNB][kNB + 1];
+// substitution in shared memory; dinv[b][i][c] = x_i (rows past n: identity)
+__global__ void __launch_bounds__(kNB) dinv_kernel(const float* __restrict__ L, int64_t n, float* __restrict__ dinv) {
+  extern __shared__ float smem[];
+  float* D = smem;                // [kNB][kDPitch]
+  float* X = D + kNB * kDPitch;   // [kNB][kNB + 1]: column c of the inverse in column c
   const int64_t b = blockIdx.x, r0 = b * kNB;
   const int nb = (int)std::min<int64_t>(kNB, n - r0);
   for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) {
@@ -89,115 +102,146 @@ __global__ void dinv_kernel(const float* __restrict__ L, int64_t n, float* __res
     float v = 0.0f;
     if (i < nb && j < nb && j <= i) v = L[(r0 + j) * n + (r0 + i)];
     if (i >= nb && i == j) v = 1.0f;
-    D[i][j] = v;
+    D[i * kDPitch + j] = v;
   }
   __syncthreads();
   const int c = threadIdx.x;
-  if (c < kNB) {
-    float x[kNB];
-#pragma unroll
-    for (int i = 0; i < kNB; ++i) {
-      float s = (i == c) ? 1.0f : 0.0f;
-      for (int j = 0; j < i; ++j) s = fmaf(-D[i][j], x[j], s);
-      x[i] = s / D[i][i];
-    }
-    float* out = dinv + b * kNB * kNB;
-#pragma unroll
-    for (int i = 0; i < kNB; ++i) out[i * kNB + c] = x[i];
+  for (int i = 0; i < kNB; ++i) {
+    float s = (i == c) ? 1.0f : 0.0f;
+    for (int j = c; j < i; ++j) s = fmaf(-D[i * kDPitch + j], X[j * (kNB + 1) + c], s);  // x_j = 0 for j < c
+    X[i * (kNB + 1) + c] = i < c ? 0.0f : s / D[i * kDPitch + i];
   }
+  __syncthreads();
+  float* out = dinv + b * kNB * kNB;
+  for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) out[e] = X[(e / kNB) * (kNB + 1) + (e % kNB)];
 }
 
 // forward: v_b <- L_bb^-1 (v_b - sum_{k<b} L_bk v_k)
+// thread (g, i): row r0 + i, columns c0 + g + 4 jj of every earlier block
 __global__ void __launch_bounds__(kTrsvThreads) trsv_lower_kernel(const float* __restrict__ L, int64_t n,
                                                                   float* __restrict__ v,
                                                                   const float* __restrict__ dinv, int* flags,
                                                                   int* ticket, int epoch, int* err) {
+  extern __shared__ float smem[];
+  float* D = smem;                  // the diagonal block's inverse [kNB][kDPitch]
+  float* part = D + kNB * kDPitch;  // [kGroups][kNB]
+  float* acc = part + kGroups * kNB;
   __shared__ int sb;
-  __shared__ float part[4][kNB];
-  __shared__ float acc[kNB];
-  __shared__ float D[kNB][kNB + 1];  // the diagonal block's inverse, padded against bank conflicts
   if (threadIdx.x == 0) sb = atomicAdd(ticket, 1);
   __syncthreads();
   const int64_t b = sb, r0 = b * kNB;
   const int nb = (int)std::min<int64_t>(kNB, n - r0);
-  const int t = threadIdx.x, i = t & (kNB - 1), g = t >> 6, lane = t & 31;
-  for (int e = t; e < kNB * kNB; e += blockDim.x) D[e / kNB][e % kNB] = dinv[b * kNB * kNB + e];
+  const int t = threadIdx.x, i = t & (kNB - 1), g = t >> 7;
+  for (int e = t; e < kNB * kNB; e += blockDim.x) D[(e / kNB) * kDPitch + e % kNB] = dinv[b * kNB * kNB + e];
   float a = 0.0f;
+  constexpr int kPer = kNB / kGroups;  // 32 columns of each earlier block per thread
   for (int64_t k = 0; k < b; ++k) {
-    if (lane == 0) wait_flag(flags + k, epoch, err);
-    __syncwarp();
     const int64_t c0 = k * kNB;
+    float lv[kPer];
     if (i < nb) {
-      const float* col = L + c0 * n + r0 + i;
-#pragma unroll 4
-      for (int j = g; j < kNB; j += 4) a = fmaf(col[(int64_t)j * n], __ldcg(v + c0 + j), a);
+      const float* col = L + (c0 + g) * n + r0 + i;
+#pragma unroll
+      for (int jj = 0; jj < kPer; ++jj) lv[jj] = col[(int64_t)(kGroups * jj) * n];
+    }
+    warp_wait_flag(flags + k, epoch, err);
+    if (i < nb) {
+#pragma unroll
+      for (int jj = 0; jj < kPer; ++jj) a = fmaf(lv[jj], __ldcg(v + c0 + g + kGroups * jj), a);
     }
   }
-  part[g][i] = a;
+  part[g * kNB + i] = a;
   __syncthreads();
-  if (t < kNB) acc[t] = (t < nb ? __ldcg(v + r0 + t) : 0.0f) - (part[0][t] + part[1][t] + part[2][t] + part[3][t]);
-  __syncthreads();
-  if (t < nb) {
-    float y = 0.0f;
-    for (int j = 0; j <= t; ++j) y = fmaf(D[t][j], acc[j], y);
-    __stcg(v + r0 + t, y);
+  if (t < kNB) {
+    float s = t < nb ? __ldcg(v + r0 + t) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < kGroups; ++q) s -= part[q * kNB + t];
+    acc[t] = s;
   }
+  __syncthreads();
+  // y_i = sum_{j <= i} D[i][j] acc_j, the j range split over the four groups
+  {
+    float y = 0.0f;
+    const int j0 = g * kPer;
+#pragma unroll 8
+    for (int j = j0; j < j0 + kPer; ++j)
+      if (j <= i) y = fmaf(D[i * kDPitch + j], acc[j], y);
+    part[g * kNB + i] = y;
+  }
+  __syncthreads();
+  if (t < nb) __stcg(v + r0 + t, part[t] + part[kNB + t] + part[2 * kNB + t] + part[3 * kNB + t]);
   __threadfence();
   __syncthreads();
   if (t == 0) st_release(flags + b, epoch);
 }
 
 // backward: v_b <- L_bb^-T (v_b - sum_{k>b} L_kb^T v_k), blocks in reverse ticket order
+// warp w owns columns i = w + 16 q of block b; lane l covers rows j0 + l + 32 r of block k
 __global__ void __launch_bounds__(kTrsvThreads) trsv_upper_kernel(const float* __restrict__ L, int64_t n,
                                                                   float* __restrict__ v,
                                                                   const float* __restrict__ dinv, int* flags,
                                                                   int* ticket, int epoch, int* err) {
+  extern __shared__ float smem[];
+  float* D = smem;
+  float* part = D + kNB * kDPitch;
+  float* acc = part + kGroups * kNB;
   __shared__ int sb;
-  __shared__ float acc[kNB];
-  __shared__ float D[kNB][kNB + 1];
+  constexpr int kWarps = kTrsvThreads / 32;  // 16
+  constexpr int kCols = kNB / kWarps;        // 8 columns per warp
+  constexpr int kRows = kNB / 32;            // 4 rows per lane
   const int64_t nbk = (n + kNB - 1) / kNB;
   if (threadIdx.x == 0) sb = (int)(nbk - 1) - atomicAdd(ticket, 1);
   __syncthreads();
   const int64_t b = sb, r0 = b * kNB;
   const int nb = (int)std::min<int64_t>(kNB, n - r0);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  for (int e = t; e < kNB * kNB; e += blockDim.x) D[e / kNB][e % kNB] = dinv[b * kNB * kNB + e];
+  for (int e = t; e < kNB * kNB; e += blockDim.x) D[(e / kNB) * kDPitch + e % kNB] = dinv[b * kNB * kNB + e];
   const int* bflags = flags + nbk;  // the backward pass's publications
-  // warp w owns columns i = w, w + 8, ... of block b: a_i = sum_{rows j of later blocks} L[j][r0 + i] v_j
-  float a[kNB / 8];
+  float a[kCols];
 #pragma unroll
-  for (int q = 0; q < kNB / 8; ++q) a[q] = 0.0f;
+  for (int q = 0; q < kCols; ++q) a[q] = 0.0f;
   for (int64_t k = nbk - 1; k > b; --k) {
-    if (lane == 0) wait_flag(bflags + k, epoch, err);
-    __syncwarp();
     const int64_t j0 = k * kNB;
     const int kn = (int)std::min<int64_t>(kNB, n - j0);
-    const float v0 = lane < kn ? __ldcg(v + j0 + lane) : 0.0f;
-    const float v1 = lane + 32 < kn ? __ldcg(v + j0 + lane + 32) : 0.0f;
+    float lv[kCols][kRows];
 #pragma unroll
-    for (int q = 0; q < kNB / 8; ++q) {
-      const int i = warp + 8 * q;
-      if (i < nb) {
-        const float* col = L + (r0 + i) * n + j0;  // column r0 + i, rows j0 ..
-        float s = lane < kn ? col[lane] * v0 : 0.0f;
-        if (lane + 32 < kn) s = fmaf(col[lane + 32], v1, s);
-        a[q] += s;
+    for (int q = 0; q < kCols; ++q) {
+      const int ic = warp + kWarps * q;
+      const float* col = L + (r0 + ic) * n + j0;  // column r0 + ic, rows j0 ..
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const int row = lane + 32 * r;
+        lv[q][r] = (ic < nb && row < kn) ? col[row] : 0.0f;
       }
     }
+    warp_wait_flag(bflags + k, epoch, err);
+    float vv[kRows];
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) vv[r] = lane + 32 * r < kn ? __ldcg(v + j0 + lane + 32 * r) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < kCols; ++q)
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) a[q] = fmaf(lv[q][r], vv[r], a[q]);
   }
 #pragma unroll
-  for (int q = 0; q < kNB / 8; ++q) {
+  for (int q = 0; q < kCols; ++q) {
     const float s = warp_sum(a[q]);
-    const int i = warp + 8 * q;
-    if (lane == 0 && i < kNB) acc[i] = (i < nb ? __ldcg(v + r0 + i) : 0.0f) - s;
+    const int ic = warp + kWarps * q;
+    if (lane == 0) acc[ic] = (ic < nb ? __ldcg(v + r0 + ic) : 0.0f) - s;
   }
   __syncthreads();
-  if (t < nb) {
-    // x_t = sum_j (L_bb^-T)[t][j] acc_j = sum_{j >= t} dinv[j][t] acc_j
+  // x_i = sum_{j >= i} (L_bb^-1)[j][i] acc_j, the j range split over four groups
+  {
+    const int i = t & (kNB - 1), g = t >> 7;
+    constexpr int kPer = kNB / kGroups;
     float x = 0.0f;
-    for (int j = t; j < nb; ++j) x = fmaf(D[j][t], acc[j], x);
-    __stcg(v + r0 + t, x);
+    const int j0 = g * kPer;
+#pragma unroll 8
+    for (int j = j0; j < j0 + kPer; ++j)
+      if (j >= i) x = fmaf(D[j * kDPitch + i], acc[j], x);
+    part[g * kNB + i] = x;
   }
+  __syncthreads();
+  if (t < nb) __stcg(v + r0 + t, part[t] + part[kNB + t] + part[2 * kNB + t] + part[3 * kNB + t]);
   __threadfence();
   __syncthreads();
   if (t == 0) st_release(flags + nbk + b, epoch);
@@ -214,9 +258,15 @@ int64_t trsv_chol_workspace_bytes(int64_t n) {
 int trsv_chol_prepare(const float* L, int64_t n, void* work, cudaStream_t st) {
   const TrsvWork w = layout(n, work);
   const int64_t nb = nblocks(n);
+  const size_t dsmem = (size_t)kNB * kDPitch * 4 + (size_t)kNB * (kNB + 1) * 4;
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(dinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(trsv_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)trsv_smem_bytes()));
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(trsv_upper_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)trsv_smem_bytes()));
   QGX_CHECK_CUDA(cudaMemsetAsync(w.flags, 0, 2 * nb * sizeof(int), st));
   QGX_CHECK_CUDA(cudaMemsetAsync(w.tickets, 0, 3 * sizeof(int), st));
-  dinv_kernel<<<(unsigned)nb, kNB, 0, st>>>(L, n, w.dinv);
+  dinv_kernel<<<(unsigned)nb, kNB, dsmem, st>>>(L, n, w.dinv);
   return launch_status();
 }
 
@@ -224,10 +274,12 @@ int trsv_chol_prepare(const float* L, int64_t n, void* work, cudaStream_t st) {
 int trsv_chol_apply(const float* L, int64_t n, float* v, void* work, uint32_t epoch, cudaStream_t st) {
   const TrsvWork w = layout(n, work);
   const int64_t nb = nblocks(n);
+  const size_t smem = trsv_smem_bytes();
   QGX_CHECK_CUDA(cudaMemsetAsync(w.tickets, 0, 2 * sizeof(int), st));
-  trsv_lower_kernel<<<(unsigned)nb, kTrsvThreads, 0, st>>>(L, n, v, w.dinv, w.flags, w.tickets, (int)epoch, w.err);
-  trsv_upper_kernel<<<(unsigned)nb, kTrsvThreads, 0, st>>>(L, n, v, w.dinv, w.flags, w.tickets + 1, (int)epoch,
-                                                           w.err);
+  trsv_lower_kernel<<<(unsigned)nb, kTrsvThreads, smem, st>>>(L, n, v, w.dinv, w.flags, w.tickets, (int)epoch,
+                                                               w.err);
+  trsv_upper_kernel<<<(unsigned)nb, kTrsvThreads, smem, st>>>(L, n, v, w.dinv, w.flags, w.tickets + 1, (int)epoch,
+                                                               w.err);
   return launch_status();
 }
 

@@ -575,11 +575,15 @@ def main():
     if not args.no_forms:
         # precision forms, same seed: tcgen05 Gram (+ tensor-core convolutions for ResConv)
         # and FP32 Cholesky with FP64 refinement
+        # accurate_*: the plain path's arithmetic (FP32 network, FP32-accurate split-TF32 Gram)
+        # with the FP64-refined solve in place of the FP64 factorisation
         if args.workload == "resconv":
-            variants = [("precision_tf32_conv_tf32_gram_mixed_solve", "tf32", "tf32"),
+            variants = [("accurate_fp32_conv_3xtf32_gram_mixed_solve", "fp32", "3xtf32"),
+                        ("precision_tf32_conv_tf32_gram_mixed_solve", "tf32", "tf32"),
                         ("precision_bf16_conv_bf16_gram_mixed_solve", "bf16", "bf16")]
         else:
-            variants = [("precision_tf32_gram_mixed_solve", "fp32", "tf32")]
+            variants = [("accurate_3xtf32_gram_mixed_solve", "fp32", "3xtf32"),
+                        ("precision_tf32_gram_mixed_solve", "fp32", "tf32")]
         for name, conv, gram in variants:
             prec = run_form(args, rank, world, gram, "mixed", e2e=False, conv=conv)
             de = [abs(a - b) / abs(b) for a, b in zip(prec["energies"], plain["energies"])]

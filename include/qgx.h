@@ -53,8 +53,8 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
 #define QGX_GRAM_TF32 1    /* tcgen05 kind::tf32, FP32 accumulation in TMEM */
 #define QGX_GRAM_BF16 2    /* tcgen05 kind::f16 with bf16 operands, FP32 accumulation */
 #define QGX_GRAM_3XTF32 3  /* tcgen05 split-TF32 (hi*hi + hi*lo + lo*hi), FP32 accuracy */
-#define QGX_GRAM_FP64 4    /* FP64 SIMT products and accumulation: the exact Gram of the FP32
-                            * operand up to FP64 rounding (for solves that keep eigenvalues
+#define QGX_GRAM_FP64 4    /* SIMT, exact FP32 products summed as float pairs: the Gram of the
+                            * FP32 operand to about 48 bits (for solves that keep eigenvalues
                             * below FP32 resolution, e.g. lstsq_pinv_eig(rtol=1e-9)) */
 
 /* ---- library ----------------------------------------------------------------- */

@@ -1,9 +1,11 @@
 // Gram matrices of the SR / MinSR solve (quantax/optimizer/solver.py:139 T = A A^T and
 // :157 S = A^T A), FP32 operands, written as FP64 for the solver.
 //
-// This file holds the SIMT paths: QGX_GRAM_FP32 (FP32 accumulation) and QGX_GRAM_FP64 (FP64
-// products and accumulation: a product of two FP32 numbers is exact in FP64, so the result is
-// the Gram of the FP32 matrix up to FP64 rounding). 128 x 128 output tiles, 256
+// This file holds the SIMT paths: QGX_GRAM_FP32 (FP32 accumulation) and QGX_GRAM_FP64, the
+// Gram of the FP32 matrix to about 48 bits: every product is formed exactly as a float pair
+// (TwoProd by FMA) and summed into a float-pair accumulator (TwoSum). FP64 arithmetic runs at
+// a small fraction of the FP32 rate on this GPU, and this keeps the work on the FP32 pipe.
+// 128 x 128 output tiles, 256
 // threads with 8 x 8 register micro-tiles, K staged through shared memory in chunks of
 // 16 with a register prefetch of the next chunk. Only tiles on or below the diagonal
 // are computed; each off-diagonal tile is written twice (itself and its mirror). The
@@ -32,7 +34,17 @@ __device__ inline float load_elem(const float* __restrict__ A, int64_t lda, int6
   return TRANS ? __ldg(A + kk * lda + vec) : __ldg(A + vec * lda + kk);
 }
 
-template <bool TRANS, typename ACC>
+// (h, l) += a * b exactly rounded to a float pair; the _rn intrinsics are never contracted
+__device__ inline void ds_fma(float a, float b, float& h, float& l) {
+  const float p = __fmul_rn(a, b);
+  const float e = fmaf(a, b, -p);
+  const float t = __fadd_rn(h, p);
+  const float z = __fsub_rn(t, h);
+  l = __fadd_rn(l, __fadd_rn(__fadd_rn(__fsub_rn(h, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+  h = t;
+}
+
+template <bool TRANS, bool DS>
 __global__ void __launch_bounds__(NT, 1)
     gram_simt_kernel(const float* __restrict__ A, int64_t nvec, int64_t klen, int64_t lda, double* __restrict__ T,
                      int64_t ldt) {
@@ -85,11 +97,15 @@ __global__ void __launch_bounds__(NT, 1)
     }
   };
 
-  ACC acc[8][8];
+  float acc[8][8], accl[DS ? 8 : 1][DS ? 8 : 1];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = ACC(0);
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < (DS ? 8 : 1); ++i)
+#pragma unroll
+    for (int j = 0; j < (DS ? 8 : 1); ++j) accl[i][j] = 0.0f;
 
   const int64_t nk = (klen + BK - 1) / BK;
   gload(0);
@@ -112,7 +128,28 @@ __global__ void __launch_bounds__(NT, 1)
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = fma((ACC)a[i], (ACC)b[j], acc[i][j]);
+        for (int j = 0; j < 8; ++j) {
+          if constexpr (DS) {
+            ds_fma(a[i], b[j], acc[i][j], accl[i & (DS ? 7 : 0)][j & (DS ? 7 : 0)]);
+          } else {
+            acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+          }
+        }
+    }
+    if constexpr (DS) {
+      // renormalise each pair (FastTwoSum, |h| >= |l|) once per chunk: the low word stays
+      // below half an ulp of the high word, which keeps its own rounding negligible (about
+      // 1e-13 relative at K = 8192, against 3e-12 without)
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float& h = acc[i][j];
+          float& l = accl[i & (DS ? 7 : 0)][j & (DS ? 7 : 0)];
+          const float t = __fadd_rn(h, l);
+          l = __fsub_rn(l, __fsub_rn(t, h));
+          h = t;
+        }
     }
     if (kc + 1 < nk) sstore(buf ^ 1);
     __syncthreads();
@@ -126,19 +163,21 @@ __global__ void __launch_bounds__(NT, 1)
     for (int j = 0; j < 8; ++j) {
       const int64_t c = col0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
       if (r < nvec && c < nvec) {
-        T[r * ldt + c] = (double)acc[i][j];
-        if (bi != bj) T[c * ldt + r] = (double)acc[i][j];
+        double v = (double)acc[i][j];
+        if constexpr (DS) v += (double)accl[i & (DS ? 7 : 0)][j & (DS ? 7 : 0)];
+        T[r * ldt + c] = v;
+        if (bi != bj) T[c * ldt + r] = v;
       }
     }
   }
 }
 
-template <bool TRANS, typename ACC = float>
+template <bool TRANS, bool DS = false>
 int launch_gram_simt(const float* A, int64_t nvec, int64_t klen, int64_t lda, double* T, int64_t ldt, cudaStream_t st) {
   const int64_t nb = (nvec + BM - 1) / BM;
   const int64_t tiles = nb * (nb + 1) / 2;
   if (tiles > 0x7fffffff) return QGX_ERR_UNSUPPORTED;
-  gram_simt_kernel<TRANS, ACC><<<(unsigned)tiles, NT, 0, st>>>(A, nvec, klen, lda, T, ldt);
+  gram_simt_kernel<TRANS, DS><<<(unsigned)tiles, NT, 0, st>>>(A, nvec, klen, lda, T, ldt);
   return launch_status();
 }
 
@@ -155,7 +194,7 @@ int qgx_gram(const float* A, int64_t rows, int64_t k, int64_t lda, double* T, in
   if (rows == 0) return QGX_OK;
   QGX_CHECK_ARG(A && T);
   if (mode == QGX_GRAM_FP32) return launch_gram_simt<false>(A, rows, k, lda, T, ldt, as_cuda(stream));
-  if (mode == QGX_GRAM_FP64) return launch_gram_simt<false, double>(A, rows, k, lda, T, ldt, as_cuda(stream));
+  if (mode == QGX_GRAM_FP64) return launch_gram_simt<false, true>(A, rows, k, lda, T, ldt, as_cuda(stream));
   if (mode == QGX_GRAM_TF32 || mode == QGX_GRAM_BF16 || mode == QGX_GRAM_3XTF32)
     return gram_tc(A, rows, k, lda, T, ldt, mode, as_cuda(stream));
   return QGX_ERR_ARG;

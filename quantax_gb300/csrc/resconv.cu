@@ -375,15 +375,19 @@ __global__ void rc_symm_combine_kernel(const float2* __restrict__ lp_g, int64_t 
     out[c] = make_float2(-INFINITY, 0.0f);
     return;
   }
-  double zr = 0.0, zi = 0.0;
+  // FP32 arithmetic: the inputs are FP32 log psi, and FP64 transcendentals run at a small
+  // fraction of the FP32 rate on this GPU
+  float zr = 0.0f, zi = 0.0f;
   for (int g = 0; g < nsymm; ++g) {
-    const double e = exp((double)l[g].x - (double)m);
-    const double ar = e * cos((double)l[g].y), ai = e * sin((double)l[g].y);
-    const double wr = weight[2 * g], wi = weight[2 * g + 1];
+    const float e = expf(l[g].x - m);
+    float sn, cs;
+    sincosf(l[g].y, &sn, &cs);
+    const float ar = e * cs, ai = e * sn;
+    const float wr = (float)weight[2 * g], wi = (float)weight[2 * g + 1];
     zr += wr * ar - wi * ai;
     zi += wr * ai + wi * ar;
   }
-  out[c] = make_float2((float)((double)m + 0.5 * log(zr * zr + zi * zi)), (float)atan2(zi, zr));
+  out[c] = make_float2(m + 0.5f * logf(zr * zr + zi * zi), atan2f(zi, zr));
 }
 
 // ---- per-sample log-derivatives (Variational.jacobian, quantax/state/variational.py:424-511) ----

@@ -35,6 +35,18 @@ def test_gram_fp32(cuda, shape):
     assert np.array_equal(T, T.T)
 
 
+@pytest.mark.parametrize("shape", [(300, 8192), (130, 1000), (1, 7)])
+def test_gram_fp64_mode(cuda, shape):
+    """QGX_GRAM_FP64: exact FP32 products summed as float pairs, renormalised every 16 terms:
+    the Gram of the FP32 matrix to about 1e-13. Stated: 1e-12 of sqrt(T_ii T_jj) per entry
+    (FP32 accumulation would be about 1e-6 here)."""
+    A = np.random.default_rng(shape[1]).normal(size=shape).astype(np.float32)
+    T = gram(A, mode=4)
+    ref = A.astype(np.float64) @ A.astype(np.float64).T
+    tol = 1e-12 * np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+    assert (np.abs(T - ref) <= tol + 1e-300).all()
+
+
 def test_gram_transposed(cuda):
     L = lib()
     A = np.random.default_rng(3).normal(size=(500, 130)).astype(np.float32)

@@ -279,7 +279,9 @@ class Operator:
         return float(Em.real)
 
     # ---- exact diagonalisation (operator.py:331-359), small systems only -------------------
-    def to_sparse(self, nup=None):
+    def to_sparse(self, nup=None, return_states: bool = False):
+        """Sparse H in the computational basis (bit i of a state's index = site i up), on the
+        sector with nup up spins when given; return_states also returns those basis indices."""
         n = get_sites().N
         if n > 30:
             raise ValueError("exact diagonalisation is limited to N <= 30 sites")
@@ -311,19 +313,67 @@ class Operator:
             ok = (el != 0) & (tgt >= 0)
             rows.append(np.flatnonzero(ok)); cols.append(tgt[ok]); vals.append(el[ok])
         m = len(states)
-        return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(m, m))
+        H = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(m, m))
+        return (H, states) if return_states else H
 
     def todense(self, nup=None) -> np.ndarray:
         return self.to_sparse(nup).toarray()
 
     def diagonalize(self, symm=None, k: Union[int, str] = 1, nup=None):
-        if symm is not None:
-            raise NotImplementedError("symmetry-projected diagonalisation is not implemented")
-        H = self.to_sparse(nup)
-        if k == "full" or H.shape[0] <= 256:
-            w, v = np.linalg.eigh(H.toarray())
+        """Lowest k eigenpairs (operator.py:331-359), on the sites' fixed-magnetisation sector
+        when Nparticles is given. With a symmetry, the spectrum of H inside the symmetry sector:
+        the lowest eigenvalues of P (H - c) P + c, P = sum_g w_g T_g the sector's projector
+        (Symmetry.symmetrize), c >= ||H|| so that P's null space lies above every sector
+        energy. The reference builds the reduced QuSpin basis instead; here the eigenvectors
+        are returned in the full (fixed-magnetisation) computational basis, normalised."""
+        sites = get_sites()
+        if nup is None and isinstance(sites.Nparticles, tuple):
+            nup = sites.Nparticles[0]
+        H, states = self.to_sparse(nup, return_states=True)
+        if symm is None or symm.is_identity:
+            if k == "full" or H.shape[0] <= 256:
+                w, v = np.linalg.eigh(H.toarray())
+                return (w, v) if k == "full" else (w[:k], v[:, :k])
+            return spla.eigsh(H, k=k, which="SA", tol=1e-12)
+        P = self._sector_projector(symm, states)
+        c = float(abs(H).sum(axis=1).max())  # an upper bound of ||H||_2
+        D = H.shape[0]
+        if k == "full" or D <= 256:
+            w, v = np.linalg.eigh((P @ (H - c * sp.identity(D)) @ P).toarray())
+            keep = w < -1e-9 * c
+            w, v = w[keep] + c, v[:, keep]
             return (w, v) if k == "full" else (w[:k], v[:, :k])
-        return spla.eigsh(H, k=k, which="SA", tol=1e-12)
+        Hc = (H - c * sp.identity(D)).tocsr()
+        op = spla.LinearOperator((D, D), matvec=lambda x: P @ (Hc @ (P @ x)), dtype=P.dtype)
+        v0 = P @ np.random.default_rng(0).normal(size=D).astype(P.dtype)
+        w, v = spla.eigsh(op, k=k, which="SA", v0=v0, tol=1e-12)
+        order = np.argsort(w)
+        v = v[:, order]
+        return w[order] + c, v / np.linalg.norm(v, axis=0, keepdims=True)
+
+    @staticmethod
+    def _sector_projector(symm, states):
+        """(P x)(s) = sum_g w_g x(T_g s) on the basis `states` (sparse, D x D)."""
+        n = get_sites().N
+        spins = ((states[:, None] >> np.arange(n)) & 1).astype(np.int64)  # 1 = up
+        lookup = {int(c): i for i, c in enumerate(states)}
+        weights = symm.weights()
+        perms = symm.perm
+        rows, cols, vals = [], [], []
+        D = len(states)
+        for g, w in enumerate(weights):
+            bits = spins[:, perms[g % len(perms)]]
+            if g >= len(perms):
+                bits = 1 - bits  # Z2 inversion
+            codes = (bits << np.arange(n)).sum(axis=1)
+            try:
+                idx = np.fromiter((lookup[int(c)] for c in codes), dtype=np.int64, count=D)
+            except KeyError:
+                raise ValueError("the symmetry does not preserve the basis (spin inversion needs Nup = N/2)")
+            rows.append(np.arange(D)); cols.append(idx); vals.append(np.full(D, w))
+        dtype = np.complex128 if np.iscomplexobj(weights) and np.any(np.imag(weights) != 0) else np.float64
+        vals = np.concatenate(vals).astype(dtype) if dtype == np.complex128 else np.real(np.concatenate(vals))
+        return sp.csr_matrix((vals, (np.concatenate(rows), np.concatenate(cols))), shape=(D, D))
 
 
 # ---- site operators (site_operator.py:8-132) ------------------------------------------------

@@ -184,11 +184,15 @@ __global__ void __launch_bounds__(kFwdThreads)
 
 // ---- SpinExchange step ----------------------------------------------------------------
 // proposal of chain c at draw t: site i uniform among the hopping spins, j uniform in the
-// padded neighbour row of i (-1: no move); writes the swapped configuration and changed flag
-__global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* __restrict__ prop,
-                                  int8_t* __restrict__ changed, int64_t ns, int n, uint64_t seed,
-                                  const uint64_t* __restrict__ step_base, int t, const int32_t* __restrict__ nbr, int z,
-                                  int hop) {
+// padded neighbour row of i (-1: no move). Only proposals that change the configuration are
+// evaluated (as the reference's chunked sweep does, sampler/metropolis.py:216-242): a changed
+// one is appended to the compacted batch comp at an atomic position, recorded in comp_idx[c]
+// (-1: unchanged); *n_live counts them. Every configuration's forward is independent of the
+// others in its batch, so the order of the batch does not change any result.
+__global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* __restrict__ comp,
+                                  int32_t* __restrict__ comp_idx, unsigned long long* __restrict__ n_live, int64_t ns,
+                                  int n, uint64_t seed, const uint64_t* __restrict__ step_base, int t,
+                                  const int32_t* __restrict__ nbr, int z, int hop) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ns) return;
   const uint64_t step = *step_base + (uint64_t)t;
@@ -196,24 +200,34 @@ __global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* 
   uint32_t w[8];
   for (int k = 0; k < nw; ++k) w[k] = spins[c * nw + k];
   const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
-  const int8_t ch = propose_exchange(w, n, nw, r, nbr, z, hop) ? 1 : 0;
-  for (int k = 0; k < nw; ++k) prop[c * nw + k] = w[k];
-  changed[c] = ch;
+  if (!propose_exchange(w, n, nw, r, nbr, z, hop)) {
+    comp_idx[c] = -1;
+    return;
+  }
+  const unsigned long long pos = atomicAdd(n_live, 1ull);
+  for (int k = 0; k < nw; ++k) comp[pos * nw + k] = w[k];
+  comp_idx[c] = (int32_t)pos;
 }
 
+// Metropolis test of the changed chains against their compacted log psi; thread 0 resets the
+// live count for the next step (its forward has finished reading it)
 __global__ void rc_accept_kernel(uint32_t* __restrict__ spins, float2* __restrict__ lp,
-                                 const uint32_t* __restrict__ prop, const float2* __restrict__ lp_prop,
-                                 const int8_t* __restrict__ changed, int32_t* __restrict__ accepts, int64_t ns, int n,
-                                 uint64_t seed, const uint64_t* __restrict__ step_base, int t, float reweight) {
+                                 const uint32_t* __restrict__ comp, const float2* __restrict__ lp_comp,
+                                 const int32_t* __restrict__ comp_idx, unsigned long long* __restrict__ n_live,
+                                 int32_t* __restrict__ accepts, int64_t ns, int n, uint64_t seed,
+                                 const uint64_t* __restrict__ step_base, int t, float reweight) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c == 0) *n_live = 0ull;
   if (c >= ns) return;
+  const int32_t idx = comp_idx[c];
+  if (idx < 0) return;
   const uint64_t step = *step_base + (uint64_t)t;
   const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
   const float rhs = log1pf(-unit_float(r.y));
-  if (changed[c] && reweight * (lp_prop[c].x - lp[c].x) > rhs) {
+  if (reweight * (lp_comp[idx].x - lp[c].x) > rhs) {
     const int nw = words_for(n);
-    for (int k = 0; k < nw; ++k) spins[c * nw + k] = prop[c * nw + k];
-    lp[c] = lp_prop[c];
+    for (int k = 0; k < nw; ++k) spins[c * nw + k] = comp[(int64_t)idx * nw + k];
+    lp[c] = lp_comp[idx];
     if (accepts) accepts[c] += 1;
   }
 }
@@ -291,7 +305,11 @@ __global__ void rc_conn_write_kernel(qgx_operator_t op, const uint32_t* __restri
 }
 
 // E_loc(s) = diag(s) + sum_k elem_k exp(log psi(s'_k) - log psi(s)), complex
-__global__ void rc_set_step_kernel(uint64_t* __restrict__ step_base, uint64_t step0) { *step_base = step0; }
+// the Philox step base of a sweep, and the live count of the compacted proposals (zero)
+__global__ void rc_set_step_kernel(uint64_t* __restrict__ step_base, uint64_t step0) {
+  step_base[0] = step0;
+  step_base[1] = 0;
+}
 
 __global__ void rc_eloc_reduce_kernel(qgx_operator_t op, const uint32_t* __restrict__ spins, int64_t ns, int n,
                                       const float2* __restrict__ lp, const int64_t* __restrict__ offsets,
@@ -859,7 +877,8 @@ int qgx_resconv_log_psi(const float* table, int32_t L, int32_t nblocks, int32_t 
 int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns) {
   if (L < 1 || ns < 1) return 0;
   const int nw = words_for(L * L);
-  return al256(ns * nw * 4) + al256(ns * 8) + al256(ns) + al256(8);  // + the Philox step base
+  // compacted proposals, their log psi, their positions, then the step base and live count
+  return al256(ns * nw * 4) + al256(ns * 8) + al256(ns * 4) + al256(16);
 }
 
 }  // extern "C"
@@ -874,11 +893,12 @@ int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels,
   const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
   const int nw = words_for(net.N);
   char* ws = static_cast<char*>(workspace);
-  uint32_t* prop = reinterpret_cast<uint32_t*>(ws);
-  float2* lp_prop = reinterpret_cast<float2*>(ws + al256(ns * nw * 4));
-  int8_t* changed = reinterpret_cast<int8_t*>(ws + al256(ns * nw * 4) + al256(ns * 8));
-  uint64_t* step_base = reinterpret_cast<uint64_t*>(ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns));
-  char* sscratch = ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns) + al256(8);
+  uint32_t* comp = reinterpret_cast<uint32_t*>(ws);
+  float2* lp_comp = reinterpret_cast<float2*>(ws + al256(ns * nw * 4));
+  int32_t* comp_idx = reinterpret_cast<int32_t*>(ws + al256(ns * nw * 4) + al256(ns * 8));
+  uint64_t* step_base = reinterpret_cast<uint64_t*>(ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns * 4));
+  unsigned long long* n_live = reinterpret_cast<unsigned long long*>(step_base + 1);
+  char* sscratch = ws + al256(ns * nw * 4) + al256(ns * 8) + al256(ns * 4) + al256(16);
   float2* lp = reinterpret_cast<float2*>(log_psi);
   const unsigned g = (unsigned)((ns + 127) / 128);
   // the launch sequence of the sweep (recorded into the graph)
@@ -887,10 +907,12 @@ int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels,
     if (rc != QGX_OK) return rc;
     if (accepts) QGX_CHECK_CUDA(cudaMemsetAsync(accepts, 0, ns * sizeof(int32_t), s));
     for (int t = 0; t < nsteps; ++t) {
-      rc_propose_kernel<<<g, 128, 0, s>>>(spins, prop, changed, ns, net.N, seed, step_base, t, nbr, z, hop);
-      if ((rc = symm_forward(table, net, sym, prop, ns, nullptr, lp_prop, sscratch, s)) != QGX_OK) return rc;
-      rc_accept_kernel<<<g, 128, 0, s>>>(spins, lp, prop, lp_prop, changed, accepts, ns, net.N, seed, step_base, t,
-                                         reweight);
+      rc_propose_kernel<<<g, 128, 0, s>>>(spins, comp, comp_idx, n_live, ns, net.N, seed, step_base, t, nbr, z,
+                                          hop);
+      rc = symm_forward(table, net, sym, comp, ns, reinterpret_cast<const int64_t*>(n_live), lp_comp, sscratch, s);
+      if (rc != QGX_OK) return rc;
+      rc_accept_kernel<<<g, 128, 0, s>>>(spins, lp, comp, lp_comp, comp_idx, n_live, accepts, ns, net.N, seed,
+                                         step_base, t, reweight);
     }
     return launch_status();
   };

@@ -523,6 +523,8 @@ def main():
                     help="plain-path Gram: split-TF32 on the tensor cores is FP32-class (accumulation error "
                          "6.6e-6 against 8.2e-5 for fp32 on the CUDA cores)")
     ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--conv", default="fp32", choices=["fp32", "tf32", "bf16"],
+                    help="resconv: arithmetic of the convolutions of the main run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
     ap.add_argument("--tutorial-steps", type=int, default=200, help="*_tutorial: SR steps per phase")
@@ -570,7 +572,8 @@ def main():
         run_rbm_example(args, rank)
         return
 
-    plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None)
+    plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None,
+                     conv=args.conv)
     forms = {}
     if not args.no_forms:
         # precision forms, same seed: tcgen05 Gram (+ tensor-core convolutions for ResConv)
@@ -624,7 +627,7 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 solve)",
             "data": "synthetic",
             "config": dict(WORKLOAD if args.workload == "rbm" else WORKLOAD_RESCONV, parallelism=f"replicas x{world}",
-                           gram=args.gram, solve=args.solve),
+                           gram=args.gram, solve=args.solve, **({"conv": args.conv} if args.workload == "resconv" else {})),
             "samples_per_s": world * args.steps * (8192 if args.workload == "rbm" else 16384) / elapsed, "p50_step_ms": percentile(plain["lat"], 0.5),
             "p99_step_ms": percentile(plain["lat"], 0.99),
             "phases_ms": {k: round(v, 4) for k, v in phases.items()}, "energy": plain["energies"][-1],

@@ -143,7 +143,7 @@ KERNELS_PER_CALL = {
     "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6, "qgx_resconv_log_psi_symm": 3, "qgx_resconv_eloc_symm": 10,
     "qgx_resconv_jacobian_symm": 4,
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
-    "qgx_center_columns": 3, "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1,
+    "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1,
     "qgx_rbm_conv_jacobian": 1, "qgx_apply_update": 2,
 }
 launch_count = 0
@@ -152,6 +152,8 @@ launch_count = 0
 def _kernels(name, args):
     if name in ("qgx_minsr_solve", "qgx_sr_solve", "qgx_sym_solve"):
         return int(lib().qgx_last_solve_kernels())
+    if name == "qgx_center_columns":  # partial sums, reduction, mean split, then 65535 rows per centring launch
+        return 3 + (int(args[1]) - 1) // 65535 + 1 if int(args[1]) > 0 else 0
     if name == "qgx_scale_columns":
         return 1 + (int(args[1]) - 1) // 65535 if int(args[1]) > 0 and int(args[2]) > 0 else 0
     if name == "qgx_resconv_sweep":

@@ -230,31 +230,45 @@ __global__ void __launch_bounds__(kStatThreads) reweight_kernel(const float* __r
 constexpr int kColThreads = 256;
 constexpr int kColRows = 128;  // rows per partial-sum chunk
 
+// per column and chunk of kColRows rows: sum of O and of r O, as float-pair sums (DSum)
 __global__ void col_partial_kernel(const float* __restrict__ O, int64_t ns, int64_t np, int64_t ldo,
                                    const double* __restrict__ r, double* __restrict__ part_u,
                                    double* __restrict__ part_w) {
-  const int64_t col = blockIdx.x * (int64_t)kColThreads + threadIdx.x;
+  __shared__ float2 rs[kColRows];
   const int64_t chunk = blockIdx.y;
-  if (col >= np) return;
   const int64_t r0 = chunk * kColRows;
   const int64_t r1 = min(ns, r0 + kColRows);
-  double su = 0.0, sw = 0.0;
+  for (int64_t s = r0 + threadIdx.x; s < r1; s += blockDim.x) rs[s - r0] = split_double(r ? r[s] : 1.0);
+  __syncthreads();
+  const int64_t col = blockIdx.x * (int64_t)kColThreads + threadIdx.x;
+  if (col >= np) return;
+  DSum su, sw;
   for (int64_t s = r0; s < r1; ++s) {
-    const double v = (double)O[s * ldo + col];
-    su += v;
-    sw += v * (r ? r[s] : 1.0);
+    const float v = O[s * ldo + col];
+    su.add(v);
+    const float2 rv = rs[s - r0];
+    sw.add_prod(v, rv.x, rv.y);
   }
-  part_u[chunk * np + col] = su;
-  part_w[chunk * np + col] = sw;
+  part_u[chunk * np + col] = su.value();
+  part_w[chunk * np + col] = sw.value();
 }
 
+// O[s][col] <- (O[s][col] - mean[col]) sqrt(r_s / ns) in FP32: the mean enters as two floats
+// (hi + lo), so the difference is within about two ulps of the FP64-computed one
 __global__ void col_center_kernel(float* __restrict__ O, int64_t row0, int64_t ns, int64_t np, int64_t ldo,
-                                  const double* __restrict__ r, const double* __restrict__ mean_u) {
+                                  const double* __restrict__ r, const float2* __restrict__ mean2) {
   const int64_t s = row0 + blockIdx.y;
-  const double f = sqrt((r ? r[s] : 1.0) / (double)ns);
+  const float f = (float)sqrt((r ? r[s] : 1.0) / (double)ns);
+  float* row = O + s * ldo;
   for (int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; col < np; col += (int64_t)gridDim.x * blockDim.x) {
-    O[s * ldo + col] = (float)(((double)O[s * ldo + col] - mean_u[col]) * f);
+    const float2 m = mean2[col];
+    row[col] = __fmul_rn(__fsub_rn(__fsub_rn(row[col], m.x), m.y), f);
   }
+}
+
+__global__ void split_mean_kernel(const double* __restrict__ mean_u, int64_t np, float2* __restrict__ mean2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x)
+    mean2[i] = split_double(mean_u[i]);
 }
 
 // ---- guarded update ---------------------------------------------------------------------
@@ -408,7 +422,7 @@ int qgx_reweight_factor(const float* log_psi, int64_t ns, float reweight, double
 int64_t qgx_center_columns_workspace_bytes(int64_t ns, int64_t np) {
   if (ns <= 0 || np <= 0) return 0;
   const int64_t nchunk = (ns + kColRows - 1) / kColRows;
-  return (2 * nchunk * np + np) * (int64_t)sizeof(double);
+  return (2 * nchunk * np + 2 * np) * (int64_t)sizeof(double);  // partials, the mean, its float pair
 }
 
 int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const double* r, double* omean,
@@ -420,14 +434,16 @@ int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const doub
   double* part_u = static_cast<double*>(workspace);
   double* part_w = part_u + nchunk * np;
   double* mean_u = part_w + nchunk * np;
+  float2* mean2 = reinterpret_cast<float2*>(mean_u + np);
   cudaStream_t st = as_cuda(stream);
   dim3 g1(blocks_for(np, kColThreads), (unsigned)nchunk);
   col_partial_kernel<<<g1, kColThreads, 0, st>>>(O, ns, np, ldo, r, part_u, part_w);
   col_reduce_kernel<<<blocks_for(np, 256), 256, 0, st>>>(part_u, part_w, nchunk, np, ns, mean_u, omean, nullptr);
+  split_mean_kernel<<<blocks_for(np, 256), 256, 0, st>>>(mean_u, np, mean2);
   const unsigned gx = (unsigned)std::min<int64_t>(blocks_for(np, 256), 64);
   for (int64_t r0 = 0; r0 < ns; r0 += 65535) {
     const int64_t rows = std::min<int64_t>(65535, ns - r0);
-    col_center_kernel<<<dim3(gx, (unsigned)rows), 256, 0, st>>>(O, r0, ns, np, ldo, r, mean_u);
+    col_center_kernel<<<dim3(gx, (unsigned)rows), 256, 0, st>>>(O, r0, ns, np, ldo, r, mean2);
   }
   return launch_status();
 }

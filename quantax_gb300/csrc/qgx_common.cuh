@@ -84,6 +84,35 @@ __host__ __device__ inline float unit_float(uint32_t w) { return (float)(w >> 8)
 __host__ __device__ inline int words_for(int n) { return (n + 31) >> 5; }
 
 // ---- warp helpers ----------------------------------------------------------------------
+// A sum kept as an unevaluated pair of floats (h + l), about 48 bits: exact FP32 products
+// (TwoProd by FMA) and TwoSum accumulation on the FP32 pipe, where FP64 arithmetic runs at a
+// small fraction of the FP32 rate. The _rn intrinsics are never contracted into FMAs, which
+// would void the error terms.
+struct DSum {
+  float h = 0.0f, l = 0.0f;
+  __device__ inline void add2(float p, float e) {  // (h, l) += p + e, |e| small
+    const float t = __fadd_rn(h, p);
+    const float z = __fsub_rn(t, h);
+    l = __fadd_rn(l, __fadd_rn(__fadd_rn(__fsub_rn(h, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+    h = t;
+  }
+  __device__ inline void add(float v) { add2(v, 0.0f); }
+  // += a * (yh + yl), the product formed exactly
+  __device__ inline void add_prod(float a, float yh, float yl) {
+    const float p = __fmul_rn(a, yh);
+    float e = fmaf(a, yh, -p);
+    e = fmaf(a, yl, e);
+    add2(p, e);
+  }
+  __device__ inline double value() const { return (double)h + (double)l; }
+};
+
+// a double as two floats, hi + lo
+__device__ inline float2 split_double(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
 __device__ inline float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

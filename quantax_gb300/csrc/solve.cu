@@ -68,35 +68,16 @@ __global__ void shift_diag_kernel(double* __restrict__ T, int64_t n, int64_t ldt
 }
 
 // partial[chunk, col] = sum_{rows in chunk} A[s, col] y[s] to about 48 bits (the reference
-// forms x = A^T y in float64, solver.py:58-61, 144-146). FP64 arithmetic runs at a small
-// fraction of the FP32 rate on this GPU, so the sum is kept as an unevaluated pair of floats:
-// y = yh + yl (two floats), a*yh exactly as p + e (TwoProd by FMA), a*yl added to e, and
-// (sh, sl) += (p, e) by TwoSum. Four columns per thread, 16-byte loads; the chunk's y split
-// once into shared memory.
-struct DSum {
-  float h = 0.0f, l = 0.0f;
-  // the _rn intrinsics are never contracted into FMAs, which would void the error terms
-  __device__ inline void add_prod(float a, float yh, float yl) {
-    const float p = __fmul_rn(a, yh);
-    float e = fmaf(a, yh, -p);
-    e = fmaf(a, yl, e);
-    const float t = __fadd_rn(h, p);
-    const float z = __fsub_rn(t, h);
-    l = __fadd_rn(l, __fadd_rn(__fadd_rn(__fsub_rn(h, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
-    h = t;
-  }
-  __device__ inline double value() const { return (double)h + (double)l; }
-};
-
+// forms x = A^T y in float64, solver.py:58-61, 144-146), as float-pair sums (DSum) with
+// y = yh + yl. Four columns per thread, 16-byte loads; the chunk's y split once into shared
+// memory.
 __global__ void project_partial_kernel(const float* __restrict__ A, int64_t nrow, int64_t ncol, int64_t lda,
                                        const double* __restrict__ y, double* __restrict__ part, bool vec4) {
   __shared__ float2 ys[kProjRows];
   const int64_t r0 = (int64_t)blockIdx.y * kProjRows;
   const int64_t r1 = min(nrow, r0 + kProjRows);
   for (int64_t s = r0 + threadIdx.x; s < r1; s += blockDim.x) {
-    const double v = y[s];
-    const float hi = (float)v;
-    ys[s - r0] = make_float2(hi, (float)(v - (double)hi));
+    ys[s - r0] = split_double(y[s]);
   }
   __syncthreads();
   const int64_t c0 = 4 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);

@@ -380,6 +380,11 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda,
 int qgx_obar_rmatvec_workspace_bytes(int64_t rows, int64_t cols, int64_t* bytes);
 int qgx_obar_rmatvec(const float* A, int64_t rows, int64_t cols, int64_t lda, const double* b,
                      double* y, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+/* out[col] = sum over rows of A[row][col]^2 (diag(A^T A)), about 48-bit sums; workspace from
+ * qgx_column_sumsq_workspace_bytes (lstsq_shift_cg's relative shift, solver.py:24-47). */
+int64_t qgx_column_sumsq_workspace_bytes(int64_t rows, int64_t cols);
+int qgx_column_sumsq(const float* A, int64_t rows, int64_t cols, int64_t lda, double* out,
+                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
 /* x = S^-1 f for a symmetric S (n x n FP64, overwritten): PINV is pinvh_solve
  * (solver.py:104-111, eigh with the soft inverse), SHIFT the shifted Cholesky solve.
  * Workspace: qgx_solve_workspace_bytes(n, 1, method). */

@@ -170,3 +170,30 @@ def adamsr_step(A, b, m, v, t, mu, beta, solver, a_dtype=np.float32):
     As = (A * (1.0 / V)[None, :]).astype(a_dtype).astype(np.float64)
     step = solver(As, b) / V + mh
     return step, m, v
+
+
+# ---- further solvers of quantax/optimizer/solver.py ---------------------------------------
+def sgd(A, b):
+    """sgd_solver (solver.py:297-302)."""
+    return A.conj().T @ b / b.shape[0]
+
+
+def lstsq_shift_direct(A, b, diag_shift):
+    """The solution lstsq_shift_cg (solver.py:24-47) converges to: (S + diag_shift diag(S)) x = A^H b."""
+    S = A.conj().T @ A
+    return np.linalg.solve(S + diag_shift * np.diag(np.diag(S)), A.conj().T @ b)
+
+
+def block_pinv(A, b, blocks, rtol=None, atol=0.0):
+    """block_pinv_eig (solver.py:204-259): auto pinv per layer's columns, b / nlayers."""
+    out, c0 = [], 0
+    for n in blocks:
+        out.append(auto(A[:, c0:c0 + n], b / len(blocks), "pinv", rtol=rtol, atol=atol))
+        c0 += n
+    return np.concatenate(out)
+
+
+def minsr_pinv(T, b, rtol=None, atol=0.0):
+    """minsr_pinv_eig (solver.py:262-294) without the SNR truncation."""
+    lam, U = np.linalg.eigh(T)
+    return U @ (eigs_inv(lam, rtol, atol) * (U.conj().T @ b))

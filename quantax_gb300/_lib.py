@@ -119,6 +119,8 @@ SIGNATURES = {
     "qgx_rbm_conv_table_floats": (i64, [i32, i32, i32]),
     "qgx_rbm_conv_prepare": (C.c_int, [vp, i32, i32, i32, vp, vp]),
     "qgx_rbm_conv_jacobian": (C.c_int, [vp, i32, i32, i32, vp, i64, vp, i64, vp]),
+    "qgx_column_sumsq_workspace_bytes": (i64, [i64, i64]),
+    "qgx_column_sumsq": (C.c_int, [vp, i64, i64, i64, vp, vp, i64, vp]),
     "qgx_obar_rmatvec_workspace_bytes": (C.c_int, [i64, i64, vp]),
     "qgx_obar_rmatvec": (C.c_int, [vp, i64, i64, i64, vp, vp, vp, i64, vp]),
     "qgx_sym_solve": (C.c_int, [vp, i64, vp, i32, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
@@ -143,7 +145,7 @@ KERNELS_PER_CALL = {
     "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6, "qgx_resconv_log_psi_symm": 3, "qgx_resconv_eloc_symm": 10,
     "qgx_resconv_jacobian_symm": 4,
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
-    "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1,
+    "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1, "qgx_column_sumsq": 2,
     "qgx_rbm_conv_jacobian": 1, "qgx_apply_update": 2,
 }
 launch_count = 0

@@ -271,6 +271,30 @@ __global__ void split_mean_kernel(const double* __restrict__ mean_u, int64_t np,
     mean2[i] = split_double(mean_u[i]);
 }
 
+// out[col] = sum_s A[s][col]^2 as float-pair sums (diag(A^T A), the relative shift of
+// lstsq_shift_cg, solver.py:32-36); one thread per column, rows in chunks of kColRows
+__global__ void col_sumsq_kernel(const float* __restrict__ A, int64_t rows, int64_t cols, int64_t lda,
+                                 double* __restrict__ part) {
+  const int64_t col = blockIdx.x * (int64_t)kColThreads + threadIdx.x;
+  if (col >= cols) return;
+  const int64_t r0 = (int64_t)blockIdx.y * kColRows, r1 = min(rows, r0 + kColRows);
+  DSum acc;
+  for (int64_t s = r0; s < r1; ++s) {
+    const float v = A[s * lda + col];
+    acc.add_prod(v, v, 0.0f);
+  }
+  part[blockIdx.y * cols + col] = acc.value();
+}
+
+__global__ void col_sum_parts_kernel(const double* __restrict__ part, int64_t nchunk, int64_t cols,
+                                     double* __restrict__ out) {
+  const int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (col >= cols) return;
+  double s = 0.0;
+  for (int64_t c = 0; c < nchunk; ++c) s += part[c * cols + col];
+  out[col] = s;
+}
+
 // ---- guarded update ---------------------------------------------------------------------
 __global__ void finite_check_kernel(const double* __restrict__ step, int64_t np, int32_t* __restrict__ flag) {
   bool bad = false;
@@ -445,6 +469,25 @@ int qgx_center_columns(float* O, int64_t ns, int64_t np, int64_t ldo, const doub
     const int64_t rows = std::min<int64_t>(65535, ns - r0);
     col_center_kernel<<<dim3(gx, (unsigned)rows), 256, 0, st>>>(O, r0, ns, np, ldo, r, mean2);
   }
+  return launch_status();
+}
+
+int64_t qgx_column_sumsq_workspace_bytes(int64_t rows, int64_t cols) {
+  if (rows <= 0 || cols <= 0) return 0;
+  return ((rows + kColRows - 1) / kColRows) * cols * (int64_t)sizeof(double);
+}
+
+int qgx_column_sumsq(const float* A, int64_t rows, int64_t cols, int64_t lda, double* out, void* workspace,
+                     int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(rows > 0 && cols > 0 && lda >= cols && A && out && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_column_sumsq_workspace_bytes(rows, cols));
+  const int64_t nchunk = (rows + kColRows - 1) / kColRows;
+  QGX_CHECK_ARG(nchunk <= 65535);
+  cudaStream_t st = as_cuda(stream);
+  double* part = static_cast<double*>(workspace);
+  col_sumsq_kernel<<<dim3(blocks_for(cols, kColThreads), (unsigned)nchunk), kColThreads, 0, st>>>(A, rows, cols, lda,
+                                                                                                   part);
+  col_sum_parts_kernel<<<blocks_for(cols, 256), 256, 0, st>>>(part, nchunk, cols, out);
   return launch_status();
 }
 

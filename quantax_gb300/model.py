@@ -76,6 +76,10 @@ class RBM_Dense:
     def nparams(self) -> int:
         return self.M * self.N + self.M + (self.N if self.visible_bias else 0)
 
+    def param_blocks(self) -> list:
+        """Parameter counts of the layers that hold parameters (one Linear layer)."""
+        return [self.nparams]
+
     @classmethod
     def from_arrays(cls, W, b, a=None):
         """Model with explicit parameters (W (M, N), b (M), optional a (N))."""
@@ -237,6 +241,15 @@ class ResConv:
     @property
     def nparams(self) -> int:
         return int(self.init_params.size)
+
+    def param_blocks(self) -> list:
+        """Parameter counts of the layers that hold parameters: one per residual block
+        (conv_nets.py:26-92; the reshape, final and symmetrising layers hold none)."""
+        C, out = self.channels, []
+        for b in range(self.nblocks):
+            cin = 1 if b == 0 else C
+            out.append(C * cin * 9 + C + C * C * 9 + (C if b != self.nblocks - 1 else 0))
+        return out
 
     def table_floats(self) -> int:
         return int(_lib.lib().qgx_resconv_table_floats(self.nblocks, self.channels))

@@ -33,6 +33,9 @@ class Solver:
     atol: float = 0.0
     tol_snr: float = 0.0
     precision: str = "fp64"   # "fp64" or "mixed" (FP32 Cholesky + FP64 refinement, shift only)
+    diag_shift: float = 0.0   # shift_cg: relative diagonal shift
+    maxiter: Optional[int] = None  # shift_cg: iteration limit (default 10 Np, as jax's cg)
+    blocks: Optional[tuple] = None  # block_pinv_eig: parameter counts of the layers
 
     def use_minnorm(self, ns: int, np_: int) -> bool:
         if self.branch == "auto":
@@ -69,6 +72,51 @@ def minnorm_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4, prec
 def lstsq_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4) -> Solver:
     """solver.py:65-77"""
     return Solver("shift", "lstsq", rshift=rshift, ashift=ashift)
+
+
+def lstsq_shift_cg(diag_shift: float = 0.01, rtol: float = 1e-5, atol: float = 0.0,
+                   maxiter: Optional[int] = None) -> Solver:
+    """solver.py:24-47: conjugate gradients on (S + diag_shift diag(S)) x = A^T b, S = A^T A
+    applied without forming it; stops when |r| <= max(rtol |A^T b|, atol) (jax's cg)."""
+    return Solver("shift_cg", "lstsq", rtol=rtol, atol=atol, diag_shift=float(diag_shift), maxiter=maxiter)
+
+
+def sgd_solver() -> Solver:
+    """solver.py:297-302: x = A^T b / len(b)."""
+    return Solver("sgd")
+
+
+def block_pinv_eig(state, rtol: Optional[float] = None, atol: float = 0.0, tol_snr: float = 0.0) -> Solver:
+    """solver.py:204-259: auto_pinv_eig on each layer's columns of Obar with Ebar / nlayers,
+    the layers being those of the model's Sequential that hold parameters."""
+    blocks = tuple(int(b) for b in state.model.param_blocks())
+    if sum(blocks) != state.nparams:
+        raise ValueError("the model's layer sizes do not add up to its parameter count")
+    return Solver("pinv", "auto", rtol=rtol, atol=atol, tol_snr=tol_snr, blocks=blocks)
+
+
+class minsr_pinv_eig:
+    """solver.py:262-294: x = T^+ b for a Hermitian T (FP64 device tensors), the soft
+    pseudo-inverse of the eigendecomposition. Called as solver(T, b); T is not modified."""
+
+    def __init__(self, rtol: Optional[float] = None, atol: float = 0.0, tol_snr: float = 0.0):
+        if tol_snr > 1e-6:
+            raise NotImplementedError("minsr_pinv_eig: the SNR truncation needs the per-sample terms")
+        self.rtol, self.atol = rtol, atol
+
+    def __call__(self, T: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+        import ctypes as C
+        n = T.shape[0]
+        S = T.to(torch.float64).clone()
+        f = b.to(torch.float64).contiguous()
+        nbytes = C.c_int64(0)
+        _lib.call("qgx_solve_workspace_bytes", n, 1, _lib.SOLVE_PINV, C.byref(nbytes))
+        ws = torch.empty(max(nbytes.value, 256), dtype=torch.uint8, device=T.device)
+        x = torch.empty(n, dtype=torch.float64, device=T.device)
+        rtol = _OBAR_RTOL if self.rtol is None else self.rtol
+        _lib.call("qgx_sym_solve", _lib.ptr(S), n, _lib.ptr(f), _lib.SOLVE_PINV, 0.0, 0.0, rtol, self.atol,
+                  _lib.ptr(x), None, _lib.ptr(ws), ws.numel(), _lib.stream_ptr())
+        return x
 
 
 # Default relative shift / eigenvalue cut-off: solver.py:12-21 takes it from the dtype of the
@@ -155,8 +203,74 @@ class QNGD:
                 # parameters keeps the real part: zero (sr.py:98-100, 111)
                 return torch.zeros(np_, dtype=torch.float64, device=A.device)
             h = ns // 2
-            b = torch.cat([-b[h:], b[:h]])  # [-Im; Re] (sr.py:105)
+            b = torch.cat([-b[h:], b[:h]]).contiguous()  # [-Im; Re] (sr.py:105)
         sv = self._solver
+        if sv.kind == "sgd":
+            return self._rmatvec(A, b) / b.shape[0]
+        if sv.kind == "shift_cg":
+            return self._shift_cg(A, b, sv)
+        if sv.blocks is not None:
+            # layer by layer, Ebar / nlayers (solver.py:251-257)
+            parts, c0 = [], 0
+            sub = Solver(sv.kind, sv.branch, sv.rshift, sv.ashift, sv.rtol, sv.atol, sv.tol_snr, sv.precision)
+            for n_i in sv.blocks:
+                blk = torch.zeros((ns, _round8(n_i)), dtype=torch.float32, device=A.device)
+                blk[:, :n_i].copy_(A[:, c0:c0 + n_i])  # 16-byte aligned rows for the tensor-core Gram
+                parts.append(self._solve_matrix(blk[:, :n_i], b / len(sv.blocks), sub))
+                c0 += n_i
+            return torch.cat(parts)
+        return self._solve_matrix(A, b, sv)
+
+    def _rmatvec(self, A: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+        """A^T b (FP64) by qgx_obar_rmatvec."""
+        import ctypes as C
+        rows, cols = A.shape
+        nb = C.c_int64(0)
+        _lib.call("qgx_obar_rmatvec_workspace_bytes", rows, cols, C.byref(nb))
+        ws = self._state.workspace("rmatvec", nb.value)
+        y = torch.empty(cols, dtype=torch.float64, device=A.device)
+        _lib.call("qgx_obar_rmatvec", _lib.ptr(A), rows, cols, A.stride(0), _lib.ptr(b), _lib.ptr(y), _lib.ptr(ws),
+                  ws.numel(), _lib.stream_ptr())
+        return y
+
+    def _matvec(self, A: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+        rows, cols = A.shape
+        x = x.contiguous()
+        y = torch.empty(rows, dtype=torch.float64, device=A.device)
+        _lib.call("qgx_obar_matvec", _lib.ptr(A), rows, cols, A.stride(0), _lib.ptr(x), _lib.ptr(y),
+                  _lib.stream_ptr())
+        return y
+
+    def _shift_cg(self, A: torch.Tensor, b: torch.Tensor, sv: Solver) -> torch.Tensor:
+        """lstsq_shift_cg (solver.py:24-47): CG on (S + diag_shift diag(S)) x = A^T b, the Obar
+        passes on the device; stops when |r| <= max(rtol |F|, atol) or after maxiter (10 Np)."""
+        rows, cols = A.shape
+        F = self._rmatvec(A, b)
+        d = torch.empty(cols, dtype=torch.float64, device=A.device)
+        ws = self._state.workspace("sumsq", int(_lib.lib().qgx_column_sumsq_workspace_bytes(rows, cols)))
+        _lib.call("qgx_column_sumsq", _lib.ptr(A), rows, cols, A.stride(0), _lib.ptr(d), _lib.ptr(ws), ws.numel(),
+                  _lib.stream_ptr())
+        d *= sv.diag_shift
+        x = torch.zeros_like(F)
+        r = F.clone()
+        p = r.clone()
+        rs = float(r @ r)
+        tol2 = max(sv.rtol * float(torch.linalg.vector_norm(F)), sv.atol) ** 2
+        for _ in range(10 * cols if sv.maxiter is None else int(sv.maxiter)):
+            if rs <= tol2:
+                break
+            Ap = self._rmatvec(A, self._matvec(A, p)) + d * p
+            alpha = rs / float(p @ Ap)
+            x += alpha * p
+            r -= alpha * Ap
+            rs_new = float(r @ r)
+            p = r + (rs_new / rs) * p
+            rs = rs_new
+        return x
+
+    def _solve_matrix(self, A: torch.Tensor, b: torch.Tensor, sv: Solver) -> torch.Tensor:
+        """The pinv / shift solvers on the real matrix A and right-hand side b."""
+        ns, np_ = A.shape
         method = _lib.SOLVE_SHIFT if sv.kind == "shift" else _lib.SOLVE_PINV
         rshift = _OBAR_RTOL if sv.rshift is None else sv.rshift
         rtol = _OBAR_RTOL if sv.rtol is None else sv.rtol

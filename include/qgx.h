@@ -320,6 +320,22 @@ int qgx_obar_matvec(const float* A, int64_t rows, int64_t cols, int64_t lda, con
 int qgx_scale_columns(float* A, int64_t rows, int64_t cols, int64_t lda, const double* s,
                       qgx_stream_t stream);
 
+/* ---- exact reconfiguration (ER, quantax/optimizer/sr.py:432-513) over a whole basis ---- */
+/* y = H x for a CSR matrix (nrows x nrows; rowptr nrows + 1 int64, col int32, val FP64):
+ * nvec = 1 for real x, y (nrows doubles), 2 for complex ones as (re, im) pairs. Replaces the
+ * QuSpin product `hamiltonian @ DenseState` of ER.get_Ebar (sr.py:488-495). */
+int qgx_csr_matvec(const int64_t* rowptr, const int32_t* col, const double* val, int64_t nrows,
+                   const double* x, int nvec, double* y, qgx_stream_t stream);
+/* Omat = psi_s O_s in place, a NaN product set to 0 (ER.get_Obar, sr.py:497-505). cplx = 0:
+ * O (ns x cols, row stride ldo floats), psi ns doubles; cplx = 1: O holds [Re O; Im O]
+ * (2 ns rows), psi ns (re, im) pairs. */
+int qgx_er_weight_rows(float* O, int64_t ns, int64_t cols, int64_t ldo, const double* psi, int cplx,
+                       qgx_stream_t stream);
+/* Obar = Omat - psi Omean^T in place, Omean = psi^H Omat (cols doubles, or cols real parts then
+ * cols imaginary parts when cplx = 1). */
+int qgx_er_center(float* O, int64_t ns, int64_t cols, int64_t ldo, const double* psi, int cplx,
+                  const double* omean, qgx_stream_t stream);
+
 /* ---- Gram matrices (quantax/optimizer/solver.py:139, 157) ---------------------------- */
 /* T = A A^T for A (rows x k, row stride lda floats), written as FP64 rows x rows
  * (full symmetric matrix, row stride ldt). mode = QGX_GRAM_*. */

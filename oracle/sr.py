@@ -197,3 +197,20 @@ def minsr_pinv(T, b, rtol=None, atol=0.0):
     """minsr_pinv_eig (solver.py:262-294) without the SNR truncation."""
     lam, U = np.linalg.eigh(T)
     return U @ (eigs_inv(lam, rtol, atol) * (U.conj().T @ b))
+
+
+def er_terms(log_psi, O, H):
+    """ER.get_Ebar / get_Obar (quantax/optimizer/sr.py:485-505) over a whole basis: psi =
+    exp(log psi) normalised, energy = <psi|H|psi>, Ebar = H psi - energy psi, Omat = psi O with
+    NaN entries set to 0, Omean = psi^H Omat, Obar = Omat - psi Omean^T. H is any matrix with
+    H @ vector (dense or scipy sparse). Returns (energy, Ebar, Obar, Omean)."""
+    lp = np.asarray(log_psi)
+    psi = np.exp(lp - lp.real.max())
+    psi = psi / np.linalg.norm(psi)
+    Hpsi = H @ psi
+    energy = np.vdot(psi, Hpsi)
+    Ebar = Hpsi - psi * energy
+    Omat = np.asarray(O) * psi[:, None]
+    Omat = np.where(np.isnan(Omat), 0, Omat)
+    Omean = psi.conj() @ Omat
+    return energy.real, Ebar, Omat - np.outer(psi, Omean), Omean

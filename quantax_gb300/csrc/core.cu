@@ -334,6 +334,81 @@ __global__ void scale_columns_kernel(float* __restrict__ A, int64_t rows, int64_
     A[row * lda + j] = (float)((double)A[row * lda + j] * s[j]);
 }
 
+// ---- exact reconfiguration over a whole basis (sr.py:432-513) ---------------------------
+// y[r][c] = sum over row r's entries e of val[e] x[col[e]][c], c < nvec (1: real vectors,
+// 2: complex ones as (re, im) pairs). One warp per row, FP64; a column index outside
+// [0, nrows) is skipped.
+__global__ void csr_matvec_kernel(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                  const double* __restrict__ val, int64_t nrows, const double* __restrict__ x,
+                                  int nvec, double* __restrict__ y) {
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= nrows) return;  // whole warps: 256-thread blocks hold 8 rows
+  double s0 = 0.0, s1 = 0.0;
+  const int64_t e1 = rowptr[row + 1];
+  for (int64_t e = rowptr[row] + lane; e < e1; e += 32) {
+    const int64_t c = col[e];
+    if (c < 0 || c >= nrows) continue;
+    s0 = fma(val[e], x[c * nvec], s0);
+    if (nvec == 2) s1 = fma(val[e], x[c * 2 + 1], s1);
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  if (lane == 0) {
+    y[row * nvec] = s0;
+    if (nvec == 2) y[row * 2 + 1] = s1;
+  }
+}
+
+// Omat = psi_s O_s in place (variational.py jacobian times psi, sr.py:500-501). Real psi:
+// O (ns x cols). Complex psi ((re, im) pairs): O holds [Re O; Im O] (2 ns rows). A NaN
+// product becomes 0, both parts of a complex one, as jnp.where(isnan(Omat), 0, Omat) does.
+__global__ void er_weight_rows_kernel(float* __restrict__ O, int64_t ns, int64_t cols, int64_t ldo,
+                                      const double* __restrict__ psi, int cplx) {
+  for (int64_t row = blockIdx.y; row < ns; row += gridDim.y) {
+    float* a = O + row * ldo;
+    if (!cplx) {
+      const double p = psi[row];
+      for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cols; j += (int64_t)gridDim.x * blockDim.x) {
+        const double v = (double)a[j] * p;
+        a[j] = isnan(v) ? 0.f : (float)v;
+      }
+    } else {
+      float* b = O + (row + ns) * ldo;
+      const double pr = psi[2 * row], pi = psi[2 * row + 1];
+      for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cols; j += (int64_t)gridDim.x * blockDim.x) {
+        const double re = (double)a[j] * pr - (double)b[j] * pi;
+        const double im = (double)a[j] * pi + (double)b[j] * pr;
+        const bool bad = isnan(re) || isnan(im);
+        a[j] = bad ? 0.f : (float)re;
+        b[j] = bad ? 0.f : (float)im;
+      }
+    }
+  }
+}
+
+// Obar = Omat - psi Omean^T in place (sr.py:503-504); complex: Omean as cols real parts then
+// cols imaginary parts, the product psi_s Omean_k complex.
+__global__ void er_center_kernel(float* __restrict__ O, int64_t ns, int64_t cols, int64_t ldo,
+                                 const double* __restrict__ psi, int cplx, const double* __restrict__ omean) {
+  for (int64_t row = blockIdx.y; row < ns; row += gridDim.y) {
+    float* a = O + row * ldo;
+    if (!cplx) {
+      const double p = psi[row];
+      for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cols; j += (int64_t)gridDim.x * blockDim.x)
+        a[j] = (float)((double)a[j] - p * omean[j]);
+    } else {
+      float* b = O + (row + ns) * ldo;
+      const double pr = psi[2 * row], pi = psi[2 * row + 1];
+      for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < cols; j += (int64_t)gridDim.x * blockDim.x) {
+        const double mr = omean[j], mi = omean[cols + j];
+        a[j] = (float)((double)a[j] - (pr * mr - pi * mi));
+        b[j] = (float)((double)b[j] - (pr * mi + pi * mr));
+      }
+    }
+  }
+}
+
 }  // namespace qgx
 
 using namespace qgx;
@@ -359,6 +434,37 @@ int qgx_scale_columns(float* A, int64_t rows, int64_t cols, int64_t lda, const d
     const int64_t rr = std::min<int64_t>(65535, rows - r0);
     scale_columns_kernel<<<dim3(gx, (unsigned)rr), 256, 0, st>>>(A + r0 * lda, rr, cols, lda, s);
   }
+  return launch_status();
+}
+
+int qgx_csr_matvec(const int64_t* rowptr, const int32_t* col, const double* val, int64_t nrows, const double* x,
+                   int nvec, double* y, qgx_stream_t stream) {
+  QGX_CHECK_ARG(nrows >= 0 && (nvec == 1 || nvec == 2));
+  if (nrows == 0) return QGX_OK;
+  QGX_CHECK_ARG(rowptr && col && val && x && y);
+  csr_matvec_kernel<<<blocks_for(nrows * 32, 256), 256, 0, as_cuda(stream)>>>(rowptr, col, val, nrows, x, nvec, y);
+  return launch_status();
+}
+
+static dim3 er_grid(int64_t ns, int64_t cols) {
+  return dim3((unsigned)std::min<int64_t>((cols + 255) / 256, 64), (unsigned)std::min<int64_t>(ns, 65535));
+}
+
+int qgx_er_weight_rows(float* O, int64_t ns, int64_t cols, int64_t ldo, const double* psi, int cplx,
+                       qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns >= 0 && cols >= 0 && ldo >= cols);
+  if (ns == 0 || cols == 0) return QGX_OK;
+  QGX_CHECK_ARG(O && psi);
+  er_weight_rows_kernel<<<er_grid(ns, cols), 256, 0, as_cuda(stream)>>>(O, ns, cols, ldo, psi, cplx != 0);
+  return launch_status();
+}
+
+int qgx_er_center(float* O, int64_t ns, int64_t cols, int64_t ldo, const double* psi, int cplx,
+                  const double* omean, qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns >= 0 && cols >= 0 && ldo >= cols);
+  if (ns == 0 || cols == 0) return QGX_OK;
+  QGX_CHECK_ARG(O && psi && omean);
+  er_center_kernel<<<er_grid(ns, cols), 256, 0, as_cuda(stream)>>>(O, ns, cols, ldo, psi, cplx != 0, omean);
   return launch_status();
 }
 

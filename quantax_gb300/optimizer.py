@@ -515,6 +515,121 @@ class AdamSR(_MomentumSR):
         return step / V + m
 
 
+class ER(QNGD):
+    """Exact reconfiguration (sr.py:432-513): Obar theta_dot = Ebar summed over a whole basis
+    instead of samples, for small systems.
+
+    The basis is the computational one of the sites' fixed-magnetisation sector (all 2^N
+    configurations without Nparticles). The reference sums over the representatives of its
+    symmetry's QuSpin basis with psi(rep) / norm(rep) as coefficients. A state projected on
+    that symmetry lies in the span of the symmetric vectors, onto which the representatives'
+    orthonormal vectors map isometrically, so Ebar, Obar^H Obar, Obar^H Ebar and the step are
+    the same in either basis; the full basis costs |G| times more forwards.
+
+    On the device: psi by the model's forward over the basis, H psi as a CSR product
+    (qgx_csr_matvec), Omat = psi O by qgx_er_weight_rows after the jacobian kernel, Omean =
+    psi^H Omat by qgx_obar_rmatvec, Obar = Omat - psi Omean^T by qgx_er_center, then the
+    SR / MinSR solve. The Gram defaults to the FP64-class mode: an exact step has no sampling
+    noise to hide FP32 Gram rounding behind."""
+
+    def __init__(self, state, hamiltonian, imag_time: bool = True, solver: Optional[Solver] = None, symm=None,
+                 gram: str = "fp64"):
+        import numpy as np
+        from .global_defs import get_sites
+        from .state import pack_spins
+        super().__init__(state, imag_time, solver, gram)
+        if symm is not None and symm is not state.symm and not (symm.is_identity and state.symm.is_identity):
+            raise NotImplementedError("ER sums over the sector of the state's own symmetry: pass symm=None")
+        self._hamiltonian = hamiltonian
+        self._energy = None
+        sites = get_sites()
+        nup = sites.Nparticles[0] if isinstance(sites.Nparticles, tuple) else None
+        H, states = hamiltonian.to_sparse(nup, return_states=True)
+        H = H.tocsr()
+        H.sort_indices()
+        n = state.Nmodes
+        spins = (((states[:, None] >> np.arange(n)) & 1) * 2 - 1).astype(np.int8)
+        dev = state.params.device
+        self._spins = spins
+        self._packed = pack_spins(spins, n)
+        self._rowptr = torch.as_tensor(H.indptr.astype(np.int64), device=dev)
+        self._col = torch.as_tensor(H.indices.astype(np.int32), device=dev)
+        self._val = torch.as_tensor(H.data.astype(np.float64), device=dev)
+        self._dim = len(states)
+
+    @property
+    def hamiltonian(self):
+        return self._hamiltonian
+
+    @property
+    def energy(self) -> Optional[float]:
+        return self._energy
+
+    @property
+    def basis_spins(self):
+        """The basis configurations (dim x N, +-1 int8, numpy)."""
+        return self._spins
+
+    def psi(self) -> torch.Tensor:
+        """The normalised amplitudes over the basis (float64, complex128 for complex output)."""
+        lp = self._state.log_psi_packed(self._packed)
+        lp = lp.to(torch.complex128 if lp.is_complex() else torch.float64)
+        psi = torch.exp(lp - lp.real.max())  # the normalisation below removes the shift
+        if psi.is_complex() and not self._state.is_complex:
+            psi = psi.real  # a signed real state: phase 0 or pi
+        return psi / torch.linalg.vector_norm(psi)
+
+    @staticmethod
+    def _pairs(psi: torch.Tensor) -> torch.Tensor:
+        return (torch.view_as_real(psi) if psi.is_complex() else psi).contiguous()
+
+    def get_Ebar(self, psi: torch.Tensor) -> torch.Tensor:
+        """Ebar = H psi - <psi|H|psi> psi (sr.py:488-495); [Re; Im] stacked for complex output,
+        the layout solve() takes."""
+        x = self._pairs(psi)
+        y = torch.empty_like(x)
+        _lib.call("qgx_csr_matvec", _lib.ptr(self._rowptr), _lib.ptr(self._col), _lib.ptr(self._val), self._dim,
+                  _lib.ptr(x), 2 if psi.is_complex() else 1, _lib.ptr(y), _lib.stream_ptr())
+        Hpsi = torch.view_as_complex(y) if psi.is_complex() else y
+        energy = torch.vdot(psi, Hpsi)
+        self._energy = float(energy.real)
+        ebar = Hpsi - psi * energy
+        return torch.cat([ebar.real, ebar.imag]).contiguous() if ebar.is_complex() else ebar
+
+    def get_Obar(self, psi: torch.Tensor) -> torch.Tensor:
+        """Obar = psi O - psi Omean^T with Omean = psi^H (psi O) (sr.py:497-505): FP32 rows,
+        [Re; Im] stacked for complex output, padded to 16-byte strides for the Gram."""
+        st = self._state
+        np_ = st.nparams
+        rows = st.obar_rows(self._dim)
+        out = self._buffer("obar", (rows, _round8(np_)), torch.float32)
+        O = out[:, :np_]
+        st.jacobian_rows(self._packed, O)
+        cplx = psi.is_complex()
+        x = self._pairs(psi)
+        s = _lib.stream_ptr()
+        _lib.call("qgx_er_weight_rows", _lib.ptr(O), self._dim, np_, O.stride(0), _lib.ptr(x), int(cplx), s)
+        if cplx:
+            # Omean = sum conj(psi) Omat: Re = Re psi . Re Omat + Im psi . Im Omat,
+            # Im = Re psi . Im Omat - Im psi . Re Omat, as A^T b over the stacked rows
+            b_re = torch.cat([psi.real, psi.imag]).contiguous()
+            b_im = torch.cat([-psi.imag, psi.real]).contiguous()
+            m = torch.stack([self._rmatvec(O, b_re), self._rmatvec(O, b_im)]).contiguous()
+            self._Omean = torch.complex(m[0], m[1])
+        else:
+            m = self._rmatvec(O, x)
+            self._Omean = m
+        _lib.call("qgx_er_center", _lib.ptr(O), self._dim, np_, O.stride(0), _lib.ptr(x), int(cplx), _lib.ptr(m), s)
+        return O
+
+    def get_step(self, samples=None) -> torch.Tensor:
+        """The exact step; `samples` is accepted for the drivers' calling convention and unused."""
+        psi = self.psi()
+        Ebar = self.get_Ebar(psi)
+        Obar = self.get_Obar(psi)
+        return self.solve(Obar, Ebar)
+
+
 def pinvh_solve(rtol: Optional[float] = None, atol: float = 0.0) -> Solver:
     """solver.py:104-111: S x = F by eigh with the soft inverse (TimeEvol's default)."""
     return Solver("pinv", "lstsq", rtol=rtol, atol=atol)
@@ -598,3 +713,95 @@ class TimeEvol(SR):
 
 
 MinSR = SR
+
+
+# ---- time-stepping drivers (optimizer/driver.py) ---------------------------------------------
+class Driver:
+    """A sampler and an optimizer stepped with a step length; energy and VarE traced against
+    the accumulated time (driver.py:9-27)."""
+
+    def __init__(self, state, sampler, optimizer, step_length: float):
+        from .utils import DataTracer
+        self._state = state
+        self._sampler = sampler
+        self._optimizer = optimizer
+        self._step_length = step_length
+        self._time = 0.0
+        self.energy = DataTracer()
+        self.VarE = DataTracer()
+
+    @property
+    def time(self) -> float:
+        return self._time
+
+    @property
+    def step_length(self) -> float:
+        return self._step_length
+
+    def step(self) -> None:
+        """One iteration."""
+
+
+class Euler(Driver):
+    """First-order Euler driver (driver.py:30-39): theta -= dt * step(samples)."""
+
+    def step(self) -> None:
+        samples = self._sampler.sweep()
+        step = self._optimizer.get_step(samples)
+        self._state.update(self._step_length * step)
+        self._time += self._step_length
+        self.energy.append(self._optimizer.energy, self._time)
+        self.VarE.append(self._optimizer.VarE, self._time)
+
+
+class AdaptiveHeunEvolution(Driver):
+    """Adaptive second-order Heun driver for unitary evolution (driver.py:42-104).
+
+    Per call: a full Euler step and two half steps from the same start, five sweeps and
+    TimeEvol solves; the error estimate sqrt(d^T S d) dt of the two results' difference d
+    against the last S scales the next step length by (threshold / error)^(1/3), clipped to
+    [0.2, 2] and the length to [1e-4, 1e-2]. As in the reference, the time advances by the new
+    step length, and the state keeps the two-half-step result. The reference also forms the
+    global-phase rates 1j E - Omean . step, used only by lines it leaves commented out; they are
+    not computed here."""
+
+    def __init__(self, state, sampler, tdvp, step_length: float = 1e-3, integ_threshold: float = 1e-3):
+        from .utils import DataTracer
+        super().__init__(state, sampler, tdvp, step_length)
+        self._integ_threshold = integ_threshold
+        self.step_size = DataTracer()
+
+    def step(self) -> None:
+        import numpy as np
+        tdvp = self._optimizer
+        st = self._state
+        dt = self._step_length
+
+        stepi = tdvp.get_step(self._sampler.sweep())
+        st.update(dt * stepi)
+        stepf = tdvp.get_step(self._sampler.sweep())
+        step1 = (stepi + stepf) / 2
+        st.update(-dt / 2 * stepi)
+
+        stepm = tdvp.get_step(self._sampler.sweep())
+        st.update(dt / 4 * (stepm - stepi))
+        stepmm = tdvp.get_step(self._sampler.sweep())
+        st.update(dt / 2 * stepmm)
+
+        Smat, Fvec = tdvp.get_SF(self._sampler.sweep())
+        stepff = tdvp.solve(Smat, Fvec)
+        st.update(dt / 4 * (stepff - stepmm))
+        step2 = (stepi + stepm + stepmm + stepff) / 4
+
+        diff = (step1 - step2).to(Smat.dtype)
+        err = float(torch.dot(diff, Smat @ diff)) if diff.numel() else 0.0
+        with np.errstate(divide="ignore", invalid="ignore"):
+            new_err = np.sqrt(np.float64(err)) * dt
+            ratio = np.clip((np.float64(self._integ_threshold) / new_err) ** (1 / 3), 0.2, 2)
+        new_step_length = float(np.clip(dt * ratio, 1e-4, 1e-2))
+        self._time += new_step_length
+        self._step_length = new_step_length
+
+        self.step_size.append(new_step_length, self._time)
+        self.energy.append(tdvp.energy, self._time)
+        self.VarE.append(tdvp.VarE, self._time)

@@ -190,16 +190,21 @@ class Variational:
         (variational.py:497-511)."""
         packed = s if isinstance(s, torch.Tensor) and s.dtype == torch.int32 else pack_spins(s, self.Nmodes)
         ns = packed.shape[0]
+        out = self.jacobian_rows(packed, torch.empty((self.obar_rows(ns), self.nparams), dtype=torch.float32,
+                                                     device=self._dev))
+        return torch.complex(out[:ns], out[ns:]) if self.is_complex else out
+
+    def jacobian_rows(self, packed: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+        """O of packed configurations written into out (obar_rows(ns) x nparams float32, any row
+        stride): the rows [Re O; Im O] for complex output."""
+        ns = packed.shape[0]
         if self._model.kind == "rbm":
-            out = torch.empty((ns, self.nparams), dtype=torch.float32, device=self._dev)
             self._model.jacobian(self._table, packed, out)
             return out
-        rows = 2 * ns if self.is_complex else ns
-        out = torch.empty((rows, self.nparams), dtype=torch.float32, device=self._dev)
         ws = self.workspace("jac", self._model.jacobian_workspace_bytes(ns, self._sym))
-        self._model.jacobian(self._table, packed, out[:ns], out[ns:] if self.is_complex else None, self.nparams, ws,
+        self._model.jacobian(self._table, packed, out[:ns], out[ns:] if self.is_complex else None, out.stride(0), ws,
                              self._sym)
-        return torch.complex(out[:ns], out[ns:]) if self.is_complex else out
+        return out
 
     def obar_rows(self, ns: int) -> int:
         """Rows of the matrix QNGD.solve works on: 2 ns ([Re; Im]) for complex output."""

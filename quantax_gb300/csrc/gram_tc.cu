@@ -5,7 +5,8 @@
 //                    column block, 128B-swizzled, into a ring of kStages shared-memory stages;
 //   warp 5 / lane 0  MMA issuer: tcgen05.mma M=128 N=128 (K = 8 for tf32, 16 for bf16; four
 //                    per 128-byte k-block); tcgen05.commit frees a stage when its MMAs are done;
-//   warps 6-9        (split tf32 only) split the staged operands into hi and lo parts;
+//   warps 6-9        (split tf32 only) write the low parts lo = x - tf32(x) of the staged
+//                    operands beside them;
 //   warps 0-3        epilogue (warp w owns TMEM lanes 32w..32w+31, i.e. tile rows).
 // K is accumulated in chunks of kChunkElems elements, alternately in two 128-column TMEM
 // accumulators, each chunk starting from zero. The epilogue adds every finished chunk into
@@ -77,6 +78,10 @@ __device__ inline void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc
         "l"(a), "l"(b), "r"(instr_desc<KIND>()), "r"(accumulate));
   }
 }
+
+// the TF32 value the tensor core takes from an FP32 operand: the 10 leading explicit mantissa
+// bits, the 13 below them ignored
+__device__ inline float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
 __device__ inline void record_status(int32_t* status, int code) {
   if (status) atomicExch(status, code);
@@ -191,8 +196,9 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
       }
     }
   } else if (KIND == 2 && warp >= 6) {
-    // split x = hi + lo: hi keeps the 10 explicit mantissa bits the tensor core reads
-    // (written in place), lo = x - hi exactly (second buffer, same swizzled layout)
+    // split x = hi + lo: the tensor core reads an FP32 operand as TF32 by ignoring its 13
+    // low mantissa bits, so the staged x itself is hi; lo = x - hi is exact and goes to a
+    // second buffer in the same swizzled layout (the tensor core reads lo truncated too)
     const int t = threadIdx.x - 192;
     for (int64_t kb = 0; kb < nkb && !*fail; ++kb) {
       const int s = (int)(kb % kStages);
@@ -201,18 +207,12 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
         *fail = 1;
         break;
       }
-      float4* x = reinterpret_cast<float4*>(smem + s * kStageBytes);
+      const float4* x = reinterpret_cast<const float4*>(smem + s * kStageBytes);
       float4* lo = reinterpret_cast<float4*>(smem + s * kStageBytes + 2 * kBlockBytes);
 #pragma unroll 4
       for (int e = t; e < 2 * kBlockBytes / 16; e += 128) {
-        float4 v = x[e];
-        float4 h;
-        h.x = __uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u);
-        h.y = __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u);
-        h.z = __uint_as_float(__float_as_uint(v.z) & 0xFFFFE000u);
-        h.w = __uint_as_float(__float_as_uint(v.w) & 0xFFFFE000u);
-        x[e] = h;
-        lo[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        const float4 v = x[e];
+        lo[e] = make_float4(v.x - tf32_hi(v.x), v.y - tf32_hi(v.y), v.z - tf32_hi(v.z), v.w - tf32_hi(v.w));
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&split[s])) : "memory");

@@ -111,3 +111,44 @@ def test_sr_gram_through_transpose(cuda, mode):
     d = np.sqrt(np.diag(ref))
     err = np.abs(S.cpu().numpy() - ref) / np.outer(d, d)
     assert err.max() < tol({"tf32": 0, "bf16": 1, "3xtf32": 2}[mode], ns), err.max()
+
+
+def _tf32(a, round_half=False):
+    """The TF32 value of FP32 entries: truncated (13 low mantissa bits cleared) or, with
+    round_half, rounded half away from zero on the 13th bit."""
+    bits = np.asarray(a, dtype=np.float32).view(np.uint32)
+    if round_half:
+        bits = bits + np.uint32(0x1000)
+    return (bits & np.uint32(0xFFFFE000)).view(np.float32)
+
+
+def test_tf32_operands_are_truncated(cuda):
+    """The split-TF32 Gram uses the staged FP32 operand itself as its high part, relying on the
+    tensor core reading an FP32 operand as TF32 by ignoring its 13 low mantissa bits. A TF32
+    Gram of raw operands and one of operands truncated on the host agree bit for bit, while
+    operands rounded on the host give a different result (the check has teeth)."""
+    A = np.random.default_rng(21).normal(size=(256, 512)).astype(np.float32)
+    T_raw = tc_gram(A, 0)
+    assert np.array_equal(T_raw, tc_gram(_tf32(A), 0))
+    assert not np.array_equal(T_raw, tc_gram(_tf32(A, round_half=True), 0))
+
+
+@pytest.mark.parametrize("shape", [(256, 512), (300, 1000)])
+def test_split_tf32_gram_is_its_three_products(cuda, shape):
+    """3xtf32 computes hi hi^T + hi lo^T + lo hi^T with hi = tf32(x) and lo = tf32(x - hi), the
+    values the tensor core reads. Against that sum in FP64, only the FP32 accumulation of
+    256-element chunks remains, stated in units of |a_r| |a_c|: 1e-6 off the diagonal (measured
+    below 1e-7) and the accumulation bound of the other tests on it, where the same-sign sums
+    lose up to an FP32 ulp per MMA (measured 5.5e-6 at k = 512). A wrong high part would show
+    TF32-size errors: 2^-11 / sqrt(k) = 2e-5 off the diagonal at k = 512, 2^-11 = 5e-4 on it."""
+    A = np.random.default_rng(shape[0]).normal(size=shape).astype(np.float32)
+    hi = _tf32(A)
+    lo = _tf32(A - hi)
+    h, l = hi.astype(np.float64), lo.astype(np.float64)
+    ref = h @ h.T + h @ l.T + l @ h.T
+    T = tc_gram(A, 2)
+    d = np.linalg.norm(A.astype(np.float64), axis=1)
+    err = np.abs(T - ref) / np.outer(d, d)
+    off = ~np.eye(shape[0], dtype=bool)
+    assert err[off].max() < 1e-6, err[off].max()
+    assert np.diag(err).max() < tol(2, shape[1]), np.diag(err).max()

@@ -320,6 +320,14 @@ int qgx_obar_matvec(const float* A, int64_t rows, int64_t cols, int64_t lda, con
 int qgx_scale_columns(float* A, int64_t rows, int64_t cols, int64_t lda, const double* s,
                       qgx_stream_t stream);
 
+/* ---- exact sampling (ExactSampler, quantax/sampler/sampler.py:72-119) ------------------ */
+/* idx[i] (i < ns) = the first j with cdf[j] > u_i cdf[dim - 1], cdf the inclusive prefix sums
+ * of the probabilities of a basis (dim doubles, cdf[dim - 1] > 0), u_i in [0, 1) the 53-bit
+ * uniform of Philox draw (seed, counter (i, step, tag 4)). Replaces jr.choice(..., p=prob) of
+ * ExactSampler.sweep (sampler.py:108-110). */
+int qgx_exact_draw(const double* cdf, int64_t dim, int64_t ns, uint64_t seed, uint64_t step,
+                   int64_t* idx, qgx_stream_t stream);
+
 /* ---- exact reconfiguration (ER, quantax/optimizer/sr.py:432-513) over a whole basis ---- */
 /* y = H x for a CSR matrix (nrows x nrows; rowptr nrows + 1 int64, col int32, val FP64):
  * nvec = 1 for real x, y (nrows doubles), 2 for complex ones as (re, im) pairs. Replaces the

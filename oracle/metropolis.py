@@ -115,3 +115,13 @@ def init_fixed_up(ns, n, nup, seed):
         out[chains, i] = out[chains, j]
         out[chains, j] = a
     return out
+
+
+def exact_draws(cdf, ns, seed, step):
+    """ExactSampler's draw (quantax/sampler/sampler.py:102-110, jr.choice with p = |psi|^n) on
+    the shared Philox stream: sample i of sweep `step` is the first j with cdf[j] > u cdf[-1],
+    u the 53-bit uniform of draw (seed, i, step, TAG_EXACT); cdf the inclusive prefix sums."""
+    w = philox.draw(seed, np.arange(ns), step, philox.TAG_EXACT)
+    u = philox.unit_double(w[:, 0], w[:, 1])
+    cdf = np.asarray(cdf, dtype=np.float64)
+    return np.searchsorted(cdf, u * cdf[-1], side="right")

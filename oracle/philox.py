@@ -32,6 +32,7 @@ MASK32 = np.uint64(0xFFFFFFFF)
 TAG_PROPOSE = 1      # Metropolis proposal + accept draw
 TAG_INIT = 2         # initial configurations
 TAG_INIT_PERM = 3    # fixed-magnetisation initial configurations
+TAG_EXACT = 4        # draws of the exact sampler
 
 
 def philox4x32_10(ctr, key):
@@ -97,3 +98,10 @@ def bounded(word, n):
 def unit_float(word):
     """Uniform float in [0, 1) with 24 random bits: (w >> 8) * 2**-24 (exact in fp32)."""
     return (np.asarray(word, dtype=np.uint32) >> np.uint32(8)).astype(np.float64) * (2.0 ** -24)
+
+
+def unit_double(x, y):
+    """Uniform float64 in [0, 1) with 53 random bits: ((x >> 5) 2**26 + (y >> 6)) 2**-53."""
+    x = np.asarray(x, dtype=np.uint32) >> np.uint32(5)
+    y = np.asarray(y, dtype=np.uint32) >> np.uint32(6)
+    return (x.astype(np.float64) * 67108864.0 + y.astype(np.float64)) * (2.0 ** -53)

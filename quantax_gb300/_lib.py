@@ -105,6 +105,7 @@ SIGNATURES = {
     "qgx_transpose": (C.c_int, [vp, i64, i64, i64, vp, i64, i32, vp]),
     "qgx_obar_matvec": (C.c_int, [vp, i64, i64, i64, vp, vp, vp]),
     "qgx_scale_columns": (C.c_int, [vp, i64, i64, i64, vp, vp]),
+    "qgx_exact_draw": (C.c_int, [vp, i64, i64, u64, u64, vp, vp]),
     "qgx_csr_matvec": (C.c_int, [vp, vp, vp, i64, vp, i32, vp, vp]),
     "qgx_er_weight_rows": (C.c_int, [vp, i64, i64, i64, vp, i32, vp]),
     "qgx_er_center": (C.c_int, [vp, i64, i64, i64, vp, i32, vp, vp]),
@@ -149,7 +150,7 @@ KERNELS_PER_CALL = {
     "qgx_resconv_jacobian_symm": 4,
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
     "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1, "qgx_column_sumsq": 2,
-    "qgx_rbm_conv_jacobian": 1, "qgx_apply_update": 2, "qgx_csr_matvec": 1, "qgx_er_weight_rows": 1,
+    "qgx_rbm_conv_jacobian": 1, "qgx_apply_update": 2, "qgx_csr_matvec": 1, "qgx_er_weight_rows": 1, "qgx_exact_draw": 1,
     "qgx_er_center": 1,
 }
 launch_count = 0

@@ -334,6 +334,27 @@ __global__ void scale_columns_kernel(float* __restrict__ A, int64_t rows, int64_
     A[row * lda + j] = (float)((double)A[row * lda + j] * s[j]);
 }
 
+// ---- exact sampling over a whole basis (sampler.py:72-119) --------------------------------
+// idx[i] = the first j with cdf[j] > u_i cdf[dim - 1], u_i the 53-bit uniform of draw
+// (seed, i, step, kTagExact): sample i of a sweep taken with probability p_j = cdf[j] - cdf[j-1]
+// (a j with p_j = 0 is never taken). cdf holds inclusive prefix sums.
+__global__ void exact_draw_kernel(const double* __restrict__ cdf, int64_t dim, int64_t ns, uint64_t seed,
+                                  uint64_t step, int64_t* __restrict__ idx) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  const u32x4 w = draw(seed, (uint64_t)i, step, kTagExact);
+  const double target = unit_double(w.x, w.y) * cdf[dim - 1];
+  int64_t lo = 0, hi = dim - 1;  // the answer lies in [lo, hi]: cdf[dim - 1] > target
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if (cdf[mid] > target)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  idx[i] = lo;
+}
+
 // ---- exact reconfiguration over a whole basis (sr.py:432-513) ---------------------------
 // y[r][c] = sum over row r's entries e of val[e] x[col[e]][c], c < nvec (1: real vectors,
 // 2: complex ones as (re, im) pairs). One warp per row, FP64; a column index outside
@@ -434,6 +455,15 @@ int qgx_scale_columns(float* A, int64_t rows, int64_t cols, int64_t lda, const d
     const int64_t rr = std::min<int64_t>(65535, rows - r0);
     scale_columns_kernel<<<dim3(gx, (unsigned)rr), 256, 0, st>>>(A + r0 * lda, rr, cols, lda, s);
   }
+  return launch_status();
+}
+
+int qgx_exact_draw(const double* cdf, int64_t dim, int64_t ns, uint64_t seed, uint64_t step, int64_t* idx,
+                   qgx_stream_t stream) {
+  QGX_CHECK_ARG(dim > 0 && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(cdf && idx);
+  exact_draw_kernel<<<blocks_for(ns, 256), 256, 0, as_cuda(stream)>>>(cdf, dim, ns, seed, step, idx);
   return launch_status();
 }
 

@@ -65,6 +65,7 @@ __host__ __device__ inline u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1
 constexpr uint32_t kTagPropose = 1;
 constexpr uint32_t kTagInit = 2;
 constexpr uint32_t kTagInitPerm = 3;
+constexpr uint32_t kTagExact = 4;  // draws of the exact sampler
 
 __host__ __device__ inline u32x4 draw(uint64_t seed, uint64_t chain, uint64_t step, uint32_t tag,
                                       uint32_t substream = 0) {
@@ -79,6 +80,11 @@ __host__ __device__ inline uint32_t bounded(uint32_t w, uint32_t n) {
 
 // (w >> 8) * 2^-24: uniform in [0, 1), exact in fp32
 __host__ __device__ inline float unit_float(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+
+// ((x >> 5) 2^26 + (y >> 6)) 2^-53: uniform in [0, 1) with 53 random bits, exact in fp64
+__host__ __device__ inline double unit_double(uint32_t x, uint32_t y) {
+  return ((double)(x >> 5) * 67108864.0 + (double)(y >> 6)) * (1.0 / 9007199254740992.0);
+}
 
 // ---- packed spins ----------------------------------------------------------------------
 __host__ __device__ inline int words_for(int n) { return (n + 31) >> 5; }

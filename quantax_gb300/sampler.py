@@ -1,6 +1,7 @@
-"""Metropolis samplers (quantax/sampler/metropolis.py:76-322, common_samplers.py:14-162).
+"""Samplers: Metropolis (quantax/sampler/metropolis.py:76-322, common_samplers.py:14-162) and
+the direct ones (quantax/sampler/sampler.py:14-145).
 
-Every chain lives in one warp of the sweep kernel; a sweep of n proposals is one
+Every Metropolis chain lives in one warp of the sweep kernel; a sweep of n proposals is one
 kernel launch. Draw t of chain c uses Philox4x32-10 counter (c, t, tag=1) under the
 sampler's 64-bit seed, and the sampler's step counter advances by n per sweep, so a
 run is reproducible from the global seed and independent of launch geometry.
@@ -49,16 +50,130 @@ class Samples:
         return cls(packed, lp, n)
 
 
-class Metropolis:
+def _reweight_factor(lp: torch.Tensor, reweight: float) -> Optional[torch.Tensor]:
+    """r = |psi|^(2 - n) / mean (sampler.py:66-69) from log psi (real or complex); None for n = 2."""
+    if reweight == 2.0:
+        return None
+    lp_real = (lp.real if lp.is_complex() else lp).to(torch.float32).contiguous()
+    r = torch.empty(lp_real.shape[0], dtype=torch.float64, device=lp_real.device)
+    _lib.call("qgx_reweight_factor", _lib.ptr(lp_real), lp_real.shape[0], float(reweight), _lib.ptr(r),
+              _lib.stream_ptr())
+    return r
+
+
+class Sampler:
+    """Base of the samplers (sampler.py:14-69): a state, samples per sweep and the reweight
+    factor n of the sampled probability |psi|^n."""
+
+    def __init__(self, state, nsamples: int, reweight: float = 2.0):
+        self._state = state
+        self._nsamples = int(nsamples)
+        self._reweight = float(reweight)
+
+    @property
+    def state(self):
+        return self._state
+
+    @property
+    def nsamples(self) -> int:
+        return self._nsamples
+
+    @property
+    def reweight(self) -> float:
+        return self._reweight
+
+    @property
+    def Nsites(self) -> int:
+        return self._state.Nsites
+
+    @property
+    def Nmodes(self) -> int:
+        return self._state.Nmodes
+
+    def sweep(self) -> "Samples":
+        raise NotImplementedError
+
+
+class RandomSampler(Sampler):
+    """Uniformly random configurations (sampler.py:122-145): the sites' fixed-magnetisation
+    sector when Nparticles is set, else all of them; reweight 0, so r = |psi|^2 / mean. Each
+    sweep takes a fresh seed from the global stream, as rand_states does."""
+
+    def __init__(self, state, nsamples: int):
+        super().__init__(state, nsamples, reweight=0.0)
+
+    def sweep(self) -> "Samples":
+        n = self.Nmodes
+        packed = torch.empty((self._nsamples, (n + 31) // 32), dtype=torch.int32, device=self._state.params.device)
+        nparticles = self._state.sites.Nparticles
+        if isinstance(nparticles, tuple):
+            _lib.call("qgx_spins_init_fixed_up", _lib.ptr(packed), self._nsamples, n, nparticles[0], get_subkeys(),
+                      _lib.stream_ptr())
+        else:
+            _lib.call("qgx_spins_init_uniform", _lib.ptr(packed), self._nsamples, n, get_subkeys(), _lib.stream_ptr())
+        lp = self._state.log_psi_packed(packed)
+        return Samples(packed, lp, n, _reweight_factor(lp, self._reweight))
+
+
+class ExactSampler(Sampler):
+    """Samples drawn directly from |psi|^n over the whole basis (sampler.py:72-119).
+
+    The basis is every configuration of the sites' fixed-magnetisation sector (all 2^N without
+    Nparticles); psi comes from the model's forward over it, once per sweep. The reference
+    draws representatives of its symmetry's reduced basis with probability |<r|psi>|^n and then
+    a uniform group image of each: for n = 2, or without a symmetry, that is the distribution
+    |psi(s)|^n drawn here; for n != 2 with a symmetry the reference's configurations carry an
+    extra factor |orbit|^(n/2 - 1) that its reweighting does not undo, and this sampler does
+    not reproduce it. Sample i of sweep t is the inverse-CDF image of the 53-bit uniform of
+    Philox draw (seed, i, t, tag 4) (qgx_exact_draw)."""
+
+    def __init__(self, state, nsamples: int, reweight: float = 2.0, symm=None):
+        from .utils import basis_states, states_to_spins
+        super().__init__(state, nsamples, reweight)
+        if symm is not None and symm is not state.symm and not (symm.is_identity and state.symm.is_identity):
+            raise NotImplementedError("ExactSampler sums over the sector of the state's own symmetry: pass symm=None")
+        n = self.Nmodes
+        nparticles = state.sites.Nparticles
+        self._states = basis_states(n, nparticles[0] if isinstance(nparticles, tuple) else None)
+        self._basis = pack_spins(states_to_spins(self._states, n), n)
+        self._seed = get_subkeys()
+        self._step = 0
+        self._last_cdf = None
+
+    @property
+    def basis_states(self) -> np.ndarray:
+        """Codes of the basis configurations (bit i set = site i up)."""
+        return self._states
+
+    def probabilities(self):
+        """(p, log psi): |psi|^n over the basis normalised to sum 1 (float64), and the log psi
+        values it came from."""
+        lp = self._state.log_psi_packed(self._basis)
+        x = self._reweight * (lp.real if lp.is_complex() else lp).to(torch.float64)
+        p = torch.exp(x - x[torch.isfinite(x)].max())
+        p = torch.where(torch.isfinite(p) & (p > 0), p, torch.zeros_like(p))
+        return p / p.sum(), lp
+
+    def sweep(self) -> "Samples":
+        p, lp = self.probabilities()
+        cdf = torch.cumsum(p, 0)
+        idx = torch.empty(self._nsamples, dtype=torch.int64, device=cdf.device)
+        _lib.call("qgx_exact_draw", _lib.ptr(cdf), cdf.shape[0], self._nsamples, self._seed, self._step, _lib.ptr(idx),
+                  _lib.stream_ptr())
+        self._step += 1
+        self._last_cdf = cdf
+        lp_s = lp.index_select(0, idx)
+        return Samples(self._basis.index_select(0, idx), lp_s, self.Nmodes, _reweight_factor(lp_s, self._reweight))
+
+
+class Metropolis(Sampler):
     """Metropolis-Hastings driver with one Markov chain per sample."""
 
     proposal = None
 
     def __init__(self, state, nsamples: int, reweight: float = 2.0, thermal_steps: Optional[int] = None,
                  sweep_steps: Optional[int] = None, initial_spins=None):
-        self._state = state
-        self._nsamples = int(nsamples)
-        self._reweight = float(reweight)
+        super().__init__(state, nsamples, reweight)
         n = state.Nmodes
         self._thermal_steps = 20 * n if thermal_steps is None else int(thermal_steps)
         self._sweep_steps = 2 * n if sweep_steps is None else int(sweep_steps)
@@ -78,22 +193,6 @@ class Metropolis:
 
     def _setup(self) -> None:
         pass
-
-    @property
-    def state(self):
-        return self._state
-
-    @property
-    def nsamples(self) -> int:
-        return self._nsamples
-
-    @property
-    def reweight(self) -> float:
-        return self._reweight
-
-    @property
-    def Nmodes(self) -> int:
-        return self._state.Nmodes
 
     @property
     def nflips(self) -> Optional[int]:

@@ -97,3 +97,22 @@ class DataTracer:
             plt.loglog(time, data)
         else:
             plt.plot(time, data)
+
+
+def basis_states(n: int, nup: Optional[int] = None) -> np.ndarray:
+    """Codes of the computational basis in ascending order (bit i set = site i up), all 2^n of
+    them or the fixed-magnetisation sector with nup up spins (n <= 30)."""
+    if n > 30:
+        raise ValueError("a full basis is limited to n <= 30 sites")
+    codes = np.arange(1 << n, dtype=np.int64)
+    if nup is None:
+        return codes
+    count = np.zeros_like(codes)
+    for i in range(n):
+        count += (codes >> i) & 1
+    return codes[count == nup]
+
+
+def states_to_spins(states: np.ndarray, n: int) -> np.ndarray:
+    """(len(states), n) int8 +-1 configurations of basis codes."""
+    return ((((np.asarray(states)[:, None] >> np.arange(n)) & 1) * 2) - 1).astype(np.int8)

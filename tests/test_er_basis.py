@@ -75,3 +75,33 @@ def test_er_step_lowers_the_energy_to_the_ground_state():
         e, eb, ob, _ = osr.er_terms(net.log_psi(s), net.jacobian(s), H)
         net.set_params(net.params() - 0.05 * osr.auto(ob, eb, "pinv", rtol=1e-6))
     assert abs(e - E0) <= 1e-5 * abs(E0)
+
+
+def test_exact_draws_follow_the_probabilities():
+    """The exact sampler's inverse-CDF draw on the shared Philox stream (oracle/metropolis.py,
+    restating jr.choice with p, quantax/sampler/sampler.py:108-110): zero-probability entries
+    are never drawn, counts agree with N p, and sweeps draw independently."""
+    from oracle import metropolis
+    p = np.array([0.0, 0.2, 0.0, 0.05, 0.75, 0.0])
+    cdf = np.cumsum(p)
+    a = metropolis.exact_draws(cdf, 1 << 16, 123, 0)
+    b = metropolis.exact_draws(cdf, 1 << 16, 123, 1)
+    assert not np.array_equal(a, b)
+    counts = np.bincount(np.concatenate([a, b]), minlength=6)
+    assert counts[p == 0].sum() == 0
+    expect = p * counts.sum()
+    ok = expect > 0
+    assert np.all(np.abs(counts[ok] - expect[ok]) <= 5 * np.sqrt(expect[ok]))
+    # unnormalised prefix sums give the same draws
+    np.testing.assert_array_equal(metropolis.exact_draws(3.0 * cdf, 1 << 16, 123, 0), a)
+
+
+def test_basis_helpers():
+    from math import comb
+    from quantax_gb300.utils import basis_states, states_to_spins
+    st = basis_states(10, 4)
+    assert len(st) == comb(10, 4) and np.all(np.diff(st) > 0)
+    s = states_to_spins(st, 10)
+    assert s.dtype == np.int8 and np.all((s == 1).sum(axis=1) == 4)
+    assert np.array_equal(((s > 0).astype(np.int64) << np.arange(10)).sum(axis=1), st)
+    assert len(basis_states(6)) == 64

@@ -5,7 +5,6 @@ from __future__ import annotations
 
 import warnings
 from enum import Enum
-from pathlib import Path
 from typing import Optional
 
 import numpy as np

@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .global_defs import PARTICLE_TYPE, device, get_default_dtype, get_lattice, get_sites, is_default_cpl
+from .global_defs import PARTICLE_TYPE, device, get_lattice, get_sites, is_default_cpl
 
 
 def _orbit_product(generators: np.ndarray, sectors, complex_chars: bool) -> Tuple[np.ndarray, np.ndarray]:

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from oracle import lattice, metropolis, operators as oops, rbm, resconv
+from oracle import lattice, metropolis, operators as oops, rbm
 
 from test_gpu_rbm import Rbm, pack, unpack, compiled
 from test_gpu_resconv import Net, _pack

@@ -3,7 +3,6 @@
 their restatement from the same device calls."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import operators as oops, rbm, resconv, sr as osr
 

@@ -2,7 +2,6 @@
 Metropolis replaying the same component sequence: chains, accepts and log psi."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import lattice, metropolis, rbm
 

@@ -13,7 +13,6 @@ import os
 
 import numpy as np
 import pytest
-import torch
 
 from oracle import operators as oops, resconv, sr as osr
 

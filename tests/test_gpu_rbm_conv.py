@@ -2,7 +2,6 @@
 (oracle/rbm.py RBMConv): log psi, the Metropolis sweep (bit-exact decisions), local energies,
 log-derivatives, and one SR step of the examples/RBM.ipynb workload shape. The 10 x 10 lattice
 with 16 channels is 1600 hidden units, the 2048-wide kernels."""
-import ctypes as C
 
 import numpy as np
 import pytest

@@ -3,9 +3,8 @@ inverse-CDF draw on the shared Philox stream (bit-exact indices) and against exa
 and RandomSampler's configurations and reweight factors."""
 import numpy as np
 import pytest
-import torch
 
-from oracle import metropolis, operators as oops, rbm, resconv
+from oracle import metropolis, rbm, resconv
 
 pytestmark = pytest.mark.gpu
 

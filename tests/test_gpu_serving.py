@@ -3,7 +3,6 @@ results as when each runs alone (stated tolerance: 1e-12 relative on every step'
 the kernels use fixed reduction orders, so the results are expected to be identical)."""
 import numpy as np
 import pytest
-import torch
 
 pytestmark = pytest.mark.gpu
 

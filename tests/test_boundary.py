@@ -50,6 +50,15 @@ def test_argument_errors_are_reported_without_a_device(qgx_built):
     assert L.qgx_rbm_sweep(None, 8, 16, None, None, None, 4, 1, 0, 0, 2.0, 7, None, 0, 1, None) == _lib.QGX_ERR_ARG
     assert L.qgx_gram(None, 4, 4, 2, None, 4, 0, None) == _lib.QGX_ERR_ARG
     assert L.qgx_spins_init_uniform(None, 0, 8, 1, None) == _lib.QGX_OK  # empty batch is a no-op
+    # exact sampling and exact reconfiguration entry points
+    assert L.qgx_exact_draw(None, 0, 4, 1, 0, None, None) == _lib.QGX_ERR_ARG  # empty basis
+    assert L.qgx_exact_draw(None, 8, 4, 1, 0, None, None) == _lib.QGX_ERR_ARG  # null pointers
+    assert L.qgx_exact_draw(None, 8, 0, 1, 0, None, None) == _lib.QGX_OK       # no samples
+    assert L.qgx_csr_matvec(None, None, None, 4, None, 3, None, None) == _lib.QGX_ERR_ARG  # nvec not 1 or 2
+    assert L.qgx_csr_matvec(None, None, None, 4, None, 1, None, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_er_weight_rows(None, 4, 8, 4, None, 0, None) == _lib.QGX_ERR_ARG  # ldo < cols
+    assert L.qgx_er_center(None, 4, 8, 8, None, 1, None, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_column_sumsq(None, 4, 8, 4, None, None, 0, None) == _lib.QGX_ERR_ARG
 
 
 def test_no_cpu_fallback_without_library(tmp_path):

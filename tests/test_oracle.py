@@ -191,3 +191,27 @@ def test_rbm_conv_is_the_translated_dense_rbm():
             up = rbm.RBMConv((p + e)[:C * N].reshape(C, L0, L1), (p + e)[C * N:])
             dn = rbm.RBMConv((p - e)[:C * N].reshape(C, L0, L1), (p - e)[C * N:])
             np.testing.assert_allclose((up.log_psi(s) - dn.log_psi(s)) / 2e-6, J[:, k], rtol=1e-6, atol=1e-8)
+
+
+def test_lattices_match_the_reference_code():
+    """Site coordinates and n-th nearest-neighbour bonds of the oracle and of the package
+    against the output of the reference's own quantax.sites code
+    (tests/golden/lattice_reference.json, made by tests/golden/make_lattice_golden.py):
+    pins the bond lists the Heisenberg and J1-J2 operators are built from."""
+    import json
+    from pathlib import Path
+    import quantax_gb300 as qtx
+    gold = json.loads((Path(__file__).parent / "golden" / "lattice_reference.json").read_text())
+    for key, rec in gold.items():
+        kind, L = key.split("(")[0], int(key.split("(")[1].rstrip(")"))
+        dims = (L,) if kind == "Chain" else (L, L)
+        shells = [int(n) for n in rec["neighbors"]]
+        ours = lattice.neighbors(dims, shells)
+        ours = ours if isinstance(ours, list) else [ours]
+        site = getattr(qtx.sites, kind)(L)
+        pkg = site.get_neighbor(shells)
+        np.testing.assert_allclose(np.asarray(site.coord, dtype=float), np.asarray(rec["coord"]), atol=1e-12)
+        for n, o, p in zip(shells, ours, pkg):
+            want = np.asarray(rec["neighbors"][str(n)], dtype=np.int64).reshape(-1, 2)
+            assert np.array_equal(np.asarray(o), want), (key, n)
+            assert np.array_equal(np.asarray(p), want), (key, n)

@@ -8,6 +8,9 @@ periodic or open boundaries:
   * the n-th-neighbour bonds are the pairs (i, j), i < j, whose distance equals the
     n-th smallest non-zero distance, listed in row-major (argwhere) order
     (quantax/sites/sites.py:267-283).
+
+Pinned: coordinates and bonds equal the output of the reference's own sites code for the
+lattices in tests/golden/lattice_reference.json.
 """
 from __future__ import annotations
 

@@ -60,8 +60,13 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
 /* ---- library ----------------------------------------------------------------- */
 int qgx_abi_version(void);
 const char* qgx_status_string(int status);
-/* Human-readable text of the last CUDA error seen by this thread ("" if none). */
+/* Human-readable text of the last error recorded by this thread ("" if none): a CUDA error,
+ * or the reason an entry point rejected its arguments where it gives one. */
 const char* qgx_last_error(void);
+/* Empty this thread's qgx_last_error() text (a caller clears it before a call so that the
+ * text it reads afterwards belongs to that call). Status plumbing of this library; no
+ * counterpart in the reference, whose errors are Python exceptions. */
+void qgx_clear_last_error(void);
 
 /* ---- random numbers ------------------------------------------------------------ */
 /* Raw Philox4x32-10 on n counters: out[4i..4i+3] = philox(ctr[4i..4i+3], key[0..1]).
@@ -165,7 +170,10 @@ int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias,
  * Requests needing more scratch (qgx_rbm_obar_workspace_bytes(n, m, ns) larger than the
  * array) return QGX_ERR_ARG and nothing is enqueued; qgx_last_error() then says why.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture. All calls
+ * with that device current; make that first call before any stream capture. The address is
+ * cached per device with the CUDA context it belongs to; when the device's current context
+ * changes (the primary context released and created again, e.g. by cudaDeviceReset) the next
+ * call looks it up again, so that call too should come before any capture. All calls
  * share the array and it keeps the last call's contents (every region is fully written
  * before it is read, so nothing needs clearing): calls that overlap on the GPU, on
  * different streams of one device, race on it and must be serialised by the caller. */

@@ -65,6 +65,7 @@ SIGNATURES = {
     "qgx_abi_version": (C.c_int, []),
     "qgx_status_string": (C.c_char_p, [C.c_int]),
     "qgx_last_error": (C.c_char_p, []),
+    "qgx_clear_last_error": (None, []),
     "qgx_philox4x32_10": (C.c_int, [vp, vp, vp, i64, vp]),
     "qgx_spins_init_uniform": (C.c_int, [vp, i64, i32, u64, vp]),
     "qgx_spins_init_fixed_up": (C.c_int, [vp, i64, i32, i32, u64, vp]),
@@ -137,7 +138,7 @@ class QgxError(RuntimeError):
     def __init__(self, name, status, lib):
         self.status = status
         msg = lib.qgx_status_string(status).decode()
-        detail = lib.qgx_last_error().decode() if status == QGX_ERR_CUDA else ""
+        detail = lib.qgx_last_error().decode()  # cleared before the call: this call's reason, if any
         super().__init__(f"{name} failed: {msg} ({status}) {detail}".strip())
 
 
@@ -200,6 +201,7 @@ def call(name, *args):
     """Call an entry point that returns a status code; raise on failure."""
     global launch_count
     L = load()
+    L.qgx_clear_last_error()
     rc = getattr(L, name)(*args)
     if rc != QGX_OK:
         raise QgxError(name, rc, L)

@@ -515,6 +515,8 @@ const char* qgx_status_string(int status) {
 
 const char* qgx_last_error(void) { return g_last_error; }
 
+void qgx_clear_last_error(void) { g_last_error[0] = 0; }
+
 int qgx_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int64_t n, qgx_stream_t stream) {
   QGX_CHECK_ARG(n >= 0);
   if (n == 0) return QGX_OK;

@@ -13,6 +13,8 @@
 // Mp = 128 * JT and lane l owns units {128 j + 4 l + q : j < JT, q < 4}, so every table
 // row is read with one 16-byte shared-memory load per lane and j. theta and t stay in
 // registers for the whole sweep; only the packed spins and log|psi| touch HBM.
+#include <cuda.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
@@ -964,23 +966,51 @@ int qgx_rbm_obar(const float* table, int32_t n, int32_t m, int32_t has_vbias, co
 // ---- no-allocation variant of qgx_rbm_obar -----------------------------------------------
 // Scratch for callers that cannot allocate: one static device array per GPU that loads the
 // library. Host code must not use the symbol's name as an address: the device address is
-// looked up once per device with cudaGetSymbolAddress (with that device current) and cached.
+// looked up with cudaGetSymbolAddress (with that device current) and cached per device,
+// together with the CUDA context it belongs to. A different current context on that device
+// (the primary context released and created again, e.g. after cudaDeviceReset, which also
+// reloads the module) makes the next call look the address up again, so a stale address is
+// never used.
 static __device__ __align__(256) unsigned char g_obar_scratch[QGX_RBM_OBAR_STATIC_SCRATCH_BYTES];
 
 namespace {
 constexpr int kMaxScratchDevices = 64;
 std::mutex g_scratch_mutex;
 void* g_scratch_ptr[kMaxScratchDevices] = {};
+CUcontext g_scratch_ctx[kMaxScratchDevices] = {};
+
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+
+CtxGetCurrent ctx_get_current_fn() {
+  static std::once_flag once;
+  static CtxGetCurrent fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrent>(p);
+  });
+  return fn;
+}
 
 int scratch_for_current_device(void** out) {
   int dev = 0;
   QGX_CHECK_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxScratchDevices) return QGX_ERR_UNSUPPORTED;
+  CtxGetCurrent get_ctx = ctx_get_current_fn();
+  if (!get_ctx) return QGX_ERR_UNSUPPORTED;
+  CUcontext ctx = nullptr;
+  if (get_ctx(&ctx) != CUDA_SUCCESS) return QGX_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (!ctx || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
+    // no context bound yet, or a different one: the lookup binds the device's primary
+    // context (creating it if needed) and loads the module into it
     void* p = nullptr;
     QGX_CHECK_CUDA(cudaGetSymbolAddress(&p, g_obar_scratch));
+    if (get_ctx(&ctx) != CUDA_SUCCESS || !ctx) return QGX_ERR_UNSUPPORTED;
     g_scratch_ptr[dev] = p;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return QGX_OK;

@@ -6,7 +6,7 @@ oracle_small.json: seeded outputs of the oracle for small cases (Philox stream w
 initial configurations, a LocalFlip run, E_loc and O of an RBM), pinning the oracle's
 restatement so that later changes to it are caught.
 
-    python tests/golden/make_golden.py [path-to-reference-checkout]
+    python tests/golden/make_golden.py <path-to-reference-checkout>
 """
 import json
 import re
@@ -61,7 +61,9 @@ def oracle_small():
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the quantax checkout>")
+    ref = Path(sys.argv[1])
     (HERE / "reference_energies.json").write_text(json.dumps(reference_energies(ref), indent=1) + "\n")
     (HERE / "oracle_small.json").write_text(json.dumps(oracle_small()) + "\n")
     print("wrote", HERE / "reference_energies.json", HERE / "oracle_small.json")

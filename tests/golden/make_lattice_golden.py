@@ -36,7 +36,9 @@ def load_reference_sites(ref: Path):
 
 
 def main():
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_lattice_golden.py <path of the quantax checkout>")
+    ref = Path(sys.argv[1])
     sites = load_reference_sites(ref)
     out = {}
     for kind, L, shells in CASES:

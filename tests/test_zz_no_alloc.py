@@ -2,8 +2,10 @@
 
 Callers such as a JAX/XLA FFI custom-call handler or a serving loop with a fixed HBM
 budget may not call cudaMalloc; qgx_rbm_obar_noalloc serves them from a static device
-array inside the library. This file is collected last so that a run stopping at the
-first failure has already run every other test; it also passes on its own in a fresh
+array inside the library. Both entry points run the same kernels on the same inputs, so
+their outputs must agree bit for bit: any difference means scratch left over from an
+earlier call leaked into a result. This file is collected last so that a run stopping at
+the first failure has already run every other test; it also passes on its own in a fresh
 process.
 """
 import numpy as np
@@ -14,6 +16,8 @@ from oracle import metropolis, rbm
 
 pytestmark = pytest.mark.gpu
 
+CAPACITY = 32 << 20  # QGX_RBM_OBAR_STATIC_SCRATCH_BYTES
+
 
 def _pack(s):
     ns, n = s.shape
@@ -21,6 +25,17 @@ def _pack(s):
     for j in range(n):
         out[:, j // 32] |= (s[:, j] > 0).astype(np.uint32) << np.uint32(j % 32)
     return torch.as_tensor(out.view(np.int32)).cuda()
+
+
+def _largest_ns(lib, N, M):
+    """The largest sample count whose scratch fits the static array."""
+    lo, hi = 1, 2
+    while lib.qgx_rbm_obar_workspace_bytes(N, M, hi) <= CAPACITY:
+        lo, hi = hi, 2 * hi
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        lo, hi = (mid, hi) if lib.qgx_rbm_obar_workspace_bytes(N, M, mid) <= CAPACITY else (lo, mid)
+    return lo
 
 
 def _case(N, M, ns, vb, seed):
@@ -56,24 +71,45 @@ def _no_alloc(table, N, M, vb, spins, rt, ns, npar):
     return O, om
 
 
-@pytest.mark.parametrize("N,M,ns,vb", [(16, 64, 300, True), (64, 256, 8192, False)])
-def test_no_alloc_obar_matches_workspace_entry_on_two_calls(cuda, N, M, ns, vb):
+def _check_two_calls(N, M, ns, vb):
     # two different inputs in a row: the second call must not see the first call's scratch
     for seed in (3, 11):
         table, spins, rt, npar = _case(N, M, ns, vb, seed)
         O_ref, om_ref = _with_workspace(table, N, M, vb, spins, rt, ns, npar)
         O, om = _no_alloc(table, N, M, vb, spins, rt, ns, npar)
         torch.cuda.synchronize()
-        # the tolerance of the Obar parity test (tests/test_gpu_rbm.py)
-        torch.testing.assert_close(O, O_ref, rtol=1e-4, atol=1e-6 / np.sqrt(ns))
-        torch.testing.assert_close(om, om_ref, rtol=1e-5, atol=1e-7)
+        assert torch.equal(O, O_ref), "Obar differs from qgx_rbm_obar"
+        assert torch.equal(om, om_ref), "Omean differs from qgx_rbm_obar"
+
+
+@pytest.mark.parametrize("N,M,ns,vb", [(16, 64, 300, True), (64, 256, 8192, False)])
+def test_no_alloc_obar_matches_workspace_entry_on_two_calls(cuda, N, M, ns, vb):
+    _check_two_calls(N, M, ns, vb)
+
+
+def test_no_alloc_at_capacity_and_one_sample_beyond(cuda):
+    # the largest request fills the static array to its last byte (16 sites, 64 hidden
+    # units: the scratch of 51589 samples is exactly 32 MiB); one sample more is refused
+    from quantax_gb300 import _lib as L
+    lib = L.lib()
+    N, M = 16, 64
+    ns = _largest_ns(lib, N, M)
+    assert CAPACITY - 4096 < lib.qgx_rbm_obar_workspace_bytes(N, M, ns) <= CAPACITY
+    _check_two_calls(N, M, ns, True)
+    lib.qgx_clear_last_error()
+    rc = lib.qgx_rbm_obar_noalloc(None, N, M, 1, None, None, ns + 1, None, M * N + M + N, None, None)
+    assert rc == L.QGX_ERR_ARG
+    assert b"static array" in lib.qgx_last_error()
 
 
 def test_no_alloc_rejects_requests_beyond_capacity(cuda):
     from quantax_gb300 import _lib as L
     lib = L.lib()
     N, M, ns = 64, 256, 65536  # needs about 200 MB of scratch
-    assert lib.qgx_rbm_obar_workspace_bytes(N, M, ns) > (32 << 20)
+    assert lib.qgx_rbm_obar_workspace_bytes(N, M, ns) > CAPACITY
     rc = lib.qgx_rbm_obar_noalloc(None, N, M, 0, None, None, ns, None, M * N + M, None, None)
     assert rc == L.QGX_ERR_ARG
     assert b"static array" in lib.qgx_last_error()
+    # through the Python binding the refusal carries the library's reason
+    with pytest.raises(L.QgxError, match="static array"):
+        L.call("qgx_rbm_obar_noalloc", None, N, M, 0, None, None, ns, None, M * N + M, None, None)

@@ -42,6 +42,44 @@ def reference_energies(ref: Path):
     return out
 
 
+def reference_observables(ref: Path):
+    """Expectation values the reference's notebooks print for exact ground states (read as
+    text). samples.ipynb: Square(4) with no particle-number constraint, Ising(h=1) (state0) and
+    Ising(h=3) (state1) ground states, M = sum_i sigma_z(i) / N, M2 = M @ M (:142); the cell at
+    :342 prints state1 @ M2 @ state1 under the label "h=1.0" (state1 is the h=3 state, :34), :411
+    prints exactM2[0] (the h=1 state), :451 the squared overlap of the two. exact_diag.ipynb: the
+    4x4 Heisenberg() (no MSR) ground state in the Sz = 0 sector, C_ij = (sigma_z(i) sigma_z(j)
+    + 2 sigma_p(i) sigma_m(j) + 2 sigma_m(i) sigma_p(j)) / 4 (:227-228), and the amplitude at the
+    printed configuration s (:160-161; the sign of an eigenvector is arbitrary)."""
+    out = {}
+
+    def grab(nb, pattern, cast=float):
+        lines = (ref / nb).read_text().split("\n")
+        for i, l in enumerate(lines, 1):
+            m = re.search(pattern, l)
+            if m:
+                return cast(m.group(1)), f"{nb}:{i}"
+        raise RuntimeError(f"{pattern} not found in {nb}")
+
+    v, src = grab("tutorials/samples.ipynb", r"Exact magnetization for h=1\.0: ([0-9.]+)")
+    out["square4_ising_h3_M2"] = dict(value=v, source=src, L=4, h=3.0, J=1.0, observable="M2")
+    v, src = grab("tutorials/samples.ipynb", r"Exact M2 = ([0-9.]+)")
+    out["square4_ising_h1_M2"] = dict(value=v, source=src, L=4, h=1.0, J=1.0, observable="M2")
+    v, src = grab("tutorials/samples.ipynb", r"Exact overlap:  ([0-9.]+)")
+    out["square4_ising_overlap_h1_h3"] = dict(value=v, source=src, L=4, h=[1.0, 3.0], J=1.0,
+                                              observable="|<psi(h=1)|psi(h=3)>|^2")
+    v, src = grab("tutorials/exact_diag.ipynb", r"<C01> = (-?[0-9.]+)")
+    out["square4_heisenberg_C01"] = dict(value=v, source=src, L=4, msr=False, nup=8, i=0, j=1, observable="C_ij")
+    v, src = grab("tutorials/exact_diag.ipynb", r"<C02> = (-?[0-9.]+)")
+    out["square4_heisenberg_C02"] = dict(value=v, source=src, L=4, msr=False, nup=8, i=0, j=2, observable="C_ij")
+    spins, ssrc = grab("tutorials/exact_diag.ipynb", r'"s = \[([-0-9 ]+)\]',
+                       cast=lambda t: [int(x) for x in t.split()])
+    v, src = grab("tutorials/exact_diag.ipynb", r"<s\|psi0> = \[(-?[0-9.]+)\]")
+    out["square4_heisenberg_psi0_at_s"] = dict(value=abs(v), source=f"{ssrc}, {src}", L=4, msr=False, nup=8,
+                                               s=spins, printed_digits=6, observable="|<s|psi0>|")
+    return out
+
+
 def oracle_small():
     from oracle import metropolis, operators, philox, rbm
     out = {}
@@ -64,6 +102,7 @@ if __name__ == "__main__":
     if len(sys.argv) != 2:
         sys.exit("usage: python tests/golden/make_golden.py <path of the quantax checkout>")
     ref = Path(sys.argv[1])
-    (HERE / "reference_energies.json").write_text(json.dumps(reference_energies(ref), indent=1) + "\n")
+    (HERE / "reference_energies.json").write_text(
+        json.dumps({**reference_energies(ref), **reference_observables(ref)}, indent=1) + "\n")
     (HERE / "oracle_small.json").write_text(json.dumps(oracle_small()) + "\n")
     print("wrote", HERE / "reference_energies.json", HERE / "oracle_small.json")

@@ -308,6 +308,13 @@ int qgx_resconv_jacobian_symm(const float* table, int32_t L, int32_t nblocks, in
  * stats[0..2] = {Re energy, Im energy, VarE}. */
 int qgx_energy_stats(const double* E_re, const double* E_im, const double* r, int64_t ns,
                      double* stats, double* ebar_re, double* ebar_im, qgx_stream_t stream);
+/* Consistency of log|psi| carried through local updates with a direct forward
+ * (Metropolis.sweep, quantax/sampler/metropolis.py:201-213): *count (device int) = number of
+ * samples for which neither |psi_l - psi_d| < 1e-8 nor |psi_l / psi_d - 1| < 1e-3 holds;
+ * out (may be NULL or equal local) receives the direct values, which replace the local ones
+ * as in the reference. */
+int qgx_log_psi_mismatch(const float* local, const float* direct, int64_t ns, int32_t* count,
+                         float* out, qgx_stream_t stream);
 /* Reweight factors r_s = |psi_s|^(2-n) / mean (Sampler._get_reweight_factor,
  * quantax/sampler/sampler.py:66-69), from log|psi|. */
 int qgx_reweight_factor(const float* log_psi, int64_t ns, float reweight, double* r,
@@ -400,7 +407,10 @@ int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t ld
  * iteration count). */
 int64_t qgx_last_solve_kernels(void);
 /* SR branch: given S = A^T A (np x np FP64, overwritten): x = S^-1 A^T b with the same
- * two regularisations (lstsq_shift_eig / lstsq_pinv_eig). */
+ * two regularisations (lstsq_shift_eig / lstsq_pinv_eig). PINV with tol_snr > 1e-6 applies
+ * lstsq_pinv_eig's noise truncation (solver.py:152-164 with _sum_without_noise, :114-125):
+ * rho_k = sum_s t_sk / (1 + (tol_snr / snr_k)^6) over the per-sample terms
+ * t_sk = b_s (A V)_sk, snr_k = |mean_s t_sk| / sqrt(var_s t_sk / n). */
 int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda,
                  const double* b, int32_t method, double rshift, double ashift,
                  double rtol, double atol, double tol_snr, double* x, int32_t* info,

@@ -131,6 +131,7 @@ SIGNATURES = {
     "qgx_sym_solve": (C.c_int, [vp, i64, vp, i32, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_sr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_apply_update": (C.c_int, [vp, vp, i64, vp, vp]),
+    "qgx_log_psi_mismatch": (C.c_int, [vp, vp, i64, vp, vp, vp]),
 }
 
 
@@ -152,7 +153,7 @@ KERNELS_PER_CALL = {
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
     "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1, "qgx_column_sumsq": 2,
     "qgx_rbm_conv_jacobian": 1, "qgx_apply_update": 2, "qgx_csr_matvec": 1, "qgx_er_weight_rows": 1, "qgx_exact_draw": 1,
-    "qgx_er_center": 1,
+    "qgx_er_center": 1, "qgx_log_psi_mismatch": 1,
 }
 launch_count = 0
 

@@ -430,6 +430,32 @@ __global__ void er_center_kernel(float* __restrict__ O, int64_t ns, int64_t cols
   }
 }
 
+// psi from local updates against a direct forward (Metropolis.sweep, metropolis.py:201-213):
+// close when |psi_l - psi_d| < 1e-8 or |psi_l / psi_d - 1| < 1e-3 (on log|psi|: the ratio is
+// exp(lp_l - lp_d)); counts the configurations that are neither and, when out is given,
+// writes the direct values there (out may be local itself). One block, fixed reduction order.
+__global__ void log_psi_mismatch_kernel(const float* local, const float* __restrict__ direct, int64_t ns,
+                                        int32_t* __restrict__ count, float* out) {
+  __shared__ int sh[32];
+  int c = 0;
+  for (int64_t i = threadIdx.x; i < ns; i += blockDim.x) {
+    const double l = (double)local[i], d = (double)direct[i];
+    const bool close_abs = fabs(exp(l) - exp(d)) < 1e-8;
+    const bool close_rel = fabs(expm1(l - d)) < 1e-3;
+    c += (close_abs || close_rel) ? 0 : 1;
+    if (out) out[i] = direct[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    *count = t;
+  }
+}
+
 }  // namespace qgx
 
 using namespace qgx;
@@ -578,6 +604,13 @@ int qgx_energy_stats(const double* E_re, const double* E_im, const double* r, in
 int qgx_reweight_factor(const float* log_psi, int64_t ns, float reweight, double* r, qgx_stream_t stream) {
   QGX_CHECK_ARG(ns > 0 && log_psi && r);
   reweight_kernel<<<1, kStatThreads, 0, as_cuda(stream)>>>(log_psi, ns, reweight, r);
+  return launch_status();
+}
+
+int qgx_log_psi_mismatch(const float* local, const float* direct, int64_t ns, int32_t* count, float* out,
+                         qgx_stream_t stream) {
+  QGX_CHECK_ARG(ns > 0 && local && direct && count);
+  log_psi_mismatch_kernel<<<1, 1024, 0, as_cuda(stream)>>>(local, direct, ns, count, out);
   return launch_status();
 }
 

@@ -190,6 +190,103 @@ __global__ void uv_partial_kernel(const double* __restrict__ U, int64_t n, const
   part[blockIdx.y * n + t] = acc;
 }
 
+// SR-branch noise truncation (lstsq_pinv_eig, solver.py:152-164, with _sum_without_noise,
+// :114-125): the per-sample terms y[s, k] = b[s] sum_l A[s, l] V[l, k] (A FP32 row-major,
+// V the FP64 eigenvectors of S, column-major) are formed tile by tile in FP64 and reduced at
+// once to each 64-row chunk's mean and sum of squared deviations per column; the (ns x np)
+// matrix of terms is never stored.
+constexpr int kSnrRows = 64;
+__global__ void __launch_bounds__(256) snr_terms_kernel(const float* __restrict__ A, int64_t ns, int64_t np,
+                                                        int64_t lda, const double* __restrict__ V,
+                                                        const double* __restrict__ b, double* __restrict__ part) {
+  __shared__ double As[16][kSnrRows + 1];  // [l][s]
+  __shared__ double Vs[16][kSnrRows + 1];  // [l][k]
+  __shared__ double Ys[kSnrRows][kSnrRows + 1];
+  const int64_t s0 = (int64_t)blockIdx.y * kSnrRows, k0 = (int64_t)blockIdx.x * kSnrRows;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 terms each
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int64_t l0 = 0; l0 < np; l0 += 16) {
+    for (int e = threadIdx.x; e < 16 * kSnrRows; e += 256) {
+      const int c = e & 15, r = e >> 4;
+      const int64_t srow = s0 + r, l = l0 + c, k = k0 + r;
+      As[c][r] = (srow < ns && l < np) ? (double)A[srow * lda + l] : 0.0;
+      Vs[c][r] = (k < np && l < np) ? V[k * np + l] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int c = 0; c < 16; ++c) {
+      double a[4], v[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = As[c][4 * ty + i];
+        v[i] = Vs[c][4 * tx + i];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], v[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t srow = s0 + 4 * ty + i;
+    const double bs = srow < ns ? b[srow] : 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) Ys[4 * ty + i][4 * tx + j] = acc[i][j] * bs;
+  }
+  __syncthreads();
+  if (threadIdx.x < kSnrRows) {
+    const int64_t k = k0 + threadIdx.x;
+    const int cnt = (int)min((int64_t)kSnrRows, ns - s0);
+    if (k < np) {
+      double sum = 0.0;
+      for (int r = 0; r < cnt; ++r) sum += Ys[r][threadIdx.x];
+      const double mean = sum / cnt;
+      double m2 = 0.0;
+      for (int r = 0; r < cnt; ++r) {
+        const double d = Ys[r][threadIdx.x] - mean;
+        m2 = fma(d, d, m2);
+      }
+      part[(blockIdx.y * np + k) * 2 + 0] = mean;
+      part[(blockIdx.y * np + k) * 2 + 1] = m2;
+    }
+  }
+}
+
+// merge the chunks' (mean, M2) in chunk order (Chan, Golub and LeVeque's pairwise update),
+// then x = sum, snr = |mean| / sqrt(var / ns), rho = x / (1 + (tol_snr / snr)^6), v = inv rho
+__global__ void snr_rho_kernel(const double* __restrict__ part, int64_t nchunk, int64_t ns, int64_t np,
+                               const double* __restrict__ inv, double tol_snr, double* __restrict__ v) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  double na = 0.0, mean = 0.0, m2 = 0.0;
+  for (int64_t c = 0; c < nchunk; ++c) {
+    const double nb = (double)min((int64_t)kSnrRows, ns - c * kSnrRows);
+    const double mb = part[(c * np + k) * 2 + 0];
+    const double m2b = part[(c * np + k) * 2 + 1];
+    const double n = na + nb;
+    const double d = mb - mean;
+    mean = fma(d, nb / n, mean);
+    m2 += m2b + d * d * (na * nb / n);
+    na = n;
+  }
+  const double x = mean * (double)ns;
+  double rho = x;
+  if (tol_snr > 1e-6) {
+    const double xv = sqrt(m2 / (double)ns / (double)ns);
+    const double snr = fabs(mean) / xv;
+    const double r = tol_snr / snr;
+    const double r2 = r * r;
+    rho = x / (1.0 + r2 * r2 * r2);
+  }
+  v[k] = inv[k] * rho;
+}
+
 // SHIFT_MIXED: preconditioned conjugate gradients in FP64 on (T + shift I) y = b, the
 // preconditioner being the FP32 Cholesky factor of the same matrix (or of T + shift' I with
 // a larger shift' when the FP32 factorisation breaks down)
@@ -420,7 +517,11 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   const int64_t o_inv = take(n * 8);
   const int64_t o_v = take(n * 8);
   const int64_t o_f = take(n * 8);
-  const int64_t o_part = take(nchunk * wide * 8);
+  // PINV on the SR branch with noise truncation: per 64-row chunk (mean, M2) of every column
+  const int64_t snr_part = method == QGX_SOLVE_PINV
+                               ? (std::max(n, np) + kSnrRows - 1) / kSnrRows * std::min(n, np) * 16
+                               : 0;
+  const int64_t o_part = take(std::max(nchunk * wide * 8, snr_part));
   const int64_t o_shift = take(16);
   const int64_t o_info = take(8);
   const bool mixed = method == QGX_SOLVE_SHIFT_MIXED;
@@ -645,8 +746,6 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
   QGX_CHECK_ARG(n > 0 && np > 0 && lda >= np && S && A && b && x && workspace);
   QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  // the per-sample SNR truncation of lstsq_pinv_eig needs the full (ns x np) rho matrix
-  if (method == QGX_SOLVE_PINV && tol_snr > 1e-6) return QGX_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   g_kernels = 0;
   SolveWs ws;
@@ -654,6 +753,34 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
   int rc = workspace_layout(np, n, method, workspace, workspace_bytes, &ws, &need);
   if (rc != QGX_OK) return rc;
   cudaStream_t st = as_cuda(stream);
+  if (method == QGX_SOLVE_PINV && tol_snr > 1e-6) {
+    // lstsq_pinv_eig with noise truncation: S = V diag(l) V^T, rho_k from the per-sample
+    // terms b[s] (A V)[s, k], x = V diag(l+) rho
+    cusolverDnHandle_t h;
+    cusolverDnParams_t p;
+    if ((rc = solver_for_current_device(&h, &p)) != QGX_OK) return rc;
+    if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+    void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
+    if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, np, CUDA_R_64F, S, np, CUDA_R_64F,
+                         ws.w, CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(),
+                         info ? info : ws.info) != CUSOLVER_STATUS_SUCCESS)
+      return QGX_ERR_SOLVER;
+    ++g_kernels;
+    eigs_inv_kernel<<<1, 1024, 0, st>>>(ws.w, np, rtol, atol, ws.inv);
+    const int64_t nchunk = (n + kSnrRows - 1) / kSnrRows;
+    if (nchunk > 65535) return QGX_ERR_UNSUPPORTED;
+    ++g_kernels;
+    snr_terms_kernel<<<dim3((unsigned)((np + kSnrRows - 1) / kSnrRows), (unsigned)nchunk), 256, 0, st>>>(
+        A, n, np, lda, S, b, ws.part);
+    ++g_kernels;
+    snr_rho_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(ws.part, nchunk, n, np, ws.inv, tol_snr, ws.v);
+    const int64_t vchunk = (np + kProjRows - 1) / kProjRows;
+    ++g_kernels;
+    uv_partial_kernel<<<dim3((unsigned)((np + 255) / 256), (unsigned)vchunk), 256, 0, st>>>(S, np, ws.v, ws.part);
+    ++g_kernels;
+    sum_partials_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(ws.part, vchunk, np, x);
+    return launch_status();
+  }
   // F = A^T b into ws.f, then S x = F
   if ((rc = project(A, n, np, lda, b, ws.part, ws.f, st)) != QGX_OK) return rc;
   if ((rc = solve_gram(S, np, ws.f, method, rshift, ashift, rtol, atol, 0.0, ws, info, st)) != QGX_OK) return rc;

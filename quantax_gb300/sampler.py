@@ -8,6 +8,7 @@ run is reproducible from the global seed and independent of launch geometry.
 """
 from __future__ import annotations
 
+import warnings
 from dataclasses import dataclass
 from typing import Optional, Sequence, Union
 
@@ -237,6 +238,21 @@ class Metropolis(Sampler):
             st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, nsteps, self._seed, step0,
                            self._reweight, proposal, nbr, z, hop)
 
+    def _check_local_updates(self) -> None:
+        """metropolis.py:201-213: after a sweep by local updates, log|psi| is evaluated again by a
+        direct forward; a warning names how many samples differ (neither |psi_l - psi_d| < 1e-8
+        nor |psi_l / psi_d - 1| < 1e-3), and the direct values replace the local ones. Reading
+        the count synchronises the host with the sweep, as the reference's check does."""
+        direct = self._state.log_psi_packed(self._packed)
+        if not hasattr(self, "_mismatch"):
+            self._mismatch = torch.zeros(1, dtype=torch.int32, device=self._log_psi.device)
+        _lib.call("qgx_log_psi_mismatch", _lib.ptr(self._log_psi), _lib.ptr(direct), self._nsamples,
+                  _lib.ptr(self._mismatch), _lib.ptr(self._log_psi), _lib.stream_ptr())
+        ndiff = int(self._mismatch.item())
+        if ndiff > 0:
+            warnings.warn(f"{ndiff} out of {self._nsamples} wavefunctions are not close in direct forward pass and "
+                          "local updates. This may indicate inaccurate local updates.")
+
     def _run_proposals(self, n: int) -> None:
         self._device_sweep(n, self._step, self.proposal, self._nbr, self._z, self._hop)
 
@@ -252,6 +268,8 @@ class Metropolis(Sampler):
             signed = st.symm_dev is not None or getattr(st.model, "signed_output", False)
             lp = torch.view_as_complex(self._log_psi.clone()) if st.is_complex or signed else lp_real
         else:
+            if st.use_ref and self.nflips is not None:
+                self._check_local_updates()
             lp_real = self._log_psi
             lp = self._log_psi.clone()
         self._step += n

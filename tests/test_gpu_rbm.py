@@ -305,3 +305,30 @@ def test_config2_slice_eloc_and_obar(cuda):
     Oref = net.jacobian(s)
     np.testing.assert_allclose(Ob.cpu().numpy(), osr.obar(Oref), rtol=1e-4, atol=1e-6 / np.sqrt(ns))
     np.testing.assert_allclose(om.cpu().numpy(), Oref.mean(axis=0), rtol=1e-5, atol=1e-7)
+
+
+def test_psi_consistency_check_after_local_updates(cuda):
+    """Metropolis.sweep's check (metropolis.py:201-213): log|psi| carried through the sweep's
+    local updates agrees with a direct forward, so a normal sweep warns about nothing; a sweep
+    whose updates ran on a perturbed copy of the table (inaccurate local updates) warns with the
+    number of samples that differ, and its samples carry the direct values."""
+    import warnings
+    import quantax_gb300 as qtx
+    qtx.sites.Chain(16)
+    W, b, a = rbm.init_normal(16, 32, 0.2, seed=5, visible_bias=True)
+    state = qtx.state.Variational(qtx.model.RBM_Dense.from_arrays(W, b, a))
+    sampler = qtx.sampler.LocalFlip(state, 128, thermal_steps=0, sweep_steps=64)
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        samples = sampler.sweep()
+    assert torch.equal(samples.log_psi, state.log_psi_packed(samples.packed))
+    model = state.model
+    sweep = model.sweep
+    bad = state.table.clone() * 1.05
+    model.sweep = lambda table, *args: sweep(bad, *args)
+    try:
+        with pytest.warns(UserWarning, match=r"\d+ out of 128 wavefunctions are not close"):
+            samples = sampler.sweep()
+    finally:
+        del model.sweep
+    assert torch.equal(samples.log_psi, state.log_psi_packed(samples.packed))

@@ -128,6 +128,31 @@ def test_sr_lstsq_solve(cuda, method):
     np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("ns,np_,tol_snr", [(400, 60, 0.5), (1000, 130, 2.0), (700, 64, 1.0), (300, 90, 0.0)])
+def test_sr_lstsq_pinv_noise_truncation(cuda, ns, np_, tol_snr):
+    """lstsq_pinv_eig(tol_snr) on the SR branch (Ns >= Np, solver.py:152-164): the per-sample
+    terms b_s (A V)_sk are reduced to their SNR in 64-row chunks; against the oracle's
+    _sum_without_noise restatement (stated: 1e-8 relative, FP64 throughout with the FP32 A
+    read exactly). Row counts not a multiple of 64 exercise the ragged last chunk."""
+    L = lib()
+    rng = np.random.default_rng(ns + np_)
+    A = (rng.normal(size=(ns, np_)) / 20 + 0.05 * rng.normal(size=(1, np_))).astype(np.float32)
+    b = rng.normal(size=ns)
+    A64 = A.astype(np.float64)
+    S = torch.as_tensor(A64.T @ A64).cuda()
+    At, bt = torch.as_tensor(A).cuda(), torch.as_tensor(b).cuda()
+    nb = C.c_int64(0)
+    L.call("qgx_solve_workspace_bytes", np_, ns, 1, C.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    x = torch.empty(np_, dtype=torch.float64, device="cuda")
+    L.call("qgx_sr_solve", L.ptr(S), np_, L.ptr(At), ns, np_, L.ptr(bt), 1, 0.0, 0.0, 1e-12, 0.0, tol_snr,
+           L.ptr(x), None, L.ptr(ws), ws.numel(), L.stream_ptr())
+    ref = osr.lstsq_pinv(A64, b, rtol=1e-12, tol_snr=tol_snr)
+    assert np.linalg.norm(x.cpu().numpy() - ref) < 1e-8 * np.linalg.norm(ref)
+    if tol_snr > 0:  # the truncation changes the step: the check is not vacuous
+        assert np.linalg.norm(osr.lstsq_pinv(A64, b, rtol=1e-12) - ref) > 1e-3 * np.linalg.norm(ref)
+
+
 def test_energy_stats(cuda):
     L = lib()
     rng = np.random.default_rng(2)

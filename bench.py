@@ -1,18 +1,28 @@
 #!/usr/bin/env python
 """Benchmark of the VMC inner loop on one GB300 (one JSON line on stdout).
 
-Workload (default): 1D chain L=64, periodic, transverse-field Ising h=J=1; RBM_Dense with
-256 hidden units (alpha 4, 16,640 float32 parameters, N(0, 0.01^2) init); LocalFlip with
-8192 chains, 64 single-spin proposals per sweep, 640 thermalisation proposals; MinSR
-(Ns = 8192 < Np, T 8192 x 8192) with diagonal shift 1e-4 (minnorm_shift_eig), FP32
-everywhere except the FP64 Cholesky solve. One step = one SR iteration: sweep, local
-energies, Obar, Gram, solve, parameter update.
+Default workload (--workload resconv): J1-J2 Heisenberg (J2 = 0.5, MSR) on the periodic 10 x 10
+square lattice in the Sz = 0 sector; ResConv with 8 residual blocks and 16 channels, complex
+output (34,944 float32 parameters, He-normal init); SpinExchange with 16384 chains, 200
+proposals per sweep and 200 thermalisation proposals; MinSR with diagonal shift 1e-4
+(minnorm_shift_eig) on the stacked [Re; Im] 32768 x 34944 matrix. `value` is the plain method
+(FP32 convolutions, FP32-class Gram, FP64 solve); `forms` holds the accurate form (the plain
+arithmetic with the FP32-preconditioned FP64 solve) and the precision forms (TF32 / BF16
+tensor-core convolutions and Gram) on the same seeds, each with its speed-up over the plain
+method, its p50 / p99 step latency and its energies' difference from the plain run.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+--workload rbm: chain L=64 periodic TFIM h=J=1; RBM_Dense with 256 hidden units (16,640 float32
+parameters, N(0, 0.01^2) init); LocalFlip with 8192 chains, 64 proposals per sweep, 640
+thermalisation proposals; MinSR (T 8192 x 8192) with diagonal shift 1e-4.
 
-Under torchrun with N > 1 every rank runs an independent replica of the workload (the
-chains of different replicas never interact, no collective on the data path): weak
-scaling; timing is bracketed by barriers and the max over ranks is reported.
+One step = one SR iteration: sweep, local energies, Obar, Gram, solve, parameter update.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
+
+Under torchrun with N > 1 every rank runs an independent replica of the workload (the chains
+of different replicas never interact, no collective on the data path): weak scaling; timing is
+bracketed by barriers and the max over ranks is reported. --impl reference times whole SR
+steps of the CPU restatement (oracle/cpu_vmc.py) on the host cores at the same workload.
 """
 from __future__ import annotations
 
@@ -30,11 +40,30 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "SR steps/s"
 UNIT = "SR_steps/s"
-WORKLOAD = dict(workload="tfim_chain64_rbm256_minsr8192", lattice="Chain(64) PBC", hamiltonian="Ising(h=1, J=1)",
+
+# the workload as both arms report it in `config` (arithmetic choices go to `method`)
+WORKLOADS = {
+    "resconv": dict(workload="j1j2_square10_resconv8x16_minsr16384", lattice="Square(10) PBC, Sz=0",
+                    hamiltonian="Heisenberg(J=[1, 0.5], n_neighbor=[1, 2], msr=True)",
+                    model="ResConv(8 blocks, 16 channels, complex output)", nparams=34944,
+                    sampler="SpinExchange", chains=16384, proposals_per_sweep=200, thermal_proposals=200,
+                    solver="minnorm_shift_eig(ashift=1e-4) on the stacked [Re; Im] 32768 x 34944 matrix",
+                    l2="inputs larger than L2: Obar (4.6 GB) and T (8.6 GB) exceed the 129 MB L2 every step"),
+    "rbm": dict(workload="tfim_chain64_rbm256_minsr8192", lattice="Chain(64) PBC", hamiltonian="Ising(h=1, J=1)",
                 model="RBM_Dense(features=256)", nparams=16640, sampler="LocalFlip", chains=8192,
                 proposals_per_sweep=64, thermal_proposals=640, solver="minnorm_shift_eig(ashift=1e-4)",
-                l2="Obar (545 MB) and T (537 MB) exceed the 129 MB L2 every step")
-
+                l2="inputs larger than L2: Obar (545 MB) and T (537 MB) exceed the 129 MB L2 every step"),
+}
+GRAM_ROWS = {"resconv": 32768, "rbm": 8192}  # rows of T = Obar Obar^T ([Re; Im] stacked for ResConv)
+# the plain method and the other forms: (name, conv, gram, solve)
+PLAIN = {"resconv": ("plain", "fp32", "3xtf32", "fp64"), "rbm": ("plain", "fp32", "3xtf32", "fp64")}
+FORMS = {
+    "resconv": [("accurate_fp32_conv_3xtf32_gram_mixed_solve", "fp32", "3xtf32", "mixed"),
+                ("precision_tf32_conv_tf32_gram_mixed_solve", "tf32", "tf32", "mixed"),
+                ("precision_bf16_conv_bf16_gram_mixed_solve", "bf16", "bf16", "mixed")],
+    "rbm": [("accurate_3xtf32_gram_mixed_solve", "fp32", "3xtf32", "mixed"),
+            ("precision_tf32_gram_mixed_solve", "fp32", "tf32", "mixed")],
+}
 
 # DRAM bytes per Gram launch at the bench's shapes, from
 #   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum --clock-control none \
@@ -98,72 +127,125 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(budget_s: float = 20.0):
-    """The oracle's vectorised CPU restatement on a bounded sample of the workload, each
-    phase scaled to the full workload by its complexity (linear in the chains for the
-    sweep / E_loc / Obar, quadratic for the Gram, cubic for the Cholesky)."""
-    import numpy as np
-    import scipy.linalg as sla
-    from oracle import cpu_vmc, metropolis, rbm as orbm
+# ---- the CPU restatement (oracle/cpu_vmc.py): whole SR steps, never scaled -------------------------
+class CpuWorkload:
+    """Initial state of the CPU restatement for a workload at `chains` chains: the same lattice,
+    Hamiltonian, model shape and init distribution as the GPU arm, Philox draws from the same
+    stream layout."""
 
+    def __init__(self, workload: str, chains: int, seed: int = 1234):
+        import numpy as np
+        from oracle import lattice, metropolis, rbm as orbm, resconv
+        self.workload, self.chains, self.seed, self.step = workload, chains, seed, 0
+        if workload == "resconv":
+            self.L, self.nb, self.C = 10, 8, 16
+            self.params = resconv.init_he(self.nb, self.C, seed=seed)
+            self.s = metropolis.init_fixed_up(chains, 100, 50, seed)
+            self.nbr = lattice.neighbor_table((10, 10), 1)
+            shells = lattice.neighbors((10, 10), [1, 2])
+            self.bonds = np.concatenate([shells[0], shells[1]]).astype(np.int64)
+            # per bond: diagonal coupling J, off-diagonal element 2 J sign (MSR: sign -1 on J1 bonds)
+            self.Jb = np.concatenate([np.tile([1.0, -2.0], (len(shells[0]), 1)),
+                                      np.tile([0.5, 1.0], (len(shells[1]), 1))])
+            import torch
+            from oracle import cpu_vmc
+            self.lp = cpu_vmc._resconv_forward(torch.as_tensor(self.params), self.s, self.L, self.nb, self.C)
+        else:
+            W, b, _ = orbm.init_normal(64, 256, 0.01, seed=seed)
+            self.W, self.b = W.astype(np.float64), b.astype(np.float64)
+            self.s = metropolis.init_uniform(chains, 64, seed).astype(np.float64)
+
+    def sr_step(self, timings):
+        from oracle import cpu_vmc
+        if self.workload == "resconv":
+            self.params, self.s, self.lp, e = cpu_vmc.resconv_sr_step(
+                self.params, self.s, self.lp, self.L, self.nb, self.C, self.nbr, self.bonds, self.Jb, self.seed,
+                self.step, 200, timings=timings)
+            self.step += 200
+        else:
+            self.W, self.b, self.s, e = cpu_vmc.sr_step(self.W, self.b, self.s, self.seed, self.step, 64,
+                                                        timings=timings)
+            self.step += 64
+        return e
+
+
+def _host_threads():
     cores = len(os.sched_getaffinity(0))
     try:
         import threadpoolctl
         threadpoolctl.threadpool_limits(cores)
     except Exception:
         pass
-    N, M, NS, steps = 64, 256, 8192, 64
-    ns_s = 2048
-    W, b, _ = orbm.init_normal(N, M, 0.01, seed=0)
-    W, b = W.astype(np.float64), b.astype(np.float64)
-    s = metropolis.init_uniform(ns_s, N, 1).astype(np.float64)
-    tm = {}
-    cpu_vmc.sr_step(W, b, s, 7, 0, steps, timings=tm)  # Gram / solve at ns_s
-    t_lin = tm["sweep"] + tm["eloc"] + tm["obar"]
-    ng = 4096
-    Ob = np.random.default_rng(0).normal(size=(ng, M * N + M)) * 1e-3
-    t0 = time.perf_counter()
-    T = Ob @ Ob.T
-    t_gram = time.perf_counter() - t0
-    T[np.diag_indices_from(T)] += 1e-4
-    t0 = time.perf_counter()
-    sla.solve(T, np.ones(ng), assume_a="pos")
-    t_chol = time.perf_counter() - t0
-    total = t_lin * NS / ns_s + t_gram * (NS / ng) ** 2 + t_chol * (NS / ng) ** 3
-    return {"value": 1.0 / total, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": (f"oracle/cpu_vmc.py: sweep+E_loc+Obar on {ns_s} of {NS} chains (x{NS // ns_s}), Gram "
-                       f"{ng}x{M * N + M} (x{(NS // ng) ** 2}), Cholesky n={ng} (x{(NS // ng) ** 3}); "
-                       f"seconds per full SR step {total:.1f}"),
-            "phases_s": {"linear": t_lin * NS / ns_s, "gram": t_gram * (NS / ng) ** 2,
-                         "cholesky": t_chol * (NS / ng) ** 3}}
+    import torch
+    torch.set_num_threads(cores)
+    return cores
+
+
+def time_cpu_steps(workload: str, chains: int, max_steps: int, budget_s: float):
+    """Whole SR steps of the CPU restatement: as many as `max_steps`, stopping once `budget_s`
+    has been spent (at least one). Returns (steps, seconds, per-phase mean seconds, energies)."""
+    w = CpuWorkload(workload, chains)
+    times, phases, energies = [], {}, []
+    while len(times) < max(1, max_steps):
+        tm = {}
+        t0 = time.perf_counter()
+        energies.append(w.sr_step(tm))
+        times.append(time.perf_counter() - t0)
+        for k, v in tm.items():
+            phases[k] = phases.get(k, 0.0) + v
+        if sum(times) > budget_s:
+            break
+    n = len(times)
+    return n, sum(times), {k: v / n for k, v in phases.items()}, energies
+
+
+# bounded sample of our line's cpu_baseline: whole steps at a reduced chain count (about 10-30 s)
+CPU_SAMPLE_CHAINS = {"resconv": 128, "rbm": 1024}
+
+
+def cpu_baseline(workload: str):
+    cores = _host_threads()
+    chains = CPU_SAMPLE_CHAINS[workload]
+    w = WORKLOADS[workload]
+    n, t, phases, _ = time_cpu_steps(workload, chains, 3, 15.0)
+    return {"value": n / t, "unit": UNIT, "cores": cores, "kind": "port", "scaled": False, "chains": chains,
+            "steps": n, "samples_per_s": n * chains / t,
+            "sample": (f"oracle/cpu_vmc.py: {n} whole SR step(s) of the workload on {chains} of its {w['chains']} "
+                       f"chains (sweep, local energies, O, Obar, Gram, FP64 Cholesky solve, update), "
+                       f"{t / n:.2f} s per step at that size; not scaled to the full workload"),
+            "phases_s": {k: round(v, 4) for k, v in phases.items()}}
 
 
 def run_reference(args, rank):
+    """The reference arm: whole SR steps of the CPU restatement at the full workload on all host
+    cores, as many of the requested steps as fit in --ref-budget seconds (at least one); the
+    line reports the steps actually timed."""
     if rank != 0:
         return
-    cb = cpu_baseline()
-    steps = max(1, args.steps)
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(WORKLOAD, parallelism="host cores"),
+    cores = _host_threads()
+    w = WORKLOADS[args.workload]
+    n, t, phases, energies = time_cpu_steps(args.workload, w["chains"], args.steps, args.ref_budget)
+    value = n / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": n, "warmup": 0, "ms_per_step": 1000.0 * t / n, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 model, f64 solve", "data": "synthetic", "config": dict(w),
+            "parallelism": f"host cores x{cores}",
+            "requested": {"steps": args.steps, "warmup": args.warmup,
+                          "note": (f"whole full-size steps only: {n} fit in the {args.ref_budget:.0f} s budget; "
+                                   "no warm-up step (each step is minutes of CPU work)")},
             "reference_jax": "unavailable on this box: quantax needs jax/equinox, not installed, no network",
-            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "scaled": False,
+                             "sample": (f"oracle/cpu_vmc.py: {n} whole SR step(s) of the full workload "
+                                        f"({w['chains']} chains), timed end to end"),
+                             "phases_s": {k: round(v, 3) for k, v in phases.items()}},
+            "samples_per_s": n * w["chains"] / t, "energies": energies,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-WORKLOAD_RESCONV = dict(workload="j1j2_square10_resconv8x16_minsr16384", lattice="Square(10) PBC, Sz=0",
-                        hamiltonian="Heisenberg(J=[1, 0.5], n_neighbor=[1, 2], msr=True)",
-                        model="ResConv(8 blocks, 16 channels, complex output)", nparams=34944,
-                        sampler="SpinExchange", chains=16384, proposals_per_sweep=200, thermal_proposals=200,
-                        solver="minnorm_shift_eig(ashift=1e-4) on the stacked [Re; Im] 32768 x 34944 matrix",
-                        l2="Obar (4.6 GB) and T (8.6 GB) exceed the 129 MB L2 every step")
-
-
 def build_workload(qtx, rank, gram, solve, workload="rbm", conv="fp32"):
-    import numpy as np
     from quantax_gb300 import replicas
+    import numpy as np
     qtx.set_random_seed(replicas.replica_seed(1234, rank))
     solver = qtx.optimizer.minnorm_shift_eig(ashift=1e-4, precision=solve)
     if workload == "resconv":
@@ -182,16 +264,15 @@ def build_workload(qtx, rank, gram, solve, workload="rbm", conv="fp32"):
     return state, sampler, opt
 
 
-def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32"):
-    """Warm-up + timed SR steps of one form; returns timings, phases, energies, e2e."""
+def run_form(args, rank, world, gram, solve, e2e_steps=0, clocks=None, conv="fp32"):
+    """Warm-up + timed SR steps of one form; returns timings, phases, energies and, when
+    e2e_steps > 0, the end-to-end time of that many steps through the public API."""
     import torch
-    import torch.distributed as dist
     import quantax_gb300 as qtx
     from quantax_gb300 import _lib, replicas
 
     state, sampler, opt = build_workload(qtx, rank, gram, solve, args.workload, conv)
     lr = 1e-2
-    energies = []
 
     def sr_step(ev=None):
         def mark(name):
@@ -249,12 +330,12 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
             prev = e
     phases = {k: v / args.steps for k, v in phases.items()}
     if "gram" in phases:
-        phases["cusolver_and_projection"] = phases.pop("solve")
-    energies = [float(x[0]) for x in stats]
+        phases["solve_and_projection"] = phases.pop("solve")
+    energies = [float(x[0]) for x in stats[args.warmup:]]
     out = dict(elapsed=elapsed, lat=lat, phases=phases, energies=energies, launches=launches, clocks=clk,
                nparams=state.nparams, fallbacks=opt.solve_fallbacks)
 
-    if e2e:
+    if e2e_steps > 0:
         # end to end through the public API with host buffers: parameters in from pinned host
         # memory, energy statistics and updated parameters back every step
         host_params = torch.empty(state.nparams, dtype=torch.float32).pin_memory()
@@ -266,7 +347,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        for _ in range(args.steps):
+        for _ in range(e2e_steps):
             state.params.copy_(host_params, non_blocking=True)
             state._refresh()
             sr_step()
@@ -276,8 +357,7 @@ def run_form(args, rank, world, gram, solve, e2e=True, clocks=None, conv="fp32")
             host_params.copy_(host_out)
         e1.record()
         torch.cuda.synchronize()
-        e2e_s = replicas.max_over_ranks(e0.elapsed_time(e1) / 1000.0, "cuda")
-        out["e2e_s"] = e2e_s
+        out["e2e_s"] = replicas.max_over_ranks(e0.elapsed_time(e1) / 1000.0, "cuda")
     return out
 
 
@@ -516,25 +596,29 @@ def percentile(lat, q):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--gram", default="3xtf32", choices=["fp32", "tf32", "bf16", "3xtf32"],
-                    help="plain-path Gram: split-TF32 on the tensor cores is FP32-class (accumulation error "
-                         "6.6e-6 against 8.2e-5 for fp32 on the CUDA cores)")
-    ap.add_argument("--solve", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--conv", default="fp32", choices=["fp32", "tf32", "bf16"],
-                    help="resconv: arithmetic of the convolutions of the main run")
+    ap.add_argument("--workload", default="resconv",
+                    choices=["resconv", "rbm", "serving", "trajectory", "heisenberg_tutorial", "j1j2_tutorial",
+                             "rbm_example"],
+                    help="resconv: J1-J2 10x10 with ResConv (the default line); rbm: chain-64 TFIM with RBM 256; "
+                         "serving: a Poisson stream of jobs through quantax_gb300.serving")
+    ap.add_argument("--gram", default=None, choices=["fp32", "tf32", "bf16", "3xtf32"],
+                    help="Gram of the plain method (default split-TF32 on the tensor cores, FP32-class: "
+                         "accumulation error 6.6e-6 against 8.2e-5 for fp32 on the CUDA cores)")
+    ap.add_argument("--solve", default=None, choices=["fp64", "mixed"], help="solve of the plain method")
+    ap.add_argument("--conv", default=None, choices=["fp32", "tf32", "bf16"],
+                    help="resconv: arithmetic of the plain method's convolutions")
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="steps of the end-to-end (host buffers) measurement; default min(steps, 5)")
+    ap.add_argument("--ref-budget", type=float, default=300.0,
+                    help="--impl reference: seconds of whole CPU steps to time (at least one step runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the precision form run")
+    ap.add_argument("--no-forms", action="store_true", help="skip the other forms")
     ap.add_argument("--tutorial-steps", type=int, default=200, help="*_tutorial: SR steps per phase")
     ap.add_argument("--seed", type=int, default=0, help="*_tutorial, rbm_example: random seed")
     ap.add_argument("--example-steps", type=int, default=1000, help="rbm_example: SR steps")
-    ap.add_argument("--workload", default="rbm",
-                    choices=["rbm", "resconv", "serving", "trajectory", "heisenberg_tutorial", "j1j2_tutorial",
-                             "rbm_example"],
-                    help="rbm: config 2 (the headline); resconv: config 3 (J1-J2 10x10, ResConv); "
-                         "serving: a Poisson stream of config-5 jobs through quantax_gb300.serving")
     ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
     ap.add_argument("--chains", type=int, default=2048, help="trajectory: Markov chains (samples per step)")
     ap.add_argument("--forms", default="plain:fp32:fp32:fp64,precision_bf16:bf16:bf16:mixed,"
@@ -547,6 +631,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.workload not in WORKLOADS:
+            raise SystemExit("--impl reference times the resconv and rbm workloads")
         run_reference(args, rank)
         return
 
@@ -572,71 +658,76 @@ def main():
         run_rbm_example(args, rank)
         return
 
-    plain = run_form(args, rank, world, args.gram, args.solve, e2e=True, clocks=Clocks(local) if rank == 0 else None,
-                     conv=args.conv)
+    wl = args.workload
+    _, conv0, gram0, solve0 = PLAIN[wl]
+    conv, gram, solve = args.conv or conv0, args.gram or gram0, args.solve or solve0
+    e2e_steps = min(args.steps, 5) if args.e2e_steps is None else args.e2e_steps
+    plain = run_form(args, rank, world, gram, solve, e2e_steps=e2e_steps,
+                     clocks=Clocks(local) if rank == 0 else None, conv=conv)
+    chains = WORKLOADS[wl]["chains"]
     forms = {}
     if not args.no_forms:
-        # precision forms, same seed: tcgen05 Gram (+ tensor-core convolutions for ResConv)
-        # and FP32 Cholesky with FP64 refinement
-        # accurate_*: the plain path's arithmetic (FP32 network, FP32-accurate split-TF32 Gram)
-        # with the FP64-refined solve in place of the FP64 factorisation
-        if args.workload == "resconv":
-            variants = [("accurate_fp32_conv_3xtf32_gram_mixed_solve", "fp32", "3xtf32"),
-                        ("precision_tf32_conv_tf32_gram_mixed_solve", "tf32", "tf32"),
-                        ("precision_bf16_conv_bf16_gram_mixed_solve", "bf16", "bf16")]
-        else:
-            variants = [("accurate_3xtf32_gram_mixed_solve", "fp32", "3xtf32"),
-                        ("precision_tf32_gram_mixed_solve", "fp32", "tf32")]
-        for name, conv, gram in variants:
-            prec = run_form(args, rank, world, gram, "mixed", e2e=False, conv=conv)
+        for name, fconv, fgram, fsolve in FORMS[wl]:
+            prec = run_form(args, rank, world, fgram, fsolve, conv=fconv)
             de = [abs(a - b) / abs(b) for a, b in zip(prec["energies"], plain["energies"])]
             forms[name] = {
-                "value": world * args.steps / prec["elapsed"], "unit": UNIT, "conv": conv, "gram": gram,
-                "solve": "mixed",
+                "value": world * args.steps / prec["elapsed"], "unit": UNIT,
+                "method": {"conv": fconv, "gram": fgram, "solve": fsolve},
                 "ms_per_step": 1000.0 * prec["elapsed"] / args.steps,
+                "samples_per_s": world * args.steps * chains / prec["elapsed"],
                 "p50_step_ms": percentile(prec["lat"], 0.5), "p99_step_ms": percentile(prec["lat"], 0.99),
                 "phases_ms": {k: round(v, 4) for k, v in prec["phases"].items()},
                 "speedup_vs_plain": plain["elapsed"] / prec["elapsed"],
                 "fp64_fallbacks": prec["fallbacks"],
+                "energies": [round(e, 6) for e in prec["energies"]],
                 "energy_rel_diff_vs_plain_max": max(de), "energy_rel_diff_vs_plain_last": de[-1]}
 
     if rank == 0:
         hbm, bf16, src = peaks()
         npar = plain["nparams"]
-        ns = 8192 if args.workload == "rbm" else 2 * 16384  # rows of the Gram matrix
+        ns = GRAM_ROWS[wl]
         phases = plain["phases"]
-        syrk_flop = float(ns) * (ns + 1) * npar  # lower triangle of T = Obar Obar^T, 2 flops per MAC
+        gram_flop = 2.0 * ns * ns * npar  # algorithmic: 2 Ns^2 Np (the symmetric half is not counted as saved)
         t_gram = phases.get("gram", float("nan")) / 1000.0
-        achieved = syrk_flop / t_gram / 1e12
-        rate = {"bf16": 1.0, "tf32": 0.5, "3xtf32": 0.5 / 3.0, "fp32": None}[args.gram]
-        traffic = GRAM_TRAFFIC_BYTES.get((args.workload, args.gram))
-        roof = {"kernel": f"qgx_gram {args.gram} (T = Obar Obar^T)", "bound": "tensor", "achieved": achieved,
-                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16, "peak_source": f"bf16 dense, {src}",
+        achieved = gram_flop / t_gram / 1e12
+        rate = {"bf16": 1.0, "tf32": 0.5, "3xtf32": 0.5 / 3.0, "fp32": None}[gram]
+        roof = {"kernel": f"gram_tc_kernel ({gram}, T = Obar Obar^T)", "bound": "tensor", "achieved": achieved,
+                "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                "peak_source": f"bf16 dense burst, {src} (MEASURED_PEAKS.json)",
                 "mode_peak": None if rate is None else bf16 * rate,
                 "frac_of_mode_peak": None if rate is None else achieved / (bf16 * rate),
-                "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
-                "algorithmic": f"Ns(Ns+1)Np = {syrk_flop:.3e} FLOP per launch (symmetric rank-k); operand "
-                               f"{ns * npar * 4:.3e} B read, T {ns * ns * 8:.3e} B written",
-                "note": ("the tensor-core Gram is our dominant kernel; cuSOLVER's FP64 factorisation (a library "
-                         "kernel) dominates the plain step. 3xtf32: each product is hi*hi + hi*lo + lo*hi, so its "
-                         "mode peak is a third of the TF32 rate")}
+                "traffic": GRAM_TRAFFIC_BYTES.get((wl, gram)), "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
+                "algorithmic": (f"2 Ns^2 Np = {gram_flop:.3e} FLOP per launch (Ns = {ns} rows, Np = {npar}); operand "
+                                f"{ns * npar * 4:.3e} B read, T {ns * ns * 8:.3e} B written"),
+                "duration": "CUDA events around the Gram phase (one launch) of every timed step, mean",
+                "note": ("split-TF32: each product is hi*hi + hi*lo + lo*hi, so its mode peak is a third of the TF32 "
+                         "rate" if gram == "3xtf32" else "")}
         elapsed = plain["elapsed"]
+        target = None
+        if forms:
+            best = max(forms, key=lambda k: forms[k]["speedup_vs_plain"])
+            target = {"form": best, "speedup_vs_plain": forms[best]["speedup_vs_plain"],
+                      "energy_rel_diff_vs_plain_max": forms[best]["energy_rel_diff_vs_plain_max"],
+                      "p99_step_ms": forms[best]["p99_step_ms"],
+                      "note": (f"over {args.steps} steps from identical initial parameters and seeds; the 200-step "
+                               "trajectory comparison is `--workload trajectory`")}
         line = {
             "metric": METRIC, "value": world * args.steps / elapsed, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 solve)",
-            "data": "synthetic",
-            "config": dict(WORKLOAD if args.workload == "rbm" else WORKLOAD_RESCONV, parallelism=f"replicas x{world}",
-                           gram=args.gram, solve=args.solve, **({"conv": args.conv} if args.workload == "resconv" else {})),
-            "samples_per_s": world * args.steps * (8192 if args.workload == "rbm" else 16384) / elapsed, "p50_step_ms": percentile(plain["lat"], 0.5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 solve)",
+            "data": "synthetic", "config": dict(WORKLOADS[wl]), "parallelism": f"replicas x{world}",
+            "method": {"conv": conv if wl == "resconv" else None, "gram": gram, "solve": solve},
+            "samples_per_s": world * args.steps * chains / elapsed, "p50_step_ms": percentile(plain["lat"], 0.5),
             "p99_step_ms": percentile(plain["lat"], 0.99),
             "phases_ms": {k: round(v, 4) for k, v in phases.items()}, "energy": plain["energies"][-1],
-            "e2e": {"value": world * args.steps / plain["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": npar * 4,
-                    "d2h_bytes_per_step": npar * 4 + 24},
+            "energies": [round(e, 6) for e in plain["energies"]],
+            "e2e": {"value": world * e2e_steps / plain["e2e_s"], "unit": UNIT, "steps": e2e_steps,
+                    "h2d_bytes_per_step": npar * 4, "d2h_bytes_per_step": npar * 4 + 24},
             "gpu_launches": plain["launches"], "roofline": roof, "clocks": plain["clocks"], "forms": forms,
+            "target": target,
         }
-        if not args.no_cpu_baseline and args.workload == "rbm":
-            line["cpu_baseline"] = cpu_baseline()
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(wl)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

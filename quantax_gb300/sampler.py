@@ -240,18 +240,34 @@ class Metropolis(Sampler):
 
     def _check_local_updates(self) -> None:
         """metropolis.py:201-213: after a sweep by local updates, log|psi| is evaluated again by a
-        direct forward; a warning names how many samples differ (neither |psi_l - psi_d| < 1e-8
-        nor |psi_l / psi_d - 1| < 1e-3), and the direct values replace the local ones. Reading
-        the count synchronises the host with the sweep, as the reference's check does."""
+        direct forward and the direct values replace the local ones; the number of samples that
+        differ (neither |psi_l - psi_d| < 1e-8 nor |psi_l / psi_d - 1| < 1e-3) is copied to the
+        host without stalling it and reported by a warning when it is read: at the start of the
+        next sweep, or by check_local_updates()."""
         direct = self._state.log_psi_packed(self._packed)
         if not hasattr(self, "_mismatch"):
             self._mismatch = torch.zeros(1, dtype=torch.int32, device=self._log_psi.device)
+            self._mismatch_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self.check_local_updates()  # a previous count still in flight is read first
         _lib.call("qgx_log_psi_mismatch", _lib.ptr(self._log_psi), _lib.ptr(direct), self._nsamples,
                   _lib.ptr(self._mismatch), _lib.ptr(self._log_psi), _lib.stream_ptr())
-        ndiff = int(self._mismatch.item())
+        self._mismatch_host.copy_(self._mismatch, non_blocking=True)
+        self._mismatch_event = torch.cuda.Event()
+        self._mismatch_event.record()
+
+    def check_local_updates(self) -> int:
+        """Wait for the last sweep's psi check and warn if samples differed; returns their number
+        (0 when no check is pending)."""
+        ev = getattr(self, "_mismatch_event", None)
+        if ev is None:
+            return 0
+        ev.synchronize()
+        self._mismatch_event = None
+        ndiff = int(self._mismatch_host[0])
         if ndiff > 0:
             warnings.warn(f"{ndiff} out of {self._nsamples} wavefunctions are not close in direct forward pass and "
                           "local updates. This may indicate inaccurate local updates.")
+        return ndiff
 
     def _run_proposals(self, n: int) -> None:
         self._device_sweep(n, self._step, self.proposal, self._nbr, self._z, self._hop)

@@ -11,6 +11,14 @@ server reports per-step latency percentiles, jobs/s and aggregate samples/s.
 
 A job's result does not depend on the mix: its random numbers come from its own seed
 stream (Philox counters keyed per job) and every reduction has a fixed order.
+
+Failures stay with the job that has them (the reference's own guard is the skipped
+non-finite update, quantax/state/variational.py:570-573): a spec that cannot run is refused at
+submission with a "rejected: ..." status, a job whose parameters or energy turn non-finite is
+retired with a "failed: ..." status (checked without stalling the other jobs: the energy of a
+step is read once that step's end event has completed), and cancel(name) retires a job at its
+next step boundary with the status "cancelled". Every retired job releases its memory; the
+other jobs run on unchanged.
 """
 from __future__ import annotations
 
@@ -44,6 +52,31 @@ class JobSpec:
     gram: str = "bf16"        # Gram matrix arithmetic: "fp32", "tf32", "bf16" or "3xtf32"
     solve: str = "fp64"
     arrival: float = 0.0      # seconds after the server starts
+    init_params: Optional[np.ndarray] = None  # host parameters to start from (default: the model's init)
+
+    def validate(self) -> None:
+        """Raise ValueError when the job cannot run."""
+        if self.kind not in ("tfim", "j1j2"):
+            raise ValueError(f"unknown job kind {self.kind!r}")
+        if self.nsamples <= 0 or self.steps <= 0:
+            raise ValueError("nsamples and steps must be positive")
+        if self.kind == "tfim" and not (2 <= self.L <= 128 and self.alpha >= 1):
+            raise ValueError(f"tfim chain length {self.L} / alpha {self.alpha} outside 2..128 / >= 1")
+        if self.kind == "j1j2":
+            if not (3 <= self.L <= 16) or (self.L * self.L) % 2:
+                raise ValueError(f"j1j2 needs an even number of sites on an L x L square, 3 <= L <= 16, got {self.L}")
+            if not (1 <= self.blocks <= 16) or self.channels not in (2, 4, 6, 8, 10, 12, 14, 16):
+                raise ValueError(f"ResConv with {self.blocks} blocks / {self.channels} channels is not supported")
+        if self.conv not in ("fp32", "tf32", "bf16") or self.gram not in ("fp32", "tf32", "bf16", "3xtf32"):
+            raise ValueError(f"arithmetic conv={self.conv!r} gram={self.gram!r} not supported")
+        if self.solve not in ("fp64", "fp64_lib", "mixed"):
+            raise ValueError(f"solve {self.solve!r} not supported")
+        if self.init_params is not None:
+            p = np.asarray(self.init_params)
+            if p.shape != (self.nparams(),):
+                raise ValueError(f"init_params has shape {p.shape}, the model has {self.nparams()} parameters")
+            if not np.all(np.isfinite(p)):
+                raise ValueError("init_params holds non-finite values")
 
     def nparams(self) -> int:
         if self.kind == "tfim":
@@ -100,8 +133,14 @@ class Job:
                 self.sampler = qtx.sampler.SpinExchange(self.state, spec.nsamples, thermal_steps=n, sweep_steps=n)
             else:
                 raise ValueError(spec.kind)
+            if spec.init_params is not None:
+                self.state.set_params(torch.as_tensor(np.asarray(spec.init_params, dtype=np.float32)))
+                self.sampler.reset()
             self.opt = qtx.optimizer.SR(self.state, H, solver=solver, gram=spec.gram)
             global_defs.set_default_dtype(np.float64)
+        self.status = "ok"
+        self._checked = 0  # steps whose energy has been checked for finiteness
+        self._host_energy: List[torch.Tensor] = []
 
     @property
     def done(self) -> bool:
@@ -117,16 +156,32 @@ class Job:
             step = self.opt.get_step(samples)
             self.state.update(step * self.spec.lr)
             self.stats.append(self.opt.stats.clone())
+            host = torch.empty(1, dtype=torch.float64).pin_memory()
+            host.copy_(self.stats[-1][:1], non_blocking=True)  # the energy, read once e1 has completed
+            self._host_energy.append(host)
             e1.record()
             self._events.append((e0, e1))
         self.step_index += 1
+
+    def poll_finite(self) -> bool:
+        """Check the energies of the steps that have completed on the device (no waiting);
+        False once one is not finite (the job's status then says which step)."""
+        while self._checked < len(self._events) and self._events[self._checked][1].query():
+            e = float(self._host_energy[self._checked][0])
+            if not np.isfinite(e):
+                self.status = f"failed: non-finite energy at step {self._checked}"
+                return False
+            self._checked += 1
+        return True
 
     def finish(self) -> dict:
         self.stream.synchronize()
         self.latencies = [a.elapsed_time(b) for a, b in self._events]
         energies = [float(x[0]) for x in self.stats]
-        return {"name": self.spec.name, "energies": energies, "latencies_ms": self.latencies,
-                "samples": self.spec.nsamples * self.spec.steps}
+        if self.status == "ok" and not all(np.isfinite(energies)):
+            self.status = f"failed: non-finite energy at step {int(np.argmin(np.isfinite(energies)))}"
+        return {"name": self.spec.name, "status": self.status, "energies": energies,
+                "latencies_ms": self.latencies, "samples": self.spec.nsamples * len(energies)}
 
 
 @dataclass(order=True)
@@ -147,21 +202,47 @@ class VMCServer:
         self.max_active = max_active
         self._pending: List[_Pending] = []
         self._order = 0
+        self._rejected: List[dict] = []
+        self._cancel = set()
 
-    def submit(self, spec: JobSpec) -> None:
+    def submit(self, spec: JobSpec) -> str:
+        """Queue a job; returns "queued", or "rejected: <reason>" for a spec that cannot run
+        (the job then appears in run()'s results with that status). A job larger than the whole
+        budget raises ValueError: no admission order could ever run it."""
+        try:
+            spec.validate()
+        except ValueError as e:
+            status = f"rejected: {e}"
+            self._rejected.append({"name": spec.name, "status": status, "energies": [], "latencies_ms": [],
+                                   "samples": 0})
+            return status
         if spec.hbm_bytes() > self.budget:
             raise ValueError(f"job {spec.name} needs ~{spec.hbm_bytes() >> 20} MiB, above the whole budget")
         heapq.heappush(self._pending, _Pending(spec.arrival, self._order, spec))
         self._order += 1
+        return "queued"
 
-    def run(self) -> dict:
-        """Serve every submitted job; returns per-job results and aggregate figures."""
+    def cancel(self, name: str) -> None:
+        """Retire the job at its next step boundary (or drop it if it has not started)."""
+        self._cancel.add(name)
+
+    def run(self, on_round=None) -> dict:
+        """Serve every submitted job; returns per-job results and aggregate figures.
+        on_round(server, active_jobs), if given, runs after every round of step launches."""
         active: List[Job] = []
         used = 0
-        results = []
+        results = list(self._rejected)
+        self._rejected = []
         t0 = time.perf_counter()
         streams: List[torch.cuda.Stream] = []
         while self._pending or active:
+            for p in [p for p in self._pending if p.spec.name in self._cancel]:
+                self._pending.remove(p)
+                results.append({"name": p.spec.name, "status": "cancelled", "energies": [], "latencies_ms": [],
+                                "samples": 0})
+            heapq.heapify(self._pending)
+            if not self._pending and not active:
+                break
             now = time.perf_counter() - t0
             # admit arrived jobs while memory and slots allow (in arrival order)
             while (self._pending and self._pending[0].arrival <= now and len(active) < self.max_active
@@ -177,9 +258,15 @@ class VMCServer:
                 continue
             for job in active:
                 job.step()
+            if on_round is not None:
+                on_round(self, active)
             still = []
             for job in active:
-                if job.done:
+                if job.spec.name in self._cancel:
+                    job.status = "cancelled"
+                elif not job.poll_finite():
+                    pass  # status says which step
+                if job.done or job.status != "ok":
                     results.append(job.finish())
                     used -= job.used
                     streams.append(job.stream)
@@ -189,9 +276,10 @@ class VMCServer:
             active = still
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        lat = sorted(x for r in results for x in r["latencies_ms"])
+        done = [r for r in results if r["status"] == "ok"]
+        lat = sorted(x for r in done for x in r["latencies_ms"])
         pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))] if lat else None
-        return {"jobs": results, "wall_s": wall, "jobs_per_s": len(results) / wall,
+        return {"jobs": results, "wall_s": wall, "jobs_per_s": len(done) / wall,
                 "samples_per_s": sum(r["samples"] for r in results) / wall,
                 "p50_step_ms": pct(0.5), "p99_step_ms": pct(0.99), "steps": len(lat)}
 

@@ -311,7 +311,8 @@ def test_psi_consistency_check_after_local_updates(cuda):
     """Metropolis.sweep's check (metropolis.py:201-213): log|psi| carried through the sweep's
     local updates agrees with a direct forward, so a normal sweep warns about nothing; a sweep
     whose updates ran on a perturbed copy of the table (inaccurate local updates) warns with the
-    number of samples that differ, and its samples carry the direct values."""
+    number of samples that differ when the count is read, and its samples carry the direct
+    values."""
     import warnings
     import quantax_gb300 as qtx
     qtx.sites.Chain(16)
@@ -321,14 +322,16 @@ def test_psi_consistency_check_after_local_updates(cuda):
     with warnings.catch_warnings():
         warnings.simplefilter("error")
         samples = sampler.sweep()
+        assert sampler.check_local_updates() == 0
     assert torch.equal(samples.log_psi, state.log_psi_packed(samples.packed))
     model = state.model
     sweep = model.sweep
     bad = state.table.clone() * 1.05
     model.sweep = lambda table, *args: sweep(bad, *args)
     try:
+        samples = sampler.sweep()
         with pytest.warns(UserWarning, match=r"\d+ out of 128 wavefunctions are not close"):
-            samples = sampler.sweep()
+            assert sampler.check_local_updates() > 0
     finally:
         del model.sweep
     assert torch.equal(samples.log_psi, state.log_psi_packed(samples.packed))

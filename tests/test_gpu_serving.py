@@ -47,3 +47,44 @@ def test_serving_admission_by_budget(cuda):
     assert sorted(j["name"] for j in out["jobs"]) == sorted(s.name for s in specs)
     with pytest.raises(ValueError):
         VMCServer(hbm_budget_bytes=1).submit(specs[0])
+
+
+def test_failures_stay_with_their_job(cuda):
+    """An invalid spec is rejected at submission, a job whose host parameter buffer has a NaN
+    written into it before admission fails at its first step, a job cancelled mid-run retires
+    at the next step boundary; the other jobs' energies equal their runs alone."""
+    from quantax_gb300.serving import JobSpec, VMCServer
+    good = _specs()
+    alone = {}
+    for spec in good:
+        srv = VMCServer(max_active=1)
+        srv.submit(spec)
+        alone[spec.name] = srv.run()["jobs"][0]["energies"]
+    bad_kind = JobSpec("bad_kind", "kagome", 6, 256, 3, seed=1)
+    bad_size = JobSpec("bad_size", "j1j2", 5, 256, 3, seed=2)  # 25 sites: no Sz = 0 sector
+    params = np.full(JobSpec("x", "tfim", 16, 256, 4, seed=3, alpha=1).nparams(), 0.01)
+    nan_job = JobSpec("nan_params", "tfim", 16, 256, 4, seed=3, alpha=1, init_params=params, arrival=0.02)
+    doomed = JobSpec("cancelled", "j1j2", 4, 256, 6, seed=4, blocks=2, channels=8)
+    srv = VMCServer(max_active=6)
+    assert srv.submit(bad_kind).startswith("rejected")
+    assert srv.submit(bad_size).startswith("rejected")
+    for spec in good + [nan_job, doomed]:
+        assert srv.submit(spec) == "queued"
+    params[5] = np.nan  # written into the job's host buffer after submission
+
+    def on_round(server, active):
+        for job in active:
+            if job.spec.name == "cancelled" and job.step_index == 2:
+                server.cancel("cancelled")
+
+    out = srv.run(on_round=on_round)
+    res = {j["name"]: j for j in out["jobs"]}
+    assert set(res) == {s.name for s in good} | {"bad_kind", "bad_size", "nan_params", "cancelled"}
+    assert res["bad_kind"]["status"].startswith("rejected: unknown job kind")
+    assert res["bad_size"]["status"].startswith("rejected: j1j2 needs an even number of sites")
+    assert res["nan_params"]["status"].startswith("failed: non-finite energy")
+    assert res["cancelled"]["status"] == "cancelled" and len(res["cancelled"]["energies"]) == 2
+    for spec in good:
+        j = res[spec.name]
+        assert j["status"] == "ok"
+        assert np.all(np.abs(np.array(j["energies"]) - np.array(alone[spec.name])) <= 1e-12 * np.abs(alone[spec.name]))

@@ -32,7 +32,9 @@ class Solver:
     rtol: Optional[float] = None
     atol: float = 0.0
     tol_snr: float = 0.0
-    precision: str = "fp64"   # "fp64" or "mixed" (FP32 Cholesky + FP64 refinement, shift only)
+    # shift solvers: "fp64" (this library's FP64 Cholesky, tensor-core trailing updates),
+    # "fp64_lib" (cuSOLVER's FP64 Cholesky) or "mixed" (FP32 Cholesky + FP64 refinement)
+    precision: str = "fp64"
     diag_shift: float = 0.0   # shift_cg: relative diagonal shift
     maxiter: Optional[int] = None  # shift_cg: iteration limit (default 10 Np, as jax's cg)
     blocks: Optional[tuple] = None  # block_pinv_eig: parameter counts of the layers
@@ -59,13 +61,19 @@ def lstsq_pinv_eig(rtol: Optional[float] = None, atol: float = 0.0, tol_snr: flo
 
 
 def auto_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4, precision: str = "fp64") -> Solver:
-    """solver.py:80-91. precision="mixed" factors in FP32 and refines the solution in FP64
-    (MinSR branch); it falls back to the FP64 factorisation when the refinement stalls."""
+    """solver.py:80-91. precision="fp64": the FP64 Cholesky of qgx_cholesky (FP64 diagonal
+    blocks, exact tensor-core trailing updates); "fp64_lib": cuSOLVER's FP64 Cholesky;
+    "mixed" factors in FP32 and refines the solution in FP64 (MinSR branch), falling back to
+    the FP64 factorisation when the refinement stalls."""
+    if precision not in ("fp64", "fp64_lib", "mixed"):
+        raise ValueError(f"precision {precision!r}: expected 'fp64', 'fp64_lib' or 'mixed'")
     return Solver("shift", "auto", rshift=rshift, ashift=ashift, precision=precision)
 
 
 def minnorm_shift_eig(rshift: Optional[float] = None, ashift: float = 1e-4, precision: str = "fp64") -> Solver:
     """solver.py:50-62 (see auto_shift_eig for precision)"""
+    if precision not in ("fp64", "fp64_lib", "mixed"):
+        raise ValueError(f"precision {precision!r}: expected 'fp64', 'fp64_lib' or 'mixed'")
     return Solver("shift", "minnorm", rshift=rshift, ashift=ashift, precision=precision)
 
 
@@ -271,7 +279,9 @@ class QNGD:
     def _solve_matrix(self, A: torch.Tensor, b: torch.Tensor, sv: Solver) -> torch.Tensor:
         """The pinv / shift solvers on the real matrix A and right-hand side b."""
         ns, np_ = A.shape
-        method = _lib.SOLVE_SHIFT if sv.kind == "shift" else _lib.SOLVE_PINV
+        method = _lib.SOLVE_PINV
+        if sv.kind == "shift":
+            method = _lib.SOLVE_SHIFT_LIB if sv.precision == "fp64_lib" else _lib.SOLVE_SHIFT
         rshift = _OBAR_RTOL if sv.rshift is None else sv.rshift
         rtol = _OBAR_RTOL if sv.rtol is None else sv.rtol
         x = torch.empty(np_, dtype=torch.float64, device=A.device)
@@ -474,10 +484,10 @@ class MARCH(_MomentumSR):
     def solve(self, Obar: torch.Tensor, Ebar: torch.Tensor) -> torch.Tensor:
         self._t += 1
         Ebar = Ebar.to(torch.float64) - self._mu * self._obar_dot(Obar, self._last_step)
-        if bool(torch.allclose(self._V, torch.zeros_like(self._V))):
-            V = torch.ones_like(self._V)
-        else:
-            V = (self._V / (1.0 - self._beta ** self._t)) ** 0.25 + 1e-8
+        # the reference's allclose(V, 0) test (|V| <= 1e-8 everywhere) selected on the device,
+        # so the step enqueues without waiting for the device
+        unset = (self._V.abs() <= 1e-8).all()
+        V = torch.where(unset, torch.ones_like(self._V), (self._V / (1.0 - self._beta ** self._t)) ** 0.25 + 1e-8)
         self._scale_columns(Obar, 1.0 / V)
         step = super().solve(Obar, Ebar)
         step = step / V + self._mu * self._last_step

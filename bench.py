@@ -61,7 +61,8 @@ FORMS = {
     "resconv": [("accurate_fp32_conv_3xtf32_gram_mixed_solve", "fp32", "3xtf32", "mixed"),
                 ("precision_tf32_conv_tf32_gram_mixed_solve", "tf32", "tf32", "mixed"),
                 ("precision_bf16_conv_bf16_gram_mixed_solve", "bf16", "bf16", "mixed")],
-    "rbm": [("accurate_3xtf32_gram_mixed_solve", "fp32", "3xtf32", "mixed"),
+    "rbm": [("plain_with_cusolver_fp64_factor", "fp32", "3xtf32", "fp64_lib"),
+            ("accurate_3xtf32_gram_mixed_solve", "fp32", "3xtf32", "mixed"),
             ("precision_tf32_gram_mixed_solve", "fp32", "tf32", "mixed")],
 }
 
@@ -607,7 +608,8 @@ def main():
     ap.add_argument("--gram", default=None, choices=["fp32", "tf32", "bf16", "3xtf32"],
                     help="Gram of the plain method (default split-TF32 on the tensor cores, FP32-class: "
                          "accumulation error 6.6e-6 against 8.2e-5 for fp32 on the CUDA cores)")
-    ap.add_argument("--solve", default=None, choices=["fp64", "mixed"], help="solve of the plain method")
+    ap.add_argument("--solve", default=None, choices=["fp64", "fp64_lib", "mixed"],
+                    help="solve of the plain method: fp64 (qgx_cholesky), fp64_lib (cuSOLVER Xpotrf), mixed")
     ap.add_argument("--conv", default=None, choices=["fp32", "tf32", "bf16"],
                     help="resconv: arithmetic of the plain method's convolutions")
     ap.add_argument("--e2e-steps", type=int, default=None,

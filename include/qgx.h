@@ -40,7 +40,10 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
 #define QGX_PROPOSAL_LOCAL_FLIP 0    /* quantax.sampler.LocalFlip */
 #define QGX_PROPOSAL_SPIN_EXCHANGE 1 /* quantax.sampler.SpinExchange */
 
-#define QGX_SOLVE_SHIFT 0  /* diagonal-shifted Cholesky (minnorm_shift_eig) */
+/* diagonal-shifted Cholesky (minnorm_shift_eig): this library's FP64 factorisation (FP64
+ * diagonal blocks and triangular solves, every trailing update an exact BF16-digit product on
+ * the tensor cores; see qgx_cholesky) */
+#define QGX_SOLVE_SHIFT 0
 #define QGX_SOLVE_PINV 1   /* soft pseudo-inverse via eigh (minnorm_pinv_eig) */
 /* diagonal-shifted system solved by FP64 conjugate gradients preconditioned with the FP32
  * Cholesky factor of the shifted matrix (cuSOLVER, BF16x9-emulated FP32); when that factor
@@ -48,6 +51,8 @@ typedef struct CUstream_st* qgx_stream_t; /* == cudaStream_t */
  * info = -1 when the true FP64 residual stays above 1e-10 relative after 100 iterations
  * (the caller then falls back to QGX_SOLVE_SHIFT) */
 #define QGX_SOLVE_SHIFT_MIXED 2
+/* as QGX_SOLVE_SHIFT with cuSOLVER's FP64 Xpotrf (FP64 pipe) as the factorisation */
+#define QGX_SOLVE_SHIFT_LIB 3
 
 #define QGX_GRAM_FP32 0    /* FP32 SIMT FMA, FP32 accumulation */
 #define QGX_GRAM_TF32 1    /* tcgen05 kind::tf32, FP32 accumulation in TMEM */
@@ -414,6 +419,23 @@ int64_t qgx_last_solve_kernels(void);
 int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda,
                  const double* b, int32_t method, double rshift, double ashift,
                  double rtol, double atol, double tol_snr, double* x, int32_t* info,
+                 void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+
+/* FP64 Cholesky factorisation A = L L^T of a symmetric positive definite n x n matrix
+ * (row-major, leading dimension lda; the factor step of minnorm_shift_eig / lstsq_shift_eig,
+ * quantax/optimizer/solver.py:50-91, jax.scipy.linalg.solve(assume_a="pos")). L overwrites the
+ * lower triangle (L[i][j] at A[i lda + j], i >= j); the strict upper triangle keeps the input.
+ * Read as column-major, the result is the upper factor U = L^T (A = U^T U) that cuSOLVER's
+ * potrs takes with CUBLAS_FILL_MODE_UPPER. 64 x 64 diagonal blocks and their triangular solves
+ * run in FP64; every update C -= P P^T (P a 64- or 256-column panel) runs on the tensor cores
+ * as an exact product of 8 BF16 digit slices per element (row-scaled 57-bit fixed point,
+ * integer accumulation exact in FP32), folded in int64 and applied in FP64.
+ * info (device int): 0, or the order of the first leading minor that is not positive
+ * definite. status (device int, may be NULL): QGX_ERR_TIMEOUT if a tensor-core wait ran out
+ * (the factor is then invalid). Workspace: qgx_cholesky_workspace_bytes(n), 256-byte
+ * aligned; no counterpart in the reference beyond the factorisation it calls. */
+int64_t qgx_cholesky_workspace_bytes(int64_t n);
+int qgx_cholesky(double* A, int64_t n, int64_t lda, int32_t* info, int32_t* status,
                  void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
 
 /* Real-time evolution's S-path (quantax/optimizer/time_evol.py:55-134):

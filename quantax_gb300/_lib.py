@@ -25,6 +25,7 @@ PROPOSAL_SPIN_EXCHANGE = 1
 SOLVE_SHIFT = 0
 SOLVE_PINV = 1
 SOLVE_SHIFT_MIXED = 2
+SOLVE_SHIFT_LIB = 3
 GRAM_FP32 = 0
 GRAM_TF32 = 1
 GRAM_BF16 = 2
@@ -132,6 +133,8 @@ SIGNATURES = {
     "qgx_sr_solve": (C.c_int, [vp, i64, vp, i64, i64, vp, i32, f64, f64, f64, f64, f64, vp, vp, vp, i64, vp]),
     "qgx_apply_update": (C.c_int, [vp, vp, i64, vp, vp]),
     "qgx_log_psi_mismatch": (C.c_int, [vp, vp, i64, vp, vp, vp]),
+    "qgx_cholesky_workspace_bytes": (i64, [i64]),
+    "qgx_cholesky": (C.c_int, [vp, i64, i64, vp, vp, vp, i64, vp]),
 }
 
 

@@ -1,0 +1,500 @@
+// FP64 Cholesky factorisation A = L L^T for the diagonal-shifted MinSR / SR solves
+// (quantax/optimizer/solver.py:50-62: jax.scipy.linalg.solve(T + shift, b, assume_a="pos")).
+//
+// A is n x n, symmetric, row-major with leading dimension lda. L overwrites the lower triangle
+// (L[i][j] at A[i lda + j], i >= j); the strict upper triangle is not touched, so it still
+// holds the matrix by symmetry. Read as column-major, the factor is the upper triangle
+// U = L^T with A = U^T U.
+//
+// FP64 arithmetic runs at about two FMAs per clock per SM on GB300, so only the O(n^2 b) part
+// of the work runs on the FP64 pipe: right-looking, 256-column panels, each factored as four
+// 64-column blocks (potrf of the 64 x 64 diagonal block and the 64-wide triangular solve of
+// every row below it, in FP64). Every update of the form C -= P P^T runs on the tensor cores
+// as an exact integer product (the Ozaki scheme: Ozaki, Ogita, Oishi and Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59, 2012):
+//   * each row r of the panel P (K <= 256 columns) is scaled by 2^-e_r, e_r the exponent with
+//     max_k |P_rk| < 2^e_r, and rounded to the integer F = round(P 2^(56 - e_r)), |F| <= 2^56;
+//   * F is written as 8 balanced base-128 digits S_0 .. S_7 (|S_0| <= 128, S_t in [-64, 64)
+//     for t >= 1), each exact in BF16; P_rk = 2^e_r sum_t S_t[r][k] 2^(-7(t+1)) up to 2^(e_r-57);
+//   * for each level l = t + u <= 7 the tensor core accumulates I_l = sum_(t+u=l) S_t S_u^T
+//     over K in FP32: every product is an integer below 2^14 in magnitude and every partial
+//     sum an integer below 2^24 (at most 8 pairs, K <= 256), so the FP32 accumulation is exact;
+//   * the epilogue forms V = sum_l I_l 2^(38 - 7 l) exactly in int64 (levels 6 and 7 rounded
+//     to 2^-38), converts once to FP64 and subtracts 2^(e_i + e_j - 52) V from C_ij.
+// The products with t + u >= 8 are dropped: with the digits' own truncation the update's error
+// is a few 2^-56 K 2^(e_i + e_j), below FP64's own rounding of a K-term dot product.
+//
+// The tensor-core kernel: one CTA per 128 x 64 tile of C on or below the diagonal; warp 4
+// loads the 8 digit slices of the tile's 128 A rows and 64 B rows, 32 K-elements per stage
+// (3D TMA box, 64-byte swizzle, two stages); warp 5 issues the 36 tcgen05.mma (M 128, N 64,
+// K 16, BF16 -> FP32) of each 16-element K step into the eight 64-column level accumulators
+// (all 512 TMEM columns); warps 0-3 read the levels back, fold them in int64 and apply the
+// update to C through a shared-memory transpose (coalesced row writes). Every mbarrier wait is
+// bounded (2 s); a wait that runs out records QGX_ERR_TIMEOUT, the CTA frees its TMEM and
+// leaves C alone.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "qgx_common.cuh"
+#include "qgx_tc.cuh"
+
+namespace qgx {
+namespace {
+
+constexpr int kPanel = 256;                     // columns of one tensor-core trailing update
+constexpr int kBlk = 64;                        // columns of one FP64 diagonal block
+constexpr int kSlices = 8;                      // BF16 digits per element
+constexpr int kFixBits = 56;                    // kSlices * 7 fraction bits of the sliced rows
+constexpr int kOzM = 128, kOzN = 64, kOzKB = 32;  // tile rows, tile columns, K per stage
+constexpr int kOzStages = 2;
+constexpr int kOzABytes = kSlices * kOzM * kOzKB * 2;  // 64 KB
+constexpr int kOzBBytes = kSlices * kOzN * kOzKB * 2;  // 32 KB
+constexpr int kOzStageBytes = kOzABytes + kOzBBytes;
+constexpr int kOzThreads = 192;
+constexpr size_t kOzSmem = 1024 + (size_t)kOzStages * kOzStageBytes + 256;
+constexpr uint32_t kOzTmemCols = 512;  // eight 64-column FP32 level accumulators
+constexpr int kOzDLd = kOzN + 1;       // doubles per row of the epilogue's transpose tile
+
+inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
+
+// ---- digit slices ---------------------------------------------------------------------------
+// Rows [0, m) of a K-column panel (row r at A + (row0 + r) lda + col0): exponent e_r and the
+// 8 BF16 digit slices S[t][r][k] (slice-major, row stride K). One warp per row.
+__global__ void slice_rows_kernel(const double* __restrict__ A, int64_t lda, int64_t row0, int64_t col0, int64_t m,
+                                  int K, __nv_bfloat16* __restrict__ S, int* __restrict__ ex) {
+  const int64_t r = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= m) return;  // whole warps
+  const double* a = A + (row0 + r) * lda + col0;
+  double mx = 0.0;
+  for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(a[k]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1): every |a_k| < 2^e
+  if (lane == 0) ex[r] = e;
+  for (int k = lane; k < K; k += 32) {
+    long long F = __double2ll_rn(ldexp(a[k], kFixBits - e));  // exact scaling, |F| <= 2^56
+#pragma unroll
+    for (int t = kSlices - 1; t >= 1; --t) {
+      const long long d = ((F + 64) & 127) - 64;  // balanced digit in [-64, 64)
+      S[((int64_t)t * m + r) * K + k] = __float2bfloat16_rn((float)d);
+      F = (F - d) >> 7;                           // exact
+    }
+    S[(int64_t)r * K + k] = __float2bfloat16_rn((float)F);  // |S_0| <= 128
+  }
+}
+
+// ---- FP64 diagonal block and triangular solve -----------------------------------------------
+// Cholesky of the nb x nb (nb <= 64) diagonal block at (c, c), in place. The first pivot that is
+// not positive sets *info = c + k + 1 (the order of the failing leading minor, as LAPACK and
+// cuSOLVER report it); the factorisation carries on with a NaN pivot.
+__global__ void __launch_bounds__(256) potrf_block_kernel(double* __restrict__ A, int64_t lda, int64_t c, int nb,
+                                                          int* __restrict__ info) {
+  __shared__ double a[kBlk][kBlk + 1];
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e - i * nb;
+    if (j <= i) a[i][j] = A[(c + i) * lda + c + j];
+  }
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (threadIdx.x == 0) {
+      double d = a[k][k];
+      if (!(d > 0.0)) {
+        atomicCAS(info, 0, (int)(c + k + 1));
+        d = __longlong_as_double(0x7FF8000000000000LL);
+      }
+      a[k][k] = sqrt(d);
+    }
+    __syncthreads();
+    const double inv = 1.0 / a[k][k];
+    for (int i = k + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][k] *= inv;
+    __syncthreads();
+    const int r = nb - k - 1;
+    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+      const int i = k + 1 + e / r, j = k + 1 + e % r;
+      if (j <= i) a[i][j] = fma(-a[i][k], a[j][k], a[i][j]);
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e - i * nb;
+    if (j <= i) A[(c + i) * lda + c + j] = a[i][j];
+  }
+}
+
+// rows [r0, n) of the 64 columns at c: x L_cc^T = a with L_cc the factored diagonal block, in
+// place (reference BLAS dtrsm 'R','L','T','N' order: scale by the pivot's reciprocal, then
+// update the later columns). One thread per row, the row in registers, L_cc in shared memory.
+__global__ void __launch_bounds__(128) trsm_block_kernel(double* __restrict__ A, int64_t lda, int64_t c, int64_t r0,
+                                                         int64_t n) {
+  __shared__ double l[kBlk][kBlk + 1];
+  __shared__ double dinv[kBlk];
+  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) {
+    const int i = e / kBlk, j = e % kBlk;
+    l[i][j] = j <= i ? A[(c + i) * lda + c + j] : 0.0;
+  }
+  if (threadIdx.x < kBlk) dinv[threadIdx.x] = 1.0 / A[(c + threadIdx.x) * lda + c + threadIdx.x];
+  __syncthreads();
+  const int64_t r = r0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double* row = A + r * lda + c;
+  double x[kBlk];
+#pragma unroll
+  for (int k = 0; k < kBlk; ++k) x[k] = row[k];
+#pragma unroll
+  for (int k = 0; k < kBlk; ++k) {
+    x[k] *= dinv[k];
+#pragma unroll
+    for (int i = k + 1; i < kBlk; ++i) x[i] = fma(-x[k], l[i][k], x[i]);
+  }
+#pragma unroll
+  for (int k = 0; k < kBlk; ++k) row[k] = x[k];
+}
+
+// ---- tensor-core update C -= P P^T (lower part) ----------------------------------------------
+// K-major BF16 operand rows of 64 bytes, 64-byte swizzle: 8-row groups 512 bytes apart
+__device__ inline uint64_t desc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset: 8 rows x 64 bytes
+  d |= (uint64_t)1 << 46;                   // descriptor version of tcgen05
+  d |= (uint64_t)4 << 61;                   // 64-byte swizzle
+  return d;
+}
+
+// BF16 x BF16 -> FP32, K-major A and B, M = 128, N = 64
+constexpr uint32_t kOzIdesc =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzN >> 3) << 17) | ((uint32_t)(kOzM >> 4) << 24);
+
+__device__ inline void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kOzIdesc), "r"(accumulate));
+}
+
+__device__ inline void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+      "[%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ inline void tmem_ld_16cols(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// level l's integer, scaled to 2^(38 - 7 l) (levels 6 and 7 rounded to the nearest 2^-38)
+template <int L>
+__device__ inline long long level_term(int v) {
+  constexpr int s = 38 - 7 * L;
+  if constexpr (s >= 0) {
+    return (long long)v << s;
+  } else {
+    return ((long long)v + (1LL << (-s - 1))) >> (-s);
+  }
+}
+
+// 2^x for any exponent an FP64 update can take
+__device__ inline double pow2(int x) {
+  if (x >= -1022 && x <= 1023) return __hiloint2double((x + 1023) << 20, 0);
+  return ldexp(1.0, x);
+}
+
+__global__ void __launch_bounds__(kOzThreads, 1)
+    ozaki_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                      const int* __restrict__ ex, int64_t m, int64_t ncols, int nkb, double* __restrict__ C,
+                      int64_t ldc, int32_t* __restrict__ status) {
+  const int64_t row0 = (int64_t)blockIdx.x * kOzM, col0 = (int64_t)blockIdx.y * kOzN;
+  if (row0 + kOzM - 1 < col0) return;  // the tile lies above the diagonal: nothing to update
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kOzStages * kOzStageBytes);
+  uint64_t* empty = full + kOzStages;
+  uint64_t* acc_full = empty + kOzStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 1);
+  volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kOzStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_full, 1);
+    *fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kOzTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int issued = 0;  // producer: stage loads issued
+  if (warp == 4) {
+    if (lane == 0) {
+      for (int kb = 0; kb < nkb && !*fail; ++kb, ++issued) {
+        const int s = kb % kOzStages;
+        const uint32_t ph = (uint32_t)((kb / kOzStages) & 1);
+        if (!mbar_wait(&empty[s], ph ^ 1u)) {
+          *fail = 1;
+          break;
+        }
+        uint8_t* a = smem + s * kOzStageBytes;
+        mbar_expect_tx(&full[s], kOzStageBytes);
+        tma_load_3d(a, &map_a, &full[s], kb * kOzKB, (int)row0, 0);
+        tma_load_3d(a + kOzABytes, &map_b, &full[s], kb * kOzKB, (int)col0, 0);
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      for (int kb = 0; kb < nkb && !*fail; ++kb) {
+        const int s = kb % kOzStages;
+        const uint32_t ph = (uint32_t)((kb / kOzStages) & 1);
+        if (!mbar_wait(&full[s], ph)) {
+          *fail = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t base = smem_u32(smem + s * kOzStageBytes);
+#pragma unroll 1
+        for (int kk = 0; kk < kOzKB / 16; ++kk) {  // 32 bytes of K per instruction
+#pragma unroll
+          for (int t = 0; t < kSlices; ++t) {
+            const uint64_t da = desc_sw64(base + t * (kOzM * kOzKB * 2) + kk * 32);
+#pragma unroll
+            for (int u = 0; u < kSlices - t; ++u) {
+              const uint64_t db = desc_sw64(base + kOzABytes + u * (kOzN * kOzKB * 2) + kk * 32);
+              mma_bf16(tmem + (uint32_t)(kOzN * (t + u)), da, db, (kb == 0 && kk == 0 && t == 0) ? 0u : 1u);
+            }
+          }
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(acc_full);  // also after a failed wait: tracks every MMA issued so far
+    }
+  }
+
+  // epilogue warps 0..3: fold the eight levels of each row (TMEM lane) into FP64 deltas
+  double* dt = reinterpret_cast<double*>(smem);  // 128 x 65 doubles over the (finished) stages
+  const int q = warp & 3;
+  if (warp < 4) {
+    if (!mbar_wait(acc_full, 0)) *fail = 1;
+    if (!*fail) {
+      tc_fence_after();
+      const int rl = 32 * q + lane;
+      const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+#pragma unroll 1
+      for (int g = 0; g < kOzN / 16; ++g) {
+        long long v[16];
+        float f[16];
+#define QGX_OZ_LEVEL(L)                                                          \
+  tmem_ld_16cols(lane_addr + (uint32_t)(kOzN * (L) + 16 * g), f);                \
+  _Pragma("unroll") for (int j = 0; j < 16; ++j) {                               \
+    const long long tv = level_term<L>(__float2int_rn(f[j]));                    \
+    v[j] = (L) == 0 ? tv : v[j] + tv;                                            \
+  }
+        QGX_OZ_LEVEL(0)
+        QGX_OZ_LEVEL(1)
+        QGX_OZ_LEVEL(2)
+        QGX_OZ_LEVEL(3)
+        QGX_OZ_LEVEL(4)
+        QGX_OZ_LEVEL(5)
+        QGX_OZ_LEVEL(6)
+        QGX_OZ_LEVEL(7)
+#undef QGX_OZ_LEVEL
+#pragma unroll
+        for (int j = 0; j < 16; ++j) dt[rl * kOzDLd + 16 * g + j] = (double)v[j];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();  // deltas complete; every role has left its loop
+  if (*fail) {
+    if (threadIdx.x == 0 && status) atomicExch(status, QGX_ERR_TIMEOUT);
+  } else if (warp < 4) {
+    // C[i][j] -= 2^(e_i + e_j - 52) V_ij on or below the diagonal, one row per warp step
+    for (int rr = q; rr < kOzM; rr += 4) {
+      const int64_t i = row0 + rr;
+      if (i >= m) break;
+      const int ei = ex[i];
+      double* crow = C + i * ldc;
+#pragma unroll
+      for (int h = 0; h < kOzN / 32; ++h) {
+        const int cl = 32 * h + lane;
+        const int64_t j = col0 + cl;
+        if (j < ncols && j <= i) {
+          const double s = pow2(ei + ex[j] - 52);
+          crow[j] = fma(-dt[rr * kOzDLd + cl], s, crow[j]);
+        }
+      }
+    }
+  }
+  if (*fail && warp == 4 && lane == 0) {
+    // no copy may land in shared memory after the CTA has left: wait (bounded) for the loads
+    // of the last stages issued
+    for (int kb = std::max(0, issued - kOzStages); kb < issued; ++kb)
+      mbar_wait(&full[kb % kOzStages], (uint32_t)((kb / kOzStages) & 1));
+  }
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kOzTmemCols) : "memory");
+  }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static std::once_flag once;
+  static EncodeTiled fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// slices S[8][m][K] as a 3D tensor (K, m, 8); box 32 x box_rows x 8, 64-byte swizzle, rows past
+// m read as zeros
+int encode_slices(CUtensorMap* map, const __nv_bfloat16* S, int64_t m, int K, int box_rows) {
+  EncodeTiled enc = encode_fn();
+  if (!enc) return QGX_ERR_UNSUPPORTED;
+  const cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)m, (cuuint64_t)kSlices};
+  const cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)(m * K * 2)};
+  const cuuint32_t box[3] = {(cuuint32_t)kOzKB, (cuuint32_t)box_rows, (cuuint32_t)kSlices};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult cr = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(S), dims, strides, box,
+                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return cr == CUDA_SUCCESS ? QGX_OK : QGX_ERR_UNSUPPORTED;
+}
+
+struct CholWs {
+  __nv_bfloat16* s_panel;  // 8 x n x 256 digits of a trailing panel
+  __nv_bfloat16* s_block;  // 8 x n x 64 digits of a diagonal block's column strip
+  int* e_panel;            // n row exponents
+  int* e_block;            // n row exponents
+};
+
+int64_t chol_layout(int64_t n, void* base, CholWs* ws) {
+  const int64_t o_sp = 0;
+  const int64_t o_sb = o_sp + al256(kSlices * n * kPanel * 2);
+  const int64_t o_ep = o_sb + al256(kSlices * n * kBlk * 2);
+  const int64_t o_eb = o_ep + al256(n * 4);
+  const int64_t total = o_eb + al256(n * 4);
+  if (base && ws) {
+    char* b = static_cast<char*>(base);
+    ws->s_panel = reinterpret_cast<__nv_bfloat16*>(b + o_sp);
+    ws->s_block = reinterpret_cast<__nv_bfloat16*>(b + o_sb);
+    ws->e_panel = reinterpret_cast<int*>(b + o_ep);
+    ws->e_block = reinterpret_cast<int*>(b + o_eb);
+  }
+  return total;
+}
+
+// C (m x ncols region, lower part) -= P P^T for the K-column panel at A[row0.., col0..]
+int ozaki_update(double* A, int64_t lda, int64_t row0, int64_t col0, int64_t m, int64_t ncols, int K,
+                 __nv_bfloat16* S, int* ex, int32_t* status, cudaStream_t st, int64_t* kernels) {
+  if (m <= 0 || ncols <= 0) return QGX_OK;
+  if (m > 0x7fffffffLL || (m + kOzM - 1) / kOzM > 0x7fffffffLL || (ncols + kOzN - 1) / kOzN > 65535)
+    return QGX_ERR_UNSUPPORTED;
+  slice_rows_kernel<<<(unsigned)((m + 7) / 8), 256, 0, st>>>(A, lda, row0, col0, m, K, S, ex);
+  CUtensorMap ma, mb;
+  int rc = encode_slices(&ma, S, m, K, kOzM);
+  if (rc == QGX_OK) rc = encode_slices(&mb, S, m, K, kOzN);
+  if (rc != QGX_OK) return rc;
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(ozaki_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOzSmem));
+  const dim3 grid((unsigned)((m + kOzM - 1) / kOzM), (unsigned)((ncols + kOzN - 1) / kOzN));
+  ozaki_syrk_kernel<<<grid, kOzThreads, kOzSmem, st>>>(ma, mb, ex, m, ncols, K / kOzKB,
+                                                      A + row0 * lda + row0, lda, status);
+  *kernels += 2;
+  return launch_status();
+}
+
+}  // namespace
+
+int64_t chol_f64_workspace_bytes(int64_t n) { return n > 0 ? chol_layout(n, nullptr, nullptr) : 0; }
+
+// A = L L^T in place (see the file comment). info: 0, or the order of the first leading minor
+// that is not positive definite. status (may be NULL): QGX_ERR_TIMEOUT if a tensor-core wait ran
+// out. Adds the number of kernels launched to *kernels.
+int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
+             int64_t* kernels) {
+  if ((reinterpret_cast<uintptr_t>(work) & 255) != 0) return QGX_ERR_ARG;
+  CholWs ws;
+  chol_layout(n, work, &ws);
+  QGX_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
+  if (status) QGX_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), st));
+  int rc;
+  for (int64_t c0 = 0; c0 < n; c0 += kPanel) {
+    const int64_t pe = std::min<int64_t>(c0 + kPanel, n);
+    for (int64_t cj = c0; cj < pe; cj += kBlk) {
+      const int nb = (int)std::min<int64_t>(kBlk, n - cj);
+      potrf_block_kernel<<<1, 256, 0, st>>>(A, lda, cj, nb, info);
+      ++*kernels;
+      const int64_t rb = cj + kBlk;  // first row below the block
+      if (rb >= n) break;
+      trsm_block_kernel<<<(unsigned)((n - rb + 127) / 128), 128, 0, st>>>(A, lda, cj, rb, n);
+      ++*kernels;
+      if ((rc = launch_status()) != QGX_OK) return rc;
+      // the block's columns update the rest of the panel (K = 64)
+      if (rb < pe && (rc = ozaki_update(A, lda, rb, cj, n - rb, pe - rb, kBlk, ws.s_block, ws.e_block, status, st,
+                                        kernels)) != QGX_OK)
+        return rc;
+    }
+    if (pe >= n) break;
+    // the panel updates the trailing matrix (K = 256)
+    if ((rc = ozaki_update(A, lda, pe, c0, n - pe, n - pe, kPanel, ws.s_panel, ws.e_panel, status, st, kernels)) !=
+        QGX_OK)
+      return rc;
+  }
+  return launch_status();
+}
+
+}  // namespace qgx
+
+using namespace qgx;
+
+extern "C" {
+
+int64_t qgx_cholesky_workspace_bytes(int64_t n) { return chol_f64_workspace_bytes(n); }
+
+int qgx_cholesky(double* A, int64_t n, int64_t lda, int32_t* info, int32_t* status, void* workspace,
+                 int64_t workspace_bytes, qgx_stream_t stream) {
+  QGX_CHECK_ARG(n > 0 && lda >= n && A && info && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= chol_f64_workspace_bytes(n));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  int64_t kernels = 0;
+  return chol_f64(A, n, lda, info, status, workspace, as_cuda(stream), &kernels);
+}
+
+}  // extern "C"

@@ -431,19 +431,21 @@ __global__ void er_center_kernel(float* __restrict__ O, int64_t ns, int64_t cols
 }
 
 // psi from local updates against a direct forward (Metropolis.sweep, metropolis.py:201-213):
-// close when |psi_l - psi_d| < 1e-8 or |psi_l / psi_d - 1| < 1e-3 (on log|psi|: the ratio is
-// exp(lp_l - lp_d)); counts the configurations that are neither and, when out is given,
-// writes the direct values there (out may be local itself). One block, fixed reduction order.
+// close when |psi_l - psi_d| < 1e-8 or |psi_l / psi_d - 1| < 1e-3. On log|psi| the ratio test
+// is log1p(-1e-3) < lp_l - lp_d < log1p(1e-3); the absolute test matters only for amplitudes
+// near 1e-8 and is evaluated in FP32. Counts the configurations that are neither (into a
+// zeroed *count) and, when out is given, writes the direct values there (out may be local).
 __global__ void log_psi_mismatch_kernel(const float* local, const float* __restrict__ direct, int64_t ns,
                                         int32_t* __restrict__ count, float* out) {
   __shared__ int sh[32];
   int c = 0;
-  for (int64_t i = threadIdx.x; i < ns; i += blockDim.x) {
-    const double l = (double)local[i], d = (double)direct[i];
-    const bool close_abs = fabs(exp(l) - exp(d)) < 1e-8;
-    const bool close_rel = fabs(expm1(l - d)) < 1e-3;
-    c += (close_abs || close_rel) ? 0 : 1;
-    if (out) out[i] = direct[i];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns; i += (int64_t)gridDim.x * blockDim.x) {
+    const float l = local[i], d = direct[i];
+    const float x = l - d;
+    const bool close_rel = x > -1.00050033358e-3f && x < 9.99500333084e-4f;
+    const bool close_abs = fabsf(__expf(l) - __expf(d)) < 1e-8f;
+    c += (close_rel || close_abs) ? 0 : 1;
+    if (out) out[i] = d;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
@@ -452,7 +454,7 @@ __global__ void log_psi_mismatch_kernel(const float* local, const float* __restr
   if (threadIdx.x == 0) {
     int t = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
-    *count = t;
+    if (t) atomicAdd(count, t);  // integer sums: the total does not depend on the order
   }
 }
 
@@ -610,7 +612,8 @@ int qgx_reweight_factor(const float* log_psi, int64_t ns, float reweight, double
 int qgx_log_psi_mismatch(const float* local, const float* direct, int64_t ns, int32_t* count, float* out,
                          qgx_stream_t stream) {
   QGX_CHECK_ARG(ns > 0 && local && direct && count);
-  log_psi_mismatch_kernel<<<1, 1024, 0, as_cuda(stream)>>>(local, direct, ns, count, out);
+  QGX_CHECK_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t), as_cuda(stream)));
+  log_psi_mismatch_kernel<<<blocks_for(ns, 256), 256, 0, as_cuda(stream)>>>(local, direct, ns, count, out);
   return launch_status();
 }
 

@@ -26,6 +26,8 @@ namespace qgx {
 namespace {
 
 constexpr int kFwdThreads = 256;
+constexpr int kFwdSPT = 2;      // sites per thread in the FP32 convolutions
+constexpr int kFwdSamples = 5;  // samples per CTA: 5 x 50 site pairs fill 256 threads at L = 10
 constexpr int kMaxSitesConv = 256;  // L <= 16
 
 struct ConvNet {
@@ -76,44 +78,64 @@ __device__ inline void stage_floats(float* dst, const float* src, int64_t n) {
 }
 
 // out[a][o][r] = act(sum_{i,tap} W[i][tap][o] in[a][i][nbr(r,tap)] + bias[o]); mode 0: gelu and store,
-// mode 1: accumulate into out (residual add)
-template <int C>
+// mode 1: accumulate into out (residual add). A thread computes the C outputs of SPT sites
+// r = g + k G (G = ceil(N / SPT)), so consecutive threads gather consecutive sites (no bank
+// conflicts) and every broadcast weight load feeds SPT x 4 FMAs.
+template <int C, int SPT>
 __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* __restrict__ out,
                                   const float* __restrict__ w, const int16_t* __restrict__ nbr, int N, int S,
                                   int mode) {
   const float* bias = w + cin * 9 * C;
-  for (int it = threadIdx.x; it < S * N; it += blockDim.x) {
-    const int a = it / N, r = it - a * N;
-    int nb[9];
+  const int G = (N + SPT - 1) / SPT;
+  for (int it = threadIdx.x; it < S * G; it += blockDim.x) {
+    const int a = it / G, g = it - a * G;
+    int r[SPT];
+    int nb[SPT][9];
 #pragma unroll
-    for (int t = 0; t < 9; ++t) nb[t] = nbr[r * 9 + t];
-    float acc[C];
+    for (int k = 0; k < SPT; ++k) {
+      r[k] = g + k * G;
+      const int rc = r[k] < N ? r[k] : N - 1;  // a site past the end reads a valid one, is not stored
 #pragma unroll
-    for (int o = 0; o < C; ++o) acc[o] = bias[o];
+      for (int t = 0; t < 9; ++t) nb[k][t] = nbr[rc * 9 + t];
+    }
+    float acc[SPT][C];
+#pragma unroll
+    for (int k = 0; k < SPT; ++k)
+#pragma unroll
+      for (int o = 0; o < C; ++o) acc[k][o] = bias[o];
     const float* ina = in + (int64_t)a * C * N;
     for (int i = 0; i < cin; ++i) {
       const float* ini = ina + i * N;
 #pragma unroll
       for (int t = 0; t < 9; ++t) {
-        const float v = ini[nb[t]];
+        float v[SPT];
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) v[k] = ini[nb[k][t]];
         const float4* wp = reinterpret_cast<const float4*>(w + (i * 9 + t) * C);
 #pragma unroll
         for (int o4 = 0; o4 < C / 4; ++o4) {
           const float4 ww = wp[o4];
-          acc[4 * o4] = fmaf(v, ww.x, acc[4 * o4]);
-          acc[4 * o4 + 1] = fmaf(v, ww.y, acc[4 * o4 + 1]);
-          acc[4 * o4 + 2] = fmaf(v, ww.z, acc[4 * o4 + 2]);
-          acc[4 * o4 + 3] = fmaf(v, ww.w, acc[4 * o4 + 3]);
+#pragma unroll
+          for (int k = 0; k < SPT; ++k) {
+            acc[k][4 * o4] = fmaf(v[k], ww.x, acc[k][4 * o4]);
+            acc[k][4 * o4 + 1] = fmaf(v[k], ww.y, acc[k][4 * o4 + 1]);
+            acc[k][4 * o4 + 2] = fmaf(v[k], ww.z, acc[k][4 * o4 + 2]);
+            acc[k][4 * o4 + 3] = fmaf(v[k], ww.w, acc[k][4 * o4 + 3]);
+          }
         }
       }
     }
-    float* oa = out + (int64_t)a * C * N + r;
-    if (mode == 0) {
 #pragma unroll
-      for (int o = 0; o < C; ++o) oa[o * N] = gelu_tanh(acc[o]);
-    } else {
+    for (int k = 0; k < SPT; ++k) {
+      if (r[k] >= N) continue;
+      float* oa = out + (int64_t)a * C * N + r[k];
+      if (mode == 0) {
 #pragma unroll
-      for (int o = 0; o < C; ++o) oa[o * N] += acc[o];
+        for (int o = 0; o < C; ++o) oa[o * N] = gelu_tanh(acc[k][o]);
+      } else {
+#pragma unroll
+        for (int o = 0; o < C; ++o) oa[o * N] += acc[k][o];
+      }
     }
   }
 }
@@ -165,11 +187,11 @@ __global__ void __launch_bounds__(kFwdThreads)
       }
       stage_floats(Wl, table + layer_offset(2 * b, C), layer_floats(2 * b, C));
       __syncthreads();
-      conv_layer<C>(P, cin, Q, Wl, nbr, N, S, 0);
+      conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0);
       __syncthreads();
       stage_floats(Wl, table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
       __syncthreads();
-      conv_layer<C>(Q, C, X, Wl, nbr, N, S, 1);
+      conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1);
     }
     __syncthreads();
     // log of the mean final activation over (channel, site) per sample, one warp per sample
@@ -591,7 +613,7 @@ __global__ void __launch_bounds__(kJacThreads)
       // A = conv1(P) + b1 (pre-activation kept: conv_layer mode 1 on a zeroed buffer)
       for (int e = threadIdx.x; e < CN; e += blockDim.x) Qa[e] = 0.0f;
       __syncthreads();
-      conv_layer<C>(P, cin, Qa, W, nbr, N, 1, 1);
+      conv_layer<C, 1>(P, cin, Qa, W, nbr, N, 1, 1);
       __syncthreads();
       for (int e = threadIdx.x; e < CN; e += blockDim.x) {
         xs[CN + e] = Qa[e];
@@ -599,7 +621,7 @@ __global__ void __launch_bounds__(kJacThreads)
       }
       stage_layer<C>(table, 2 * b + 1, W, WT);
       __syncthreads();
-      conv_layer<C>(Qa, C, X, W, nbr, N, 1, 1);
+      conv_layer<C, 1>(Qa, C, X, W, nbr, N, 1, 1);
     }
     __syncthreads();
     // ---- output cotangents: w_e = f'(z_e) / sum f, f = exp (exp_by_scale) or sinh + 1
@@ -736,7 +758,7 @@ int rc_smem_bytes(const ConvNet& net, int S) {
 template <int C>
 int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                      float2* out, cudaStream_t st) {
-  const int S = 4;
+  const int S = kFwdSamples;
   const int smem = rc_smem_bytes(net, S);
   auto k = rc_forward_kernel<C>;
   if (smem > 48 * 1024) QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));

@@ -18,6 +18,9 @@ int64_t trsv_chol_workspace_bytes(int64_t n);
 int trsv_chol_prepare(const float* L, int64_t n, void* work, cudaStream_t st);
 int trsv_chol_apply(const float* L, int64_t n, float* v, void* work, uint32_t epoch, cudaStream_t st);
 int trsv_chol_error(int64_t n, void* work, int* host_err, cudaStream_t st);
+int64_t chol_f64_workspace_bytes(int64_t n);
+int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
+             int64_t* kernels);
 
 namespace {
 
@@ -461,6 +464,7 @@ struct SolveWs {
   double* r;      // n
   double* acc;    // 16: iteration scalars and residual norms
   void* trsv;     // SHIFT_MIXED: the triangular solves' diagonal-block inverses and flags
+  void* chol;     // SHIFT: the factorisation's digit slices and row exponents
 };
 
 // The FP32 factorisation of SHIFT_MIXED runs with cuSOLVER's BF16x9 emulation of FP32
@@ -486,6 +490,11 @@ int query_cusolver_bytes(int64_t n, int method, size_t* dev_bytes, size_t* host_
   if (rc != QGX_OK) return rc;
   cusolverStatus_t s;
   if (method == QGX_SOLVE_SHIFT) {
+    *dev_bytes = 0;
+    *host_bytes = 0;
+    return QGX_OK;
+  }
+  if (method == QGX_SOLVE_SHIFT_LIB) {
     s = cusolverDnXpotrf_bufferSize(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, nullptr, n, CUDA_R_64F, dev_bytes,
                                     host_bytes);
   } else if (method == QGX_SOLVE_SHIFT_MIXED) {
@@ -530,6 +539,7 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   const int64_t o_r = take(mixed ? n * 8 : 0);
   const int64_t o_acc = take(mixed ? 16 * 8 : 0);
   const int64_t o_trsv = take(mixed ? trsv_chol_workspace_bytes(n) : 0);
+  const int64_t o_chol = take(method == QGX_SOLVE_SHIFT ? chol_f64_workspace_bytes(n) : 0);
   *need = off;
   if (!base) return QGX_OK;
   if (bytes < off) return QGX_ERR_ARG;
@@ -549,6 +559,7 @@ int workspace_layout(int64_t n, int64_t np, int method, void* base, int64_t byte
   ws->r = reinterpret_cast<double*>(b + o_r);
   ws->acc = reinterpret_cast<double*>(b + o_acc);
   ws->trsv = b + o_trsv;
+  ws->chol = b + o_chol;
   if (hb > g_host_ws.size()) g_host_ws.resize(hb);
   return QGX_OK;
 }
@@ -579,17 +590,24 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
   if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
   int* dinfo = info ? info : ws.info;
   void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
-  if (method == QGX_SOLVE_SHIFT) {
+  if (method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_SHIFT_LIB) {
     ++g_kernels;
     shift_diag_kernel<<<1, 1024, 0, st>>>(T, n, n, rshift, ashift, ws.shift);
     if ((rc = launch_status()) != QGX_OK) return rc;
-    if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus, ws.cus_bytes, hws,
-                         g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
+    cublasFillMode_t fill = CUBLAS_FILL_MODE_LOWER;
+    if (method == QGX_SOLVE_SHIFT) {
+      // this library's factorisation: L in the row-major lower triangle = the column-major
+      // upper factor cuSOLVER's potrs takes
+      if ((rc = chol_f64(T, n, n, dinfo, nullptr, ws.chol, st, &g_kernels)) != QGX_OK) return rc;
+      fill = CUBLAS_FILL_MODE_UPPER;
+    } else if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus, ws.cus_bytes,
+                                hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS) {
       return QGX_ERR_SOLVER;
+    }
     QGX_CHECK_CUDA(cudaMemcpyAsync(ws.y, b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     // Xpotrs reports only argument errors; it writes its own word so that the factorisation's
     // info (> 0: leading minor not positive definite) reaches the caller
-    if (cusolverDnXpotrs(h, p, CUBLAS_FILL_MODE_LOWER, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, ws.info + 1) !=
+    if (cusolverDnXpotrs(h, p, fill, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, ws.info + 1) !=
         CUSOLVER_STATUS_SUCCESS)
       return QGX_ERR_SOLVER;
     ++g_kernels;
@@ -715,7 +733,7 @@ using namespace qgx;
 extern "C" {
 
 int qgx_solve_workspace_bytes(int64_t n, int64_t np, int32_t method, int64_t* bytes) {
-  QGX_CHECK_ARG(n > 0 && np > 0 && bytes && method >= QGX_SOLVE_SHIFT && method <= QGX_SOLVE_SHIFT_MIXED);
+  QGX_CHECK_ARG(n > 0 && np > 0 && bytes && method >= QGX_SOLVE_SHIFT && method <= QGX_SOLVE_SHIFT_LIB);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   SolveWs ws;
   return workspace_layout(n, np, method, nullptr, 0, &ws, bytes);
@@ -727,7 +745,8 @@ int qgx_minsr_solve(double* T, int64_t n, const float* A, int64_t np, int64_t ld
                     double rshift, double ashift, double rtol, double atol, double tol_snr, double* x, int32_t* info,
                     void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
   QGX_CHECK_ARG(n > 0 && np > 0 && lda >= np && T && A && b && x && workspace);
-  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV || method == QGX_SOLVE_SHIFT_MIXED);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV || method == QGX_SOLVE_SHIFT_MIXED ||
+                method == QGX_SOLVE_SHIFT_LIB);
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   g_kernels = 0;
@@ -744,7 +763,7 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
                  double rshift, double ashift, double rtol, double atol, double tol_snr, double* x, int32_t* info,
                  void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
   QGX_CHECK_ARG(n > 0 && np > 0 && lda >= np && S && A && b && x && workspace);
-  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV || method == QGX_SOLVE_SHIFT_LIB);
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   g_kernels = 0;
@@ -811,7 +830,7 @@ int qgx_sym_solve(double* S, int64_t n, const double* f, int32_t method, double 
                   double atol, double* x, int32_t* info, void* workspace, int64_t workspace_bytes,
                   qgx_stream_t stream) {
   QGX_CHECK_ARG(n > 0 && S && f && x && workspace);
-  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV);
+  QGX_CHECK_ARG(method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_PINV || method == QGX_SOLVE_SHIFT_LIB);
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   std::lock_guard<std::mutex> lock(g_solver_mutex);
   g_kernels = 0;

@@ -8,6 +8,7 @@
     python -m quantax_gb300.kernel_bench rc_sweep --ns 16384 --steps 4
     python -m quantax_gb300.kernel_bench rc_eloc --ns 16384
     python -m quantax_gb300.kernel_bench rc_jacobian --ns 2048
+    python -m quantax_gb300.kernel_bench chol --rows 8192 --k 16640 --reps 3 [--lib]
 
 Prints one JSON line with the mean device time per launch (CUDA events, after warm-up).
 """
@@ -101,7 +102,8 @@ def _resconv(a, st):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["gram", "sweep", "eloc", "obar", "rc_forward", "rc_sweep", "rc_eloc",
-                                       "rc_jacobian"])
+                                       "rc_jacobian", "chol"])
+    ap.add_argument("--lib", action="store_true", help="chol: cuSOLVER's FP64 Xpotrf instead of qgx_cholesky")
     ap.add_argument("--L", type=int, default=10)
     ap.add_argument("--blocks", type=int, default=8)
     ap.add_argument("--channels", type=int, default=16)
@@ -133,6 +135,37 @@ def main():
         syrk = float(a.rows) * (a.rows + 1) * a.k
         out.update(mode=a.mode, rows=a.rows, k=a.k, ms=ms, syrk_tflops=syrk / ms / 1e9,
                    gemm_equiv_tflops=2.0 * a.rows * a.rows * a.k / ms / 1e9)
+    elif a.kernel == "chol":
+        # T = G G^T / k + 1e-4 I from an FP32 G of rows x k (the MinSR Gram's structure), factored
+        # from a fresh copy every repetition (the copy is timed apart and subtracted)
+        import ctypes as C
+        n = a.rows
+        G = torch.randn((n, a.k), dtype=torch.float32, device="cuda").double() / np.sqrt(a.k)
+        T0 = G @ G.T + 1e-4 * torch.eye(n, dtype=torch.float64, device="cuda")
+        del G
+        T = torch.empty_like(T0)
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        if a.lib:
+            A32 = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+            b = torch.zeros(n, dtype=torch.float64, device="cuda")
+            x = torch.empty(8, dtype=torch.float64, device="cuda")
+            nb = C.c_int64(0)
+            L.call("qgx_solve_workspace_bytes", n, 8, L.SOLVE_SHIFT_LIB, C.byref(nb))
+            ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+            # the solve with zero shifts: the factorisation plus two triangular solves and a
+            # projection over an 8-column A (the latter two are microseconds)
+            fn = lambda: (T.copy_(T0), L.call("qgx_minsr_solve", L.ptr(T), n, L.ptr(A32), 8, 8, L.ptr(b),
+                                                L.SOLVE_SHIFT_LIB, 0.0, 0.0, 0.0, 0.0, 0.0, L.ptr(x), L.ptr(info),
+                                                L.ptr(ws), ws.numel(), st))
+        else:
+            ws = torch.empty(L.lib().qgx_cholesky_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            fn = lambda: (T.copy_(T0), L.call("qgx_cholesky", L.ptr(T), n, n, L.ptr(info), None, L.ptr(ws),
+                                                ws.numel(), st))
+        ms = _events(fn, a.reps)
+        copy_ms = _events(lambda: T.copy_(T0), a.reps)
+        f = ms - copy_ms
+        out.update(lib=a.lib, n=n, ms=f, copy_ms=copy_ms, info=int(info.item()),
+                   fp64_tflops=n ** 3 / 3.0 / f / 1e9)
     elif a.kernel.startswith("rc_"):
         out.update(_resconv(a, st))
     else:

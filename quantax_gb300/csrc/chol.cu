@@ -92,14 +92,16 @@ __global__ void slice_rows_kernel(const double* __restrict__ A, int64_t lda, int
 // ---- FP64 diagonal block and triangular solve -----------------------------------------------
 // Cholesky of the nb x nb (nb <= 64) diagonal block at (c, c), in place. The first pivot that is
 // not positive sets *info = c + k + 1 (the order of the failing leading minor, as LAPACK and
-// cuSOLVER report it); the factorisation carries on with a NaN pivot.
+// cuSOLVER report it); the factorisation carries on with a NaN pivot. 256 threads as a 16 x 16
+// grid over the trailing block (no index division in the update loop); the pivot's inverse
+// square root scales its column.
 __global__ void __launch_bounds__(256) potrf_block_kernel(double* __restrict__ A, int64_t lda, int64_t c, int nb,
                                                           int* __restrict__ info) {
   __shared__ double a[kBlk][kBlk + 1];
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, j = e - i * nb;
-    if (j <= i) a[i][j] = A[(c + i) * lda + c + j];
-  }
+  __shared__ double piv[2];  // sqrt and inverse sqrt of the current pivot
+  const int ti = threadIdx.x >> 4, tj = threadIdx.x & 15;
+  for (int i = ti; i < nb; i += 16)
+    for (int j = tj; j <= i; j += 16) a[i][j] = A[(c + i) * lda + c + j];
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
     if (threadIdx.x == 0) {
@@ -108,52 +110,67 @@ __global__ void __launch_bounds__(256) potrf_block_kernel(double* __restrict__ A
         atomicCAS(info, 0, (int)(c + k + 1));
         d = __longlong_as_double(0x7FF8000000000000LL);
       }
-      a[k][k] = sqrt(d);
+      const double r = rsqrt(d);
+      piv[0] = d * r;  // sqrt(d)
+      piv[1] = r;
     }
     __syncthreads();
-    const double inv = 1.0 / a[k][k];
-    for (int i = k + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][k] *= inv;
+    const double r = piv[1];
+    if (threadIdx.x == 0) a[k][k] = piv[0];
+    for (int i = k + 1 + threadIdx.x; i < nb; i += blockDim.x) a[i][k] *= r;
     __syncthreads();
-    const int r = nb - k - 1;
-    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-      const int i = k + 1 + e / r, j = k + 1 + e % r;
-      if (j <= i) a[i][j] = fma(-a[i][k], a[j][k], a[i][j]);
+    for (int i = k + 1 + ti; i < nb; i += 16) {
+      const double aik = a[i][k];
+      for (int j = k + 1 + tj; j <= i; j += 16) a[i][j] = fma(-aik, a[j][k], a[i][j]);
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, j = e - i * nb;
-    if (j <= i) A[(c + i) * lda + c + j] = a[i][j];
-  }
+  for (int i = ti; i < nb; i += 16)
+    for (int j = tj; j <= i; j += 16) A[(c + i) * lda + c + j] = a[i][j];
 }
 
 // rows [r0, n) of the 64 columns at c: x L_cc^T = a with L_cc the factored diagonal block, in
 // place (reference BLAS dtrsm 'R','L','T','N' order: scale by the pivot's reciprocal, then
-// update the later columns). One thread per row, the row in registers, L_cc in shared memory.
-__global__ void __launch_bounds__(128) trsm_block_kernel(double* __restrict__ A, int64_t lda, int64_t c, int64_t r0,
-                                                         int64_t n) {
+// update the later columns). Eight lanes per row, lane l holding columns l, l + 8, ..., l + 56:
+// at step k the owner of column k scales it and an 8-lane shuffle hands it to the others, which
+// update their later columns. 16 rows per 128-thread CTA, so even a short panel's rows spread
+// over every SM (the SMs' FP64 pipes bound the work).
+constexpr int kTrsmThreads = 128;
+constexpr int kTrsmRows = kTrsmThreads / 8;
+__global__ void __launch_bounds__(kTrsmThreads) trsm_block_kernel(double* __restrict__ A, int64_t lda, int64_t c,
+                                                                  int64_t r0, int64_t n) {
   __shared__ double l[kBlk][kBlk + 1];
   __shared__ double dinv[kBlk];
   for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) {
     const int i = e / kBlk, j = e % kBlk;
     l[i][j] = j <= i ? A[(c + i) * lda + c + j] : 0.0;
   }
-  if (threadIdx.x < kBlk) dinv[threadIdx.x] = 1.0 / A[(c + threadIdx.x) * lda + c + threadIdx.x];
+  for (int i = threadIdx.x; i < kBlk; i += blockDim.x) dinv[i] = 1.0 / A[(c + i) * lda + c + i];
   __syncthreads();
-  const int64_t r = r0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  double* row = A + r * lda + c;
-  double x[kBlk];
+  const int sub = threadIdx.x & 7;  // lane within the row's group of eight
+  const int64_t r = r0 + (int64_t)blockIdx.x * kTrsmRows + (threadIdx.x >> 3);
+  const bool live = r < n;  // whole 8-lane groups share a row; dead groups keep shuffling zeros
+  double* row = A + (live ? r : r0) * lda + c;
+  double x[kBlk / 8];
 #pragma unroll
-  for (int k = 0; k < kBlk; ++k) x[k] = row[k];
+  for (int q = 0; q < kBlk / 8; ++q) x[q] = live ? row[8 * q + sub] : 0.0;
 #pragma unroll
   for (int k = 0; k < kBlk; ++k) {
-    x[k] *= dinv[k];
+    const int qk = k >> 3;
+    double xk = 0.0;
+    if (sub == (k & 7)) {
+      x[qk] *= dinv[k];
+      xk = x[qk];
+    }
+    xk = __shfl_sync(0xffffffffu, xk, k & 7, 8);
 #pragma unroll
-    for (int i = k + 1; i < kBlk; ++i) x[i] = fma(-x[k], l[i][k], x[i]);
+    for (int q = 0; q < kBlk / 8; ++q)
+      if (8 * q + sub > k) x[q] = fma(-xk, l[8 * q + sub][k], x[q]);
   }
+  if (live) {
 #pragma unroll
-  for (int k = 0; k < kBlk; ++k) row[k] = x[k];
+    for (int q = 0; q < kBlk / 8; ++q) row[8 * q + sub] = x[q];
+  }
 }
 
 // ---- tensor-core update C -= P P^T (lower part) ----------------------------------------------
@@ -217,12 +234,15 @@ __device__ inline double pow2(int x) {
   return ldexp(1.0, x);
 }
 
+// C[i][j] -= sum_k P[a0 + i][k] P[b0 + j][k] for the m x ncols region at C (ldc), where slice
+// row r is the panel's row r; only entries with a0 + i >= b0 + j (on or below the diagonal of the
+// whole matrix) are updated
 __global__ void __launch_bounds__(kOzThreads, 1)
     ozaki_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                      const int* __restrict__ ex, int64_t m, int64_t ncols, int nkb, double* __restrict__ C,
-                      int64_t ldc, int32_t* __restrict__ status) {
+                      const int* __restrict__ ex, int64_t m, int64_t ncols, int a0, int b0, int nkb,
+                      double* __restrict__ C, int64_t ldc, int32_t* __restrict__ status) {
   const int64_t row0 = (int64_t)blockIdx.x * kOzM, col0 = (int64_t)blockIdx.y * kOzN;
-  if (row0 + kOzM - 1 < col0) return;  // the tile lies above the diagonal: nothing to update
+  if (a0 + row0 + kOzM - 1 < b0 + col0) return;  // the tile lies above the diagonal: nothing to update
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kOzStages * kOzStageBytes);
@@ -265,8 +285,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         }
         uint8_t* a = smem + s * kOzStageBytes;
         mbar_expect_tx(&full[s], kOzStageBytes);
-        tma_load_3d(a, &map_a, &full[s], kb * kOzKB, (int)row0, 0);
-        tma_load_3d(a + kOzABytes, &map_b, &full[s], kb * kOzKB, (int)col0, 0);
+        tma_load_3d(a, &map_a, &full[s], kb * kOzKB, a0 + (int)row0, 0);
+        tma_load_3d(a + kOzABytes, &map_b, &full[s], kb * kOzKB, b0 + (int)col0, 0);
       }
     }
   } else if (warp == 5) {
@@ -336,19 +356,42 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   if (*fail) {
     if (threadIdx.x == 0 && status) atomicExch(status, QGX_ERR_TIMEOUT);
   } else if (warp < 4) {
-    // C[i][j] -= 2^(e_i + e_j - 52) V_ij on or below the diagonal, one row per warp step
-    for (int rr = q; rr < kOzM; rr += 4) {
-      const int64_t i = row0 + rr;
-      if (i >= m) break;
-      const int ei = ex[i];
-      double* crow = C + i * ldc;
+    // C[i][j] -= 2^(e_i + e_j - 52) V_ij on or below the diagonal: warp q takes rows q, q + 4,
+    // ..., eight rows at a time with all their loads of C issued before the first update, so
+    // the loads' latencies overlap (lane l holds columns l and l + 32 of each row)
+    constexpr int kBatch = 8;
+    int ej[kOzN / 32];
+    bool jin[kOzN / 32];
 #pragma unroll
-      for (int h = 0; h < kOzN / 32; ++h) {
-        const int cl = 32 * h + lane;
-        const int64_t j = col0 + cl;
-        if (j < ncols && j <= i) {
-          const double s = pow2(ei + ex[j] - 52);
-          crow[j] = fma(-dt[rr * kOzDLd + cl], s, crow[j]);
+    for (int h = 0; h < kOzN / 32; ++h) {
+      const int64_t j = col0 + 32 * h + lane;
+      jin[h] = j < ncols;
+      ej[h] = jin[h] ? ex[b0 + j] : 0;
+    }
+#pragma unroll 1
+    for (int rb = q; rb < kOzM; rb += 4 * kBatch) {
+      double cv[kBatch][kOzN / 32];
+      bool ok[kBatch][kOzN / 32];
+#pragma unroll
+      for (int r = 0; r < kBatch; ++r) {
+        const int64_t i = row0 + rb + 4 * r;
+#pragma unroll
+        for (int h = 0; h < kOzN / 32; ++h) {
+          const int64_t j = col0 + 32 * h + lane;
+          ok[r][h] = i < m && jin[h] && b0 + j <= a0 + i;
+          cv[r][h] = ok[r][h] ? C[i * ldc + j] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kBatch; ++r) {
+        const int rr = rb + 4 * r;
+        const int64_t i = row0 + rr;
+        const int ei = i < m ? ex[a0 + i] : 0;
+#pragma unroll
+        for (int h = 0; h < kOzN / 32; ++h) {
+          if (!ok[r][h]) continue;
+          const int cl = 32 * h + lane;
+          C[i * ldc + col0 + cl] = fma(-dt[rr * kOzDLd + cl], pow2(ei + ej[h] - 52), cv[r][h]);
         }
       }
     }
@@ -399,45 +442,90 @@ int encode_slices(CUtensorMap* map, const __nv_bfloat16* S, int64_t m, int K, in
 }
 
 struct CholWs {
-  __nv_bfloat16* s_panel;  // 8 x n x 256 digits of a trailing panel
-  __nv_bfloat16* s_block;  // 8 x n x 64 digits of a diagonal block's column strip
-  int* e_panel;            // n row exponents
-  int* e_block;            // n row exponents
+  __nv_bfloat16* s_panel[2];  // 8 x n x 256 digits of a trailing panel (two panels in flight)
+  __nv_bfloat16* s_block;     // 8 x n x 64 digits of a diagonal block's column strip
+  int* e_panel[2];            // n row exponents each
+  int* e_block;               // n row exponents
 };
 
 int64_t chol_layout(int64_t n, void* base, CholWs* ws) {
-  const int64_t o_sp = 0;
-  const int64_t o_sb = o_sp + al256(kSlices * n * kPanel * 2);
-  const int64_t o_ep = o_sb + al256(kSlices * n * kBlk * 2);
-  const int64_t o_eb = o_ep + al256(n * 4);
-  const int64_t total = o_eb + al256(n * 4);
+  int64_t off = 0;
+  auto take = [&](int64_t b) {
+    const int64_t o = off;
+    off += al256(b);
+    return o;
+  };
+  const int64_t o_sp0 = take(kSlices * n * kPanel * 2), o_sp1 = take(kSlices * n * kPanel * 2);
+  const int64_t o_sb = take(kSlices * n * kBlk * 2);
+  const int64_t o_ep0 = take(n * 4), o_ep1 = take(n * 4), o_eb = take(n * 4);
   if (base && ws) {
     char* b = static_cast<char*>(base);
-    ws->s_panel = reinterpret_cast<__nv_bfloat16*>(b + o_sp);
+    ws->s_panel[0] = reinterpret_cast<__nv_bfloat16*>(b + o_sp0);
+    ws->s_panel[1] = reinterpret_cast<__nv_bfloat16*>(b + o_sp1);
     ws->s_block = reinterpret_cast<__nv_bfloat16*>(b + o_sb);
-    ws->e_panel = reinterpret_cast<int*>(b + o_ep);
+    ws->e_panel[0] = reinterpret_cast<int*>(b + o_ep0);
+    ws->e_panel[1] = reinterpret_cast<int*>(b + o_ep1);
     ws->e_block = reinterpret_cast<int*>(b + o_eb);
   }
-  return total;
+  return off;
 }
 
-// C (m x ncols region, lower part) -= P P^T for the K-column panel at A[row0.., col0..]
-int ozaki_update(double* A, int64_t lda, int64_t row0, int64_t col0, int64_t m, int64_t ncols, int K,
-                 __nv_bfloat16* S, int* ex, int32_t* status, cudaStream_t st, int64_t* kernels) {
-  if (m <= 0 || ncols <= 0) return QGX_OK;
-  if (m > 0x7fffffffLL || (m + kOzM - 1) / kOzM > 0x7fffffffLL || (ncols + kOzN - 1) / kOzN > 65535)
-    return QGX_ERR_UNSUPPORTED;
+// digit slices of the K-column panel at A[row0 .., col0 ..] (m rows)
+int slice_panel(const double* A, int64_t lda, int64_t row0, int64_t col0, int64_t m, int K, __nv_bfloat16* S,
+                int* ex, cudaStream_t st, int64_t* kernels) {
+  if (m <= 0) return QGX_OK;
   slice_rows_kernel<<<(unsigned)((m + 7) / 8), 256, 0, st>>>(A, lda, row0, col0, m, K, S, ex);
+  ++*kernels;
+  return launch_status();
+}
+
+// C -= P P^T over the region of rows [r0, r0 + m) x columns [q0, q0 + ncols) of A, P the panel
+// sliced into S (ms rows, slice row r = matrix row s0 + r)
+int ozaki_region(double* A, int64_t lda, const __nv_bfloat16* S, const int* ex, int64_t ms, int64_t s0, int K,
+                 int64_t r0, int64_t m, int64_t q0, int64_t ncols, int32_t* status, cudaStream_t st,
+                 int64_t* kernels) {
+  if (m <= 0 || ncols <= 0) return QGX_OK;
+  if (ms > 0x7fffffffLL || (m + kOzM - 1) / kOzM > 0x7fffffffLL || (ncols + kOzN - 1) / kOzN > 65535)
+    return QGX_ERR_UNSUPPORTED;
   CUtensorMap ma, mb;
-  int rc = encode_slices(&ma, S, m, K, kOzM);
-  if (rc == QGX_OK) rc = encode_slices(&mb, S, m, K, kOzN);
+  int rc = encode_slices(&ma, S, ms, K, kOzM);
+  if (rc == QGX_OK) rc = encode_slices(&mb, S, ms, K, kOzN);
   if (rc != QGX_OK) return rc;
   QGX_CHECK_CUDA(cudaFuncSetAttribute(ozaki_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOzSmem));
   const dim3 grid((unsigned)((m + kOzM - 1) / kOzM), (unsigned)((ncols + kOzN - 1) / kOzN));
-  ozaki_syrk_kernel<<<grid, kOzThreads, kOzSmem, st>>>(ma, mb, ex, m, ncols, K / kOzKB,
-                                                      A + row0 * lda + row0, lda, status);
-  *kernels += 2;
+  ozaki_syrk_kernel<<<grid, kOzThreads, kOzSmem, st>>>(ma, mb, ex, m, ncols, (int)(r0 - s0), (int)(q0 - s0),
+                                                      K / kOzKB, A + r0 * lda + q0, lda, status);
+  ++*kernels;
   return launch_status();
+}
+
+// Per device: the look-ahead stream (highest priority) and the events that order it against the
+// caller's stream. One factorisation at a time per device (the mutex is held while enqueueing).
+struct LookAhead {
+  std::mutex mu;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t start = nullptr, end = nullptr, strip_done[2] = {}, rest_done[2] = {};
+};
+constexpr int kMaxCholDevices = 64;
+LookAhead g_look[kMaxCholDevices];
+std::mutex g_look_init;
+
+int look_ahead_for_current_device(LookAhead** out) {
+  int dev = 0;
+  QGX_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxCholDevices) return QGX_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_look_init);
+  LookAhead& la = g_look[dev];
+  if (!la.aux) {
+    int lo = 0, hi = 0;
+    QGX_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    QGX_CHECK_CUDA(cudaStreamCreateWithPriority(&la.aux, cudaStreamNonBlocking, hi));
+    cudaEvent_t* evs[6] = {&la.start, &la.end, &la.strip_done[0], &la.strip_done[1], &la.rest_done[0],
+                           &la.rest_done[1]};
+    for (cudaEvent_t* e : evs) QGX_CHECK_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  *out = &la;
+  return QGX_OK;
 }
 
 }  // namespace
@@ -447,36 +535,69 @@ int64_t chol_f64_workspace_bytes(int64_t n) { return n > 0 ? chol_layout(n, null
 // A = L L^T in place (see the file comment). info: 0, or the order of the first leading minor
 // that is not positive definite. status (may be NULL): QGX_ERR_TIMEOUT if a tensor-core wait ran
 // out. Adds the number of kernels launched to *kernels.
+//
+// Look-ahead: panel k's trailing update is split into the next panel's 256 columns (the strip)
+// and the rest. The panel chain (FP64 diagonal blocks, triangular solves, the in-panel updates),
+// the panel's slicing and the strip run on a high-priority internal stream; the rest runs on the
+// caller's stream, so the next panel's FP64 chain overlaps the large tensor-core update. Panel
+// k's chain waits for the rest update of panel k - 2 (the last one touching its columns); two
+// slice buffers alternate between panels. The caller's stream waits for the internal one at
+// the end, so the factor is complete in stream order.
 int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
              int64_t* kernels) {
   if ((reinterpret_cast<uintptr_t>(work) & 255) != 0) return QGX_ERR_ARG;
+  LookAhead* la = nullptr;
+  int rc = look_ahead_for_current_device(&la);
+  if (rc != QGX_OK) return rc;
+  std::lock_guard<std::mutex> lock(la->mu);
   CholWs ws;
   chol_layout(n, work, &ws);
+  cudaStream_t aux = la->aux;
   QGX_CHECK_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
   if (status) QGX_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), st));
-  int rc;
-  for (int64_t c0 = 0; c0 < n; c0 += kPanel) {
+  QGX_CHECK_CUDA(cudaEventRecord(la->start, st));
+  QGX_CHECK_CUDA(cudaStreamWaitEvent(aux, la->start, 0));
+  int64_t k = 0;
+  for (int64_t c0 = 0; c0 < n; c0 += kPanel, ++k) {
     const int64_t pe = std::min<int64_t>(c0 + kPanel, n);
+    if (k >= 2) QGX_CHECK_CUDA(cudaStreamWaitEvent(aux, la->rest_done[k & 1], 0));
+    // the panel chain
     for (int64_t cj = c0; cj < pe; cj += kBlk) {
       const int nb = (int)std::min<int64_t>(kBlk, n - cj);
-      potrf_block_kernel<<<1, 256, 0, st>>>(A, lda, cj, nb, info);
+      potrf_block_kernel<<<1, 256, 0, aux>>>(A, lda, cj, nb, info);
       ++*kernels;
       const int64_t rb = cj + kBlk;  // first row below the block
       if (rb >= n) break;
-      trsm_block_kernel<<<(unsigned)((n - rb + 127) / 128), 128, 0, st>>>(A, lda, cj, rb, n);
+      trsm_block_kernel<<<(unsigned)((n - rb + kTrsmRows - 1) / kTrsmRows), kTrsmThreads, 0, aux>>>(A, lda, cj, rb,
+                                                                                                      n);
       ++*kernels;
       if ((rc = launch_status()) != QGX_OK) return rc;
-      // the block's columns update the rest of the panel (K = 64)
-      if (rb < pe && (rc = ozaki_update(A, lda, rb, cj, n - rb, pe - rb, kBlk, ws.s_block, ws.e_block, status, st,
-                                        kernels)) != QGX_OK)
-        return rc;
+      if (rb < pe) {  // the block's columns update the rest of the panel (K = 64)
+        if ((rc = slice_panel(A, lda, rb, cj, n - rb, kBlk, ws.s_block, ws.e_block, aux, kernels)) != QGX_OK ||
+            (rc = ozaki_region(A, lda, ws.s_block, ws.e_block, n - rb, rb, kBlk, rb, n - rb, rb, pe - rb, status,
+                               aux, kernels)) != QGX_OK)
+          return rc;
+      }
     }
     if (pe >= n) break;
-    // the panel updates the trailing matrix (K = 256)
-    if ((rc = ozaki_update(A, lda, pe, c0, n - pe, n - pe, kPanel, ws.s_panel, ws.e_panel, status, st, kernels)) !=
-        QGX_OK)
+    // the panel's trailing update (K = 256): the strip on the internal stream, the rest on st
+    const int b = (int)(k & 1);
+    const int64_t ms = n - pe, pe2 = std::min<int64_t>(pe + kPanel, n);
+    if ((rc = slice_panel(A, lda, pe, c0, ms, kPanel, ws.s_panel[b], ws.e_panel[b], aux, kernels)) != QGX_OK ||
+        (rc = ozaki_region(A, lda, ws.s_panel[b], ws.e_panel[b], ms, pe, kPanel, pe, ms, pe, pe2 - pe, status, aux,
+                           kernels)) != QGX_OK)
       return rc;
+    if (pe2 < n) {
+      QGX_CHECK_CUDA(cudaEventRecord(la->strip_done[b], aux));
+      QGX_CHECK_CUDA(cudaStreamWaitEvent(st, la->strip_done[b], 0));
+      if ((rc = ozaki_region(A, lda, ws.s_panel[b], ws.e_panel[b], ms, pe, kPanel, pe2, n - pe2, pe2, n - pe2, status,
+                             st, kernels)) != QGX_OK)
+        return rc;
+      QGX_CHECK_CUDA(cudaEventRecord(la->rest_done[b], st));
+    }
   }
+  QGX_CHECK_CUDA(cudaEventRecord(la->end, aux));
+  QGX_CHECK_CUDA(cudaStreamWaitEvent(st, la->end, 0));
   return launch_status();
 }
 

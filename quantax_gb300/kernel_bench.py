@@ -9,6 +9,7 @@
     python -m quantax_gb300.kernel_bench rc_eloc --ns 16384
     python -m quantax_gb300.kernel_bench rc_jacobian --ns 2048
     python -m quantax_gb300.kernel_bench chol --rows 8192 --k 16640 --reps 3 [--lib]
+    python -m quantax_gb300.kernel_bench dgemm --rows 8192 --reps 3
 
 Prints one JSON line with the mean device time per launch (CUDA events, after warm-up).
 """
@@ -102,7 +103,7 @@ def _resconv(a, st):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["gram", "sweep", "eloc", "obar", "rc_forward", "rc_sweep", "rc_eloc",
-                                       "rc_jacobian", "chol"])
+                                       "rc_jacobian", "chol", "dgemm"])
     ap.add_argument("--lib", action="store_true", help="chol: cuSOLVER's FP64 Xpotrf instead of qgx_cholesky")
     ap.add_argument("--L", type=int, default=10)
     ap.add_argument("--blocks", type=int, default=8)
@@ -135,6 +136,14 @@ def main():
         syrk = float(a.rows) * (a.rows + 1) * a.k
         out.update(mode=a.mode, rows=a.rows, k=a.k, ms=ms, syrk_tflops=syrk / ms / 1e9,
                    gemm_equiv_tflops=2.0 * a.rows * a.rows * a.k / ms / 1e9)
+    elif a.kernel == "dgemm":
+        # the FP64 pipe's rate through the library GEMM (cuBLAS DGEMM via torch.matmul), n^3 square
+        n = a.rows
+        X = torch.randn((n, n), dtype=torch.float64, device="cuda")
+        Y = torch.randn((n, n), dtype=torch.float64, device="cuda")
+        Z = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        ms = _events(lambda: torch.matmul(X, Y, out=Z), a.reps)
+        out.update(n=n, ms=ms, fp64_tflops=2.0 * n ** 3 / ms / 1e9)
     elif a.kernel == "chol":
         # T = G G^T / k + 1e-4 I from an FP32 G of rows x k (the MinSR Gram's structure), factored
         # from a fresh copy every repetition (the copy is timed apart and subtracted)

@@ -66,11 +66,12 @@ FORMS = {
             ("precision_tf32_gram_mixed_solve", "fp32", "tf32", "mixed")],
 }
 
-# DRAM bytes per Gram launch at the bench's shapes, from
+# DRAM bytes per Gram launch at the bench's shapes (profiles/gram_tc_3xtf32_rows8192_k16640.md):
 #   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum --clock-control none \
-#       -k regex:gram_tc -c 3 python -m quantax_gb300.kernel_bench gram --mode 3xtf32 --rows 8192 --k 16640 --reps 1
-# (mean of three launches: 6.98 GB read, 0.51 GB written; the operand is re-read from DRAM ~13x)
-GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 7.49e9}
+#       -k regex:gram_tc -s 2 -c 1 python -m quantax_gb300.kernel_bench gram --mode 3xtf32 --rows 8192 --k 16640 --reps 1
+# rbm (8192 x 16640): 5.42 GB read + 0.51 GB written. resconv (32768 x 34944): the capture at 8192 rows x
+# 34944 (11.38 + 0.51 GB) scaled by (32768 / 8192)^2, the growth of the tile pairs that re-read the operand.
+GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 5.93e9, ("resconv", "3xtf32"): 16 * 11.89e9}
 
 
 def peaks():
@@ -698,7 +699,9 @@ def main():
                 "peak_source": f"bf16 dense burst, {src} (MEASURED_PEAKS.json)",
                 "mode_peak": None if rate is None else bf16 * rate,
                 "frac_of_mode_peak": None if rate is None else achieved / (bf16 * rate),
-                "traffic": GRAM_TRAFFIC_BYTES.get((wl, gram)), "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
+                "traffic": GRAM_TRAFFIC_BYTES.get((wl, gram)),
+                "traffic_unit": ("bytes per launch (ncu dram__bytes_read + write"
+                                 + (", scaled from 8192 rows by the square of the row count)" if wl == "resconv" else ")")),
                 "algorithmic": (f"2 Ns^2 Np = {gram_flop:.3e} FLOP per launch (Ns = {ns} rows, Np = {npar}); operand "
                                 f"{ns * npar * 4:.3e} B read, T {ns * ns * 8:.3e} B written"),
                 "duration": "CUDA events around the Gram phase (one launch) of every timed step, mean",

@@ -204,18 +204,18 @@ __device__ inline void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* 
       : "memory");
 }
 
-__device__ inline void tmem_ld_16cols(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 16 columns of this warp's 32 TMEM lanes into registers, without waiting (tmem_wait_ld makes
+// them usable): several loads can be in flight behind one wait
+__device__ inline void tmem_ld_16cols_nowait(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+
+__device__ inline void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // level l's integer, scaled to 2^(38 - 7 l) (levels 6 and 7 rounded to the nearest 2^-38)
 template <int L>
@@ -322,6 +322,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   double* dt = reinterpret_cast<double*>(smem);  // 128 x 65 doubles over the (finished) stages
   const int q = warp & 3;
   if (warp < 4) {
+    // while the MMAs run: pull this tile's rows of C into L2 for the read-modify-write below
+    for (int rr = q; rr < kOzM; rr += 4) {
+      const int64_t i = row0 + rr;
+      if (i >= m) break;
+      // lanes 0-3: the cache lines holding columns 16 lane .. of the row (every address lies in C)
+      if (lane < 4 && col0 + 16 * lane < ncols)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(C + i * ldc + col0 + 16 * lane));
+    }
     if (!mbar_wait(acc_full, 0)) *fail = 1;
     if (!*fail) {
       tc_fence_after();
@@ -330,22 +338,32 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll 1
       for (int g = 0; g < kOzN / 16; ++g) {
         long long v[16];
-        float f[16];
-#define QGX_OZ_LEVEL(L)                                                          \
-  tmem_ld_16cols(lane_addr + (uint32_t)(kOzN * (L) + 16 * g), f);                \
-  _Pragma("unroll") for (int j = 0; j < 16; ++j) {                               \
-    const long long tv = level_term<L>(__float2int_rn(f[j]));                    \
-    v[j] = (L) == 0 ? tv : v[j] + tv;                                            \
+        // four levels in flight behind one wait, twice
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          uint32_t r[4][16];
+#pragma unroll
+          for (int l4 = 0; l4 < 4; ++l4)
+            tmem_ld_16cols_nowait(lane_addr + (uint32_t)(kOzN * (4 * half + l4) + 16 * g), r[l4]);
+          tmem_wait_ld();
+#define QGX_OZ_LEVEL(L)                                                                   \
+  _Pragma("unroll") for (int j = 0; j < 16; ++j) {                                        \
+    const long long tv = level_term<L>(__float2int_rn(__uint_as_float(r[(L) & 3][j])));  \
+    v[j] = (L) == 0 ? tv : v[j] + tv;                                                     \
   }
-        QGX_OZ_LEVEL(0)
-        QGX_OZ_LEVEL(1)
-        QGX_OZ_LEVEL(2)
-        QGX_OZ_LEVEL(3)
-        QGX_OZ_LEVEL(4)
-        QGX_OZ_LEVEL(5)
-        QGX_OZ_LEVEL(6)
-        QGX_OZ_LEVEL(7)
+          if (half == 0) {
+            QGX_OZ_LEVEL(0)
+            QGX_OZ_LEVEL(1)
+            QGX_OZ_LEVEL(2)
+            QGX_OZ_LEVEL(3)
+          } else {
+            QGX_OZ_LEVEL(4)
+            QGX_OZ_LEVEL(5)
+            QGX_OZ_LEVEL(6)
+            QGX_OZ_LEVEL(7)
+          }
 #undef QGX_OZ_LEVEL
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j) dt[rl * kOzDLd + 16 * g + j] = (double)v[j];
       }

@@ -71,7 +71,7 @@ FORMS = {
 #       -k regex:gram_tc -s 2 -c 1 python -m quantax_gb300.kernel_bench gram --mode 3xtf32 --rows 8192 --k 16640 --reps 1
 # rbm (8192 x 16640): 5.42 GB read + 0.51 GB written. resconv (32768 x 34944): the capture at 8192 rows x
 # 34944 (11.38 + 0.51 GB) scaled by (32768 / 8192)^2, the growth of the tile pairs that re-read the operand.
-GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 5.93e9, ("resconv", "3xtf32"): 16 * 11.89e9}
+GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 4.30e9, ("resconv", "3xtf32"): 16 * 11.89e9}
 
 
 def peaks():

@@ -16,10 +16,25 @@ from __future__ import annotations
 import time
 
 import numpy as np
-import scipy.linalg as sla
 
 from . import philox
 from .rbm import logcosh
+
+
+def spd_solve_inplace(T, b):
+    """y = T^-1 b for a symmetric positive-definite C-ordered T, by LAPACK potrf/potrs on T's
+    own memory (T is overwritten by its factor). T.T is the same buffer in Fortran order and T
+    is symmetric, so no copy of the n x n matrix is made: at n = 32768 the matrix alone is
+    8.6 GB, and a copying solve runs out of host memory. Same factorisation as the reference's
+    jax.scipy.linalg.solve(assume_a="pos") (quantax/optimizer/solver.py:50-62)."""
+    from scipy.linalg import lapack
+    c, info = lapack.dpotrf(T.T, lower=1, clean=0, overwrite_a=1)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"potrf info {info}")
+    y, info = lapack.dpotrs(c, np.asarray(b, dtype=np.float64), lower=1)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"potrs info {info}")
+    return y
 
 
 def sweep(W, b, s, nsteps, seed, step0=0, reweight=2.0):
@@ -69,7 +84,7 @@ def sr_step(W, b, s, seed, step0, nsteps, ashift=1e-4, lr=1e-2, timings=None):
     T = Ob @ Ob.T
     t4 = time.perf_counter()
     T[np.diag_indices_from(T)] += 1e-12 * np.trace(T) + ashift
-    y = sla.solve(T, eb, assume_a="pos")
+    y = spd_solve_inplace(T, eb)
     x = Ob.T @ y
     t5 = time.perf_counter()
     M, N = W.shape
@@ -225,7 +240,7 @@ def resconv_sr_step(params, s, lp, L, nblocks, channels, nbr, bonds, Jb, seed, s
     T = A @ A.T
     t5 = time.perf_counter()
     T[np.diag_indices_from(T)] += 1e-12 * np.trace(T) + ashift
-    y = sla.solve(T, b, assume_a="pos", overwrite_a=True, check_finite=False)
+    y = spd_solve_inplace(T, b)
     x = A.T @ y
     t6 = time.perf_counter()
     params = (np.asarray(params, np.float32) - (lr * x).astype(np.float32)).astype(np.float32)

@@ -1,6 +1,7 @@
 // Tensor-core Gram matrix T = A A^T on sm_103a with tcgen05 (quantax/optimizer/solver.py:139).
 //
-// One CTA computes one 128 x 128 tile of T on or below the diagonal:
+// One CTA computes one 128 x 128 tile of T on or below the diagonal (tiles taken in 8 x 8
+// super-blocks, so that concurrently resident CTAs share operand panels in L2):
 //   warp 4 / lane 0  TMA producer: 128 x 128-byte K-major tiles of the row block and of the
 //                    column block, 128B-swizzled, into a ring of kStages shared-memory stages;
 //   warp 5 / lane 0  MMA issuer: tcgen05.mma M=128 N=128 (K = 8 for tf32, 16 for bf16; four
@@ -30,6 +31,7 @@ namespace qgx {
 namespace {
 
 constexpr int kTile = 128;          // rows / columns of a T tile
+constexpr int kGroup = 8;           // tiles per side of a rasterisation super-block
 constexpr int kRowBytes = 128;      // bytes of one operand row per k-block (one swizzle atom)
 constexpr int kBlockBytes = kTile * kRowBytes;  // one operand block of a stage
 // KIND 0: tf32, 1: bf16, 2: split tf32 (hi*hi + hi*lo + lo*hi, FP32-class accuracy)
@@ -104,12 +106,16 @@ __global__ void __launch_bounds__(GramCfg<KIND>::kThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
   volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
-  // lower-triangular tile index -> (bi, bj), bi >= bj
-  const int64_t tile = blockIdx.x;
-  int64_t bi = (int64_t)((sqrt(8.0 * (double)tile + 1.0) - 1.0) * 0.5);
-  while ((bi + 1) * (bi + 2) / 2 <= tile) ++bi;
-  while (bi * (bi + 1) / 2 > tile) --bi;
-  const int64_t bj = tile - bi * (bi + 1) / 2;
+  // block index -> tile (bi, bj), bi >= bj, grouped: kGroup x kGroup super-blocks in lower-
+  // triangular order, row-major inside, so that the CTAs resident at once share a few row and
+  // column panels of the operand in L2; blocks past the matrix or above the diagonal exit
+  const int64_t sb = blockIdx.x / (kGroup * kGroup), w = blockIdx.x % (kGroup * kGroup);
+  int64_t si = (int64_t)((sqrt(8.0 * (double)sb + 1.0) - 1.0) * 0.5);
+  while ((si + 1) * (si + 2) / 2 <= sb) ++si;
+  while (si * (si + 1) / 2 > sb) --si;
+  const int64_t sj = sb - si * (si + 1) / 2;
+  const int64_t bi = si * kGroup + w / kGroup, bj = sj * kGroup + w % kGroup;
+  if (bi * kTile >= n || bj > bi) return;
   const int row0 = (int)(bi * kTile), col0 = (int)(bj * kTile);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -316,7 +322,9 @@ int launch_gram_tc(const void* A, int64_t rows, int64_t k, int64_t lda, double* 
                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) return QGX_ERR_UNSUPPORTED;
   const int64_t nb = (rows + kTile - 1) / kTile;
-  const int64_t tiles = nb * (nb + 1) / 2;
+  const int64_t ns = (nb + kGroup - 1) / kGroup;  // super-blocks per side
+  const int64_t tiles = ns * (ns + 1) / 2 * kGroup * kGroup;
+  if (tiles > 0x7fffffffLL) return QGX_ERR_UNSUPPORTED;
   const int64_t nkb = (k + elems - 1) / elems;
   auto kern = gram_tc_kernel<KIND>;
   constexpr size_t smem = GramCfg<KIND>::kSmem;

@@ -71,7 +71,7 @@ FORMS = {
 #       -k regex:gram_tc -s 2 -c 1 python -m quantax_gb300.kernel_bench gram --mode 3xtf32 --rows 8192 --k 16640 --reps 1
 # rbm (8192 x 16640): 5.42 GB read + 0.51 GB written. resconv (32768 x 34944): the capture at 8192 rows x
 # 34944 (11.38 + 0.51 GB) scaled by (32768 / 8192)^2, the growth of the tile pairs that re-read the operand.
-GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 4.30e9, ("resconv", "3xtf32"): 16 * 11.89e9}
+GRAM_TRAFFIC_BYTES = {("rbm", "3xtf32"): 4.30e9, ("resconv", "3xtf32"): 4 * (32.79e9 + 2.14e9)}
 
 
 def peaks():
@@ -184,8 +184,9 @@ def _host_threads():
 
 
 def time_cpu_steps(workload: str, chains: int, max_steps: int, budget_s: float):
-    """Whole SR steps of the CPU restatement: as many as `max_steps`, stopping once `budget_s`
-    has been spent (at least one). Returns (steps, seconds, per-phase mean seconds, energies)."""
+    """Whole SR steps of the CPU restatement: as many as `max_steps`, stopping before a step that
+    would end past `budget_s` at the pace of the steps so far (at least one step runs). Returns
+    (steps, seconds, per-phase mean seconds, energies)."""
     w = CpuWorkload(workload, chains)
     times, phases, energies = [], {}, []
     while len(times) < max(1, max_steps):
@@ -195,7 +196,7 @@ def time_cpu_steps(workload: str, chains: int, max_steps: int, budget_s: float):
         times.append(time.perf_counter() - t0)
         for k, v in tm.items():
             phases[k] = phases.get(k, 0.0) + v
-        if sum(times) > budget_s:
+        if sum(times) + sum(times) / len(times) > budget_s:
             break
     n = len(times)
     return n, sum(times), {k: v / n for k, v in phases.items()}, energies
@@ -424,6 +425,8 @@ def run_trajectory(args, rank):
         sampler = qtx.sampler.SpinExchange(state, args.chains, thermal_steps=200, sweep_steps=200)
         if solve == "pinv":  # config 4's FP64 pseudo-inverse: eigendecomposition with rtol 1e-12
             solver = qtx.optimizer.minnorm_pinv_eig(rtol=1e-12)
+        elif solve == "pinv_atol":  # the same with the soft cutoff also at the shift's scale, 1e-4
+            solver = qtx.optimizer.minnorm_pinv_eig(rtol=1e-12, atol=1e-4)
         else:
             solver = qtx.optimizer.minnorm_shift_eig(ashift=1e-4, precision=solve)
         opt = qtx.optimizer.SR(state, H, solver=solver, gram=gram)
@@ -637,10 +640,11 @@ def main():
     ap.add_argument("--example-steps", type=int, default=1000, help="rbm_example: SR steps")
     ap.add_argument("--jobs", type=int, default=8, help="serving: number of jobs in the stream")
     ap.add_argument("--chains", type=int, default=2048, help="trajectory: Markov chains (samples per step)")
-    ap.add_argument("--forms", default="plain:fp32:fp32:fp64,precision_bf16:bf16:bf16:mixed,"
-                                       "precision_tf32:tf32:tf32:mixed",
-                    help="trajectory: comma-separated name:conv:gram:solve (solve fp64, fp64_lib, mixed or pinv: "
-                         "the FP64 pseudo-inverse with rtol 1e-12); the first is the reference run")
+    ap.add_argument("--forms", default="plain:fp32:3xtf32:fp64,precision_bf16:bf16:bf16:mixed,"
+                                       "precision_tf32:tf32:tf32:mixed,precision_bf16_pinv:bf16:bf16:pinv",
+                    help="trajectory: comma-separated name:conv:gram:solve (solve fp64, fp64_lib, mixed, pinv: "
+                         "the FP64 pseudo-inverse with rtol 1e-12, or pinv_atol: the same with atol 1e-4); "
+                         "the first is the reference run")
     ap.add_argument("--job-steps", type=int, default=50, help="serving: SR steps per job")
     args = ap.parse_args()
 

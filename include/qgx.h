@@ -223,6 +223,14 @@ int64_t qgx_resconv_table_floats(int32_t nblocks, int32_t channels);
 #define QGX_CONV_FP32 0
 #define QGX_CONV_TF32 1
 #define QGX_CONV_BF16 2
+/* OR'd into QGX_CONV_BF16: run the warp-specialised tensor-core kernel (one CTA per SM with
+ * three sample groups, one MMA warp serving them as their inputs become ready, all layers'
+ * weights resident) instead of the default per-layer-synchronous one (three CTAs per SM, each
+ * issuing a layer's MMAs and then running its epilogue). Both give bit-identical results; on
+ * GB300 the grouped kernel is slower (1.13 against 0.82 ms for 16384 forwards at L = 10,
+ * 8 blocks, 16 channels): one issuing thread takes about 115 clocks per N = 16 MMA, three
+ * CTAs issuing side by side about 47. */
+#define QGX_CONV_GROUPED 0x100
 /* Reorder the parameters into the kernels' table (FP32 layers, then the BF16 and TF32
  * weight images of the tensor-core forward); re-run after every parameter update. */
 int qgx_resconv_prepare(const float* params, int32_t nblocks, int32_t channels, float* table,

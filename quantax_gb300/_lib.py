@@ -34,6 +34,7 @@ GRAM_FP64 = 4
 CONV_FP32 = 0
 CONV_TF32 = 1
 CONV_BF16 = 2
+CONV_GROUPED = 0x100  # OR'd into CONV_BF16: the warp-specialised kernel
 RESCONV_COMPLEX = 1
 RESCONV_SINHP1 = 2
 

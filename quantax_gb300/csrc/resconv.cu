@@ -35,11 +35,13 @@ struct ConvNet {
   bool cplx;
   int prec;     // QGX_CONV_*: arithmetic of the forward convolutions
   bool sinhp1;  // final activation sinhp1_by_scale instead of exp_by_scale
+  bool grouped;  // QGX_CONV_GROUPED: the warp-specialised BF16 kernel
 };
 
 // the complex_out argument of the entry points: QGX_RESCONV_COMPLEX | QGX_RESCONV_SINHP1
 inline ConvNet make_net(int L, int B, int C, int out_flags, int prec) {
-  return ConvNet{L, L * L, B, C, (out_flags & QGX_RESCONV_COMPLEX) != 0, prec, (out_flags & QGX_RESCONV_SINHP1) != 0};
+  return ConvNet{L, L * L, B, C, (out_flags & QGX_RESCONV_COMPLEX) != 0, prec & ~QGX_CONV_GROUPED,
+                 (out_flags & QGX_RESCONV_SINHP1) != 0, (prec & QGX_CONV_GROUPED) != 0};
 }
 
 __host__ __device__ inline int64_t nparams_rc(int B, int C) {
@@ -775,7 +777,7 @@ int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, 
                    float2* out, cudaStream_t st) {
   if (net.prec != QGX_CONV_FP32)
     return rc_launch_forward_tc(table, net.L, net.B, net.C, net.cplx, net.sinhp1, cfg, ncfg, n_live, out,
-                                net.prec == QGX_CONV_BF16 ? 1 : 0, st);
+                                net.prec == QGX_CONV_BF16 ? 1 : 0, net.grouped, st);
   switch (net.C) {
     case 4: return launch_forward_c<4>(table, net, cfg, ncfg, n_live, out, st);
     case 8: return launch_forward_c<8>(table, net, cfg, ncfg, n_live, out, st);
@@ -846,7 +848,9 @@ bool valid_net(int L, int B, int C, int out_flags) {
          (!(out_flags & QGX_RESCONV_COMPLEX) || C % 2 == 0);
 }
 
-bool valid_prec(int p) { return p == QGX_CONV_FP32 || p == QGX_CONV_TF32 || p == QGX_CONV_BF16; }
+bool valid_prec(int p) {
+  return p == QGX_CONV_FP32 || p == QGX_CONV_TF32 || p == QGX_CONV_BF16 || p == (QGX_CONV_BF16 | QGX_CONV_GROUPED);
+}
 
 constexpr int kMaxSymm = 1024;
 

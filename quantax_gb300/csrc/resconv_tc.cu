@@ -302,6 +302,8 @@ struct TcForward {
         // below 256 KB, so the additions never leave the 14-bit field)
         const uint64_t da0 = desc_noswizzle(smem_u32(in) + kGuard * 16, (uint32_t)plane, 128);
         const uint64_t db0 = desc_noswizzle(smem_u32(W + buf * sh.wbuf), 256, 128);
+        // tile-major: a tile's nine taps back to back (measured on GB300: issuing tap-major,
+        // alternating accumulators, is 12% slower; the taps of one tile read nearly the same rows)
         for (int j = 0; j < sh.ntiles; ++j) {
           const uint64_t daj = da0 + (uint64_t)(j * 128);
           const uint32_t dj = tmem + (uint32_t)(16 * j);
@@ -465,6 +467,325 @@ __global__ void __launch_bounds__(128 * WG, MINB)
   f.teardown();
 }
 
+// ---- warp-specialised forward (BF16, QGX_CONV_GROUPED) --------------------------------
+// Measured on GB300 to be slower than TcForward's three CTAs per SM (1.13 against 0.82 ms for
+// 16384 forwards at L = 10, 8 blocks, 16 channels): a single
+// issuing thread gets about 115 clocks per N = 16 MMA, where three CTAs issuing side by side get
+// about 47 between them. It runs on request, and its bit-identical results check TcForward.
+// One CTA per SM holds kWsGroups independent sample groups: each group has the S samples and
+// ntiles tiles of a TcShape, its own P and Q buffers, its own TMEM accumulator columns and two
+// barriers (`full`: the group's convolution has finished, signalled by tcgen05.commit;
+// `ready`: the group's 256 epilogue threads have written the next convolution's input). One
+// MMA warp serves the groups in whatever order they become ready, so the tensor core works
+// on one group's layer while the other groups run their epilogues; the weights of every
+// layer stay resident in shared memory, loaded once per CTA. The epilogue arithmetic, the
+// halo-padded layout and the log-sum-exp are those of TcForward.
+// G groups of WG warpgroups, RPT tile rows per thread (a group holds up to WG * RPT tiles)
+template <int G, int WG, int RPT>
+struct WsCfg {
+  static constexpr int kGroupThreads = 128 * WG;
+  static constexpr int kMmaWarp = G * kGroupThreads / 32;
+  static constexpr int kThreads = G * kGroupThreads + 32;
+};
+// the launch shape (G = 3 groups of 3 samples at L = 10: the per-layer-synchronous kernel's
+// three CTAs per SM, in one CTA)
+constexpr int kWsG = 3, kWsWG = 2, kWsRPT = 2;
+
+struct WsShape {
+  TcShape sh;   // one group's shape (its own buffer offsets are not used)
+  int lb;       // bytes of one layer's weight image
+  int oG;       // byte offset of group 0's P and Q; group g at oG + g * gbytes
+  int gbytes;   // P and Q of one group
+  int oBar;     // barriers, TMEM slot, failure flag
+  int smem;
+  uint32_t tmem_cols;
+};
+
+// false when the shape does not fit (shared memory, TMEM, the log-sum-exp scratch)
+template <int G, int WG, int RPT>
+inline bool ws_shape(int L, int B, int C, bool cplx, WsShape* w) {
+  constexpr int tiles = WG * RPT;
+  if ((L + 2) * (L + 2) > tiles * 128) return false;
+  w->sh = tc_shape(L, B, C, cplx, 2, tc_samples_per_cta(L, tiles));
+  const TcShape& sh = w->sh;
+  if (sh.ntiles > tiles) return false;
+  auto al = [](int x, int a) { return (x + a - 1) / a * a; };
+  w->lb = (int)tc_layer_bytes(2);
+  const int plane = sh.rows_tot * 16;
+  w->oG = al(2 * B * w->lb, 128);
+  w->gbytes = al(2 * 2 * plane, 128);  // P and Q, two 16-byte chunk planes each
+  w->oBar = w->oG + G * w->gbytes;
+  w->smem = w->oBar + 64 + 1024;
+  uint32_t cols = 32;
+  while (cols < (uint32_t)(G * sh.ntiles * 16)) cols <<= 1;
+  w->tmem_cols = cols;
+  return w->smem <= 227 * 1024 && w->smem <= device_max_smem_optin() && cols <= 512 &&
+         sh.S * sh.C * sh.N * 4 <= w->gbytes;
+}
+
+// non-blocking probe of an mbarrier phase
+__device__ inline bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ inline void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ inline void group_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// barrier over the group's threads that also ORs a flag across them (the same result in all)
+__device__ inline bool group_sync_or(int id, int n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
+
+template <int G, int WG, int RPT>
+__global__ void __launch_bounds__(WsCfg<G, WG, RPT>::kThreads, 1)
+    rc_forward_ws_kernel(const uint8_t* __restrict__ wimg, WsShape ws, const uint32_t* __restrict__ cfg,
+                         int64_t ncfg, const int64_t* __restrict__ n_live, float2* __restrict__ out) {
+  using Cfg = TcCfg<1>;
+  constexpr int kWsGroups = G, kWsWG = WG, kWsRPT = RPT;
+  constexpr int kWsGroupThreads = WsCfg<G, WG, RPT>::kGroupThreads, kWsMmaWarp = WsCfg<G, WG, RPT>::kMmaWarp;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = aligned_smem(smem_raw);
+  const TcShape& sh = ws.sh;
+  uint8_t* W = sm;
+  uint64_t* wbar = reinterpret_cast<uint64_t*>(sm + ws.oBar);
+  uint64_t* full = wbar + 1;
+  uint64_t* ready = full + kWsGroups;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ready + kWsGroups);
+  volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int S = sh.S, nw = words_for(sh.N), nlayers = 2 * sh.B, plane = sh.rows_tot * 16;
+  const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
+  const int64_t stride = (int64_t)gridDim.x * kWsGroups * S;  // samples per round of all groups
+  const bool any_work = (int64_t)blockIdx.x * kWsGroups * S < total;
+
+  // zeroed activation buffers (guard and padding rows stay finite), barriers, TMEM, weights
+  for (int e = tid; e < kWsGroups * ws.gbytes / 16; e += blockDim.x)
+    reinterpret_cast<uint4*>(sm + ws.oG)[e] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    mbar_init(wbar, 1);
+    for (int g = 0; g < kWsGroups; ++g) {
+      mbar_init(full + g, 1);
+      mbar_init(ready + g, kWsGroupThreads / 32);  // one arrival per epilogue warp
+    }
+    *fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(ws.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  if (tid == 0 && any_work) {
+    mbar_expect_tx(wbar, (uint32_t)(nlayers * ws.lb));
+    bulk_load(W, wimg, (uint32_t)(nlayers * ws.lb), wbar);
+  }
+
+  if (warp == kWsMmaWarp) {
+    // ---- MMA warp: one elected lane issues every group's convolutions ----
+    if (lane == 0 && any_work) {
+      int64_t left[kWsGroups];
+      uint32_t lc[kWsGroups];
+      int layer[kWsGroups];
+      uint64_t daP[kWsGroups], daQ[kWsGroups];  // A descriptors of each group's P and Q at row 0
+#pragma unroll
+      for (int g = 0; g < kWsGroups; ++g) {
+        const int64_t b0 = ((int64_t)blockIdx.x * kWsGroups + g) * S;
+        left[g] = b0 < total ? (total - b0 + stride - 1) / stride * nlayers : 0;
+        lc[g] = 0;
+        layer[g] = 0;
+        const uint32_t pg = smem_u32(sm + ws.oG + g * ws.gbytes) + kGuard * 16;
+        daP[g] = desc_noswizzle(pg, (uint32_t)plane, 128);
+        daQ[g] = desc_noswizzle(pg + 2 * plane, (uint32_t)plane, 128);
+      }
+      if (!mbar_wait(wbar, 0)) *fail = 1;
+      const uint64_t db_base = desc_noswizzle(smem_u32(W), 256, 128);
+      uint64_t t_last = global_timer();
+      while (!*fail) {
+        bool pending = false, progressed = false;
+#pragma unroll
+        for (int g = 0; g < kWsGroups; ++g) {
+          if (left[g] == 0) continue;
+          pending = true;
+          if (!mbar_test(ready + g, lc[g] & 1)) continue;
+          tc_fence_after();
+          const int l = layer[g];
+          const uint64_t da0 = (l & 1) ? daQ[g] : daP[g];
+          const uint64_t db0 = db_base + (uint64_t)((l * ws.lb) >> 4);
+          const uint32_t d0 = tmem + (uint32_t)(g * sh.ntiles * 16);
+          for (int j = 0; j < sh.ntiles; ++j) {  // tile-major, as in TcForward::conv
+            const uint64_t daj = da0 + (uint64_t)(j * 128);
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+              const int off = (t / 3 - 1) * sh.Lp + (t % 3 - 1);
+              mma_tc<1>(d0 + (uint32_t)(16 * j), daj + (uint64_t)(int64_t)off,
+                        db0 + (uint64_t)(t * Cfg::chunks * 16), t > 0 ? 1u : 0u);
+            }
+          }
+          mma_commit(full + g);
+          layer[g] = l + 1 == nlayers ? 0 : l + 1;
+          ++lc[g];
+          --left[g];
+          progressed = true;
+        }
+        if (!pending) break;
+        if (progressed) {
+          t_last = global_timer();
+        } else if (global_timer() - t_last > kWaitLimitNs) {
+          *fail = 1;
+        }
+      }
+      // after a failure: no MMA may still run when TMEM is released
+#pragma unroll
+      for (int g = 0; g < kWsGroups; ++g)
+        if (*fail && lc[g] > 0) mbar_wait(full + g, (lc[g] - 1) & 1);
+    }
+  } else {
+    // ---- epilogue: the 256 threads of group g ----
+    const int g = warp / (4 * kWsWG);
+    const int tg = tid - g * kWsGroupThreads;
+    const int wg = tg >> 7, row_in_tile = tg & 127;
+    const uint32_t tl = tmem + (uint32_t)(g * sh.ntiles * 16) + ((uint32_t)(32 * (warp & 3)) << 16);
+    uint8_t* P = sm + ws.oG + g * ws.gbytes;
+    uint8_t* Q = P + 2 * plane;
+    const int L = sh.L, N = sh.N;
+    int64_t base = ((int64_t)blockIdx.x * kWsGroups + g) * S;
+    bool bad = any_work && !mbar_wait(wbar, 0);  // the biases are read from the weight image
+    uint32_t conv = 0;
+    float x[kWsRPT][16];
+    int pos[kWsRPT];
+    // the input of a forward: x = s on the C channels; P = s / sqrt 2 on channel 0
+    auto load_input = [&](int64_t b0) {
+      const int s_here = (int)(total - b0 < S ? total - b0 : S);
+      const uint32_t* c0 = cfg + b0 * nw;
+#pragma unroll
+      for (int k = 0; k < kWsRPT; ++k) {
+        const int j = wg + kWsWG * k;
+        pos[k] = j < sh.ntiles ? pack_pos(row_pos(j * 128 + row_in_tile, sh, s_here)) : -1;
+        const RowPos rp = unpack_pos(pos[k]);
+        if (!rp.live) continue;
+        const int r = (rp.py - 1) * L + (rp.px - 1);
+        const float sv = ((c0[rp.a * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
+        float v[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          x[k][c] = c < sh.C ? sv : 0.0f;
+          v[c] = c == 0 ? sv * 0.70710678118654752f : 0.0f;
+        }
+        put_row<1>(P, sh, rp, v);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(ready + g);
+    };
+    if (!bad && base < total) load_input(base);
+    for (; base < total; base += stride) {
+      for (int l = 0; l < nlayers && !bad; ++l) {
+        if (!mbar_wait(full + g, conv & 1)) {
+          bad = true;
+          break;
+        }
+        ++conv;
+        tc_fence_after();
+        const int b = l >> 1;
+        const float* bias = reinterpret_cast<const float*>(W + l * ws.lb + 9 * Cfg::chunks * 256);
+        const float scale = rsqrtf((float)(b + 2));
+#pragma unroll
+        for (int k = 0; k < kWsRPT; ++k) {
+          const int j = wg + kWsWG * k;
+          if (j >= sh.ntiles) break;
+          float v[16];
+          tmem_ld_16cols(tl + (uint32_t)(16 * j), v);
+          const RowPos rp = unpack_pos(pos[k]);
+          if (!rp.live) continue;
+          if ((l & 1) == 0) {  // conv1: Q = gelu(conv(P) + b1)
+#pragma unroll
+            for (int c = 0; c < 16; ++c) v[c] = gelu_op<1>(v[c] + bias[c]);
+            put_row<1>(Q, sh, rp, v);
+          } else {  // conv2: x += conv(Q) + b2; the next block's P = gelu(x / sqrt(b + 2))
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              x[k][c] += v[c] + bias[c];
+              v[c] = gelu_op<1>(x[k][c] * scale);
+            }
+            if (b + 1 < sh.B) put_row<1>(P, sh, rp, v);
+          }
+        }
+        if (l + 1 < nlayers) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(ready + g);
+        }
+      }
+      // the same decision in every thread of the group before its named barriers
+      if (group_sync_or(1 + g, kWsGroupThreads, bad || *fail != 0)) {
+        bad = true;
+        break;
+      }
+      tc_fence_before();
+      // log sum exp over (channel, site) per sample, z = x / sqrt(B + 1) gathered over P and Q
+      // (all of this group's convolutions have finished, and the MMA warp reads them again
+      // only after the next input has been written and signalled)
+      const int s_here = (int)(total - base < S ? total - base : S);
+      float* Z = reinterpret_cast<float*>(P);
+      const float fs = rsqrtf((float)(sh.B + 1));
+#pragma unroll
+      for (int k = 0; k < kWsRPT; ++k) {
+        const RowPos rp = unpack_pos(pos[k]);
+        if (!rp.live) continue;
+        const int r = (rp.py - 1) * L + (rp.px - 1);
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (c < sh.C) Z[(rp.a * sh.C + c) * N + r] = x[k][c] * fs;
+      }
+      group_sync(1 + g, kWsGroupThreads);
+      const int cp = sh.cplx ? sh.C / 2 : sh.C;
+      for (int a = tg >> 5; a < s_here; a += kWsGroupThreads / 32) {
+        const float2 lp = rc_warp_log_psi(Z + a * sh.C * N, cp * N, 1.0f, sh.cplx, sh.sinhp1, lane);
+        if (lane == 0) out[base + a] = lp;
+      }
+      group_sync(1 + g, kWsGroupThreads);  // Z is overwritten by the next input
+      if (base + stride < total) load_input(base + stride);
+    }
+    if (bad) {
+      // a wait timed out: this group's remaining outputs become NaN, so the failure shows in
+      // every energy and update computed from them
+      for (; base < total; base += stride)
+        for (int a = tg; a < S && base + a < total; a += kWsGroupThreads) out[base + a] = make_float2(NAN, NAN);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ws.tmem_cols) : "memory");
+  }
+}
+
 // weight images for the tensor-core kernels from the FP32 table slices
 __global__ void rc_tc_image_kernel(float* __restrict__ table, int B, int C) {
   uint8_t* tb = reinterpret_cast<uint8_t*>(table);
@@ -536,10 +857,29 @@ int tc_smem_request(const TcShape& sh) {
   return std::max(sh.smem, std::min(device_max_smem_optin(), (227 * 1024) / (TcLaunch<KIND>::CTAS + 1) + 1024));
 }
 
+// the warp-specialised BF16 forward; QGX_ERR_UNSUPPORTED when its shape does not fit
+int launch_ws(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg, int64_t ncfg,
+              const int64_t* n_live, float2* out, cudaStream_t st) {
+  WsShape ws;
+  if (!ws_shape<kWsG, kWsWG, kWsRPT>(L, B, C, cplx, &ws)) return QGX_ERR_UNSUPPORTED;
+  ws.sh.sinhp1 = sinhp1;
+  const uint8_t* wimg = reinterpret_cast<const uint8_t*>(table) + tc_image_offset(B, C, 1);
+  auto k = rc_forward_ws_kernel<kWsG, kWsWG, kWsRPT>;
+  QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, ws.smem));
+  const int64_t blocks = (ncfg + ws.sh.S - 1) / ws.sh.S;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(device_sm_count(), (blocks + kWsG - 1) / kWsG));
+  k<<<grid, WsCfg<kWsG, kWsWG, kWsRPT>::kThreads, ws.smem, st>>>(wimg, ws, cfg, ncfg, n_live, out);
+  return launch_status();
+}
+
 template <int KIND>
 int launch_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg, int64_t ncfg,
-              const int64_t* n_live, float2* out, cudaStream_t st) {
+              const int64_t* n_live, float2* out, bool grouped, cudaStream_t st) {
   using T = TcLaunch<KIND>;
+  if (KIND == 1 && grouped) {
+    const int rc = launch_ws(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, st);
+    if (rc != QGX_ERR_UNSUPPORTED) return rc;
+  }
   TcShape sh;
   if (!tc_launch_shape<KIND>(L, B, C, cplx, &sh)) return QGX_ERR_UNSUPPORTED;
   sh.sinhp1 = sinhp1;
@@ -556,10 +896,10 @@ int launch_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, c
 }  // namespace
 
 int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg,
-                         int64_t ncfg, const int64_t* n_live, float2* out, int kind, cudaStream_t st) {
+                         int64_t ncfg, const int64_t* n_live, float2* out, int kind, bool grouped, cudaStream_t st) {
   if (C < 1 || C > kCh || L < 3 || L + 3 > kGuard) return QGX_ERR_UNSUPPORTED;
-  if (kind == 1) return launch_tc<1>(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, st);
-  return launch_tc<0>(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, st);
+  if (kind == 1) return launch_tc<1>(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, grouped, st);
+  return launch_tc<0>(table, L, B, C, cplx, sinhp1, cfg, ncfg, n_live, out, false, st);
 }
 
 }  // namespace qgx

@@ -61,7 +61,8 @@ def _resconv(a, st):
     spins = torch.empty((ns, (n + 31) // 32), dtype=torch.int32, device="cuda")
     L.call("qgx_spins_init_fixed_up", L.ptr(spins), ns, n, n // 2, 5, st)
     flop_fwd = 2.0 * n * 9 * Cc * (1 + (2 * B - 1) * Cc)  # 2 x MACs per forward
-    prec = {"fp32": L.CONV_FP32, "tf32": L.CONV_TF32, "bf16": L.CONV_BF16}[a.conv]
+    prec = {"fp32": L.CONV_FP32, "tf32": L.CONV_TF32, "bf16": L.CONV_BF16,
+            "bf16_grouped": L.CONV_BF16 | L.CONV_GROUPED}[a.conv]
     res = dict(ns=ns, L=Ls, blocks=B, channels=Cc, conv=a.conv, flop_per_forward=flop_fwd)
     if a.kernel == "rc_forward":
         lp = torch.empty((ns, 2), dtype=torch.float32, device="cuda")
@@ -109,7 +110,7 @@ def main():
     ap.add_argument("--blocks", type=int, default=8)
     ap.add_argument("--channels", type=int, default=16)
     ap.add_argument("--mode", default="tf32", choices=["fp32", "tf32", "bf16", "3xtf32"])
-    ap.add_argument("--conv", default="fp32", choices=["fp32", "tf32", "bf16"],
+    ap.add_argument("--conv", default="fp32", choices=["fp32", "tf32", "bf16", "bf16_grouped"],
                     help="ResConv forward convolution arithmetic")
     ap.add_argument("--rows", type=int, default=2048)
     ap.add_argument("--k", type=int, default=16640)

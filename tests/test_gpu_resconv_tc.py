@@ -19,6 +19,7 @@ from test_gpu_resconv import Net, _pack, _unpack
 pytestmark = pytest.mark.gpu
 
 TF32, BF16 = 1, 2
+GROUPED = 0x100  # QGX_CONV_GROUPED
 TOL_LOGPSI = {TF32: 5e-3, BF16: 4e-2}
 TOL_ELOC = {TF32: 5e-3, BF16: 4e-2}
 
@@ -112,6 +113,34 @@ def test_resconv_local_energy_tensor_cores(cuda, prec, cplx):
     assert np.abs(got - want).max() <= TOL_ELOC[prec] * scale, np.abs(got - want).max() / scale
 
 
+@pytest.mark.parametrize("L,B,Cc,cplx,ns", [(10, 8, 16, True, 16384 + 5), (10, 8, 16, True, 1), (4, 2, 16, True, 300),
+                                            (6, 3, 8, False, 1000), (5, 2, 12, True, 777), (8, 6, 16, True, 4096),
+                                            (3, 1, 16, False, 50), (16, 2, 4, True, 97)])
+def test_bf16_warp_specialised_forward_equals_layer_synchronous(cuda, L, B, Cc, cplx, ns):
+    """The warp-specialised BF16 forward (QGX_CONV_GROUPED: sample groups whose epilogues
+    overlap the other groups' MMAs, one MMA warp, weights resident) and the default per-layer-
+    synchronous kernel run the same arithmetic in the same order: bit-identical log psi for
+    every sample count, including a single sample and ragged last groups."""
+    net = Net(L, B, Cc, cplx, seed=L + B + 1)
+    n = L * L
+    packed = _pack(metropolis.init_fixed_up(ns, n, n // 2, 11))
+    np.testing.assert_array_equal(net.log_psi(packed, BF16), net.log_psi(packed, BF16 | GROUPED))
+
+
+def test_bf16_warp_specialised_forward_sinhp1(cuda):
+    from quantax_gb300 import _lib as Lb
+    net = Net(10, 4, 16, True, seed=3)
+    packed = _pack(metropolis.init_fixed_up(2000, 100, 50, 12))
+    outs = []
+    for prec in (BF16, BF16 | GROUPED):
+        out = torch.empty((packed.shape[0], 2), dtype=torch.float32, device="cuda")
+        Lb.call("qgx_resconv_log_psi", Lb.ptr(net.table), 10, 4, 16, 1 | 2, prec, Lb.ptr(packed), packed.shape[0],
+                Lb.ptr(out), Lb.stream_ptr())
+        outs.append(out.cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert np.isfinite(outs[0]).all()
+
+
 def test_resconv_tensor_core_arguments(cuda):
     from quantax_gb300 import _lib as Lb
     net = Net(4, 1, 8, True)
@@ -119,3 +148,7 @@ def test_resconv_tensor_core_arguments(cuda):
     out = torch.empty((4, 2), dtype=torch.float32, device="cuda")
     rc = Lb.lib().qgx_resconv_log_psi(Lb.ptr(net.table), 4, 1, 8, 1, 7, Lb.ptr(packed), 4, Lb.ptr(out), None)
     assert rc == Lb.QGX_ERR_ARG
+    # the grouped flag selects a BF16 kernel only
+    for prec in (TF32 | GROUPED, GROUPED):
+        rc = Lb.lib().qgx_resconv_log_psi(Lb.ptr(net.table), 4, 1, 8, 1, prec, Lb.ptr(packed), 4, Lb.ptr(out), None)
+        assert rc == Lb.QGX_ERR_ARG

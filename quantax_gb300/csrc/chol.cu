@@ -37,7 +37,9 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "qgx_common.cuh"
 #include "qgx_tc.cuh"
@@ -619,6 +621,90 @@ int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void
   return launch_status();
 }
 
+// ---- factorisation graphs ------------------------------------------------------------
+// A factorisation is a long launch sequence (about 2000 kernels and event operations at
+// n = 32768). Enqueued one by one it fills the device's queue of pending launches, after which
+// every further launch waits for the GPU: the caller's thread is held for the whole
+// factorisation, and callers on other streams (the jobs of a serving loop) cannot get their
+// work queued meanwhile. The sequence is therefore captured once per set of buffers into a
+// CUDA graph (on a private stream, relaxed capture mode; the look-ahead stream joins the capture
+// through its events, which become edges of the graph) and replayed with one launch. Two
+// replays share no stream or event, so factorisations on different streams can overlap.
+namespace {
+
+struct CholKey {
+  double* A;
+  int64_t n, lda;
+  int* info;
+  int32_t* status;
+  void* work;
+  int device;
+  bool operator==(const CholKey& o) const {
+    return A == o.A && n == o.n && lda == o.lda && info == o.info && status == o.status && work == o.work &&
+           device == o.device;
+  }
+};
+
+struct CholGraph {
+  CholKey key;
+  cudaGraphExec_t exec;
+  int64_t kernels;
+  uint64_t last_use;
+};
+
+constexpr int kMaxCholGraphs = 16;
+std::mutex g_chol_graph_mutex;
+std::vector<CholGraph> g_chol_graphs;
+uint64_t g_chol_clock = 0;
+cudaStream_t g_chol_capture[kMaxCholDevices] = {};
+
+}  // namespace
+
+int chol_f64_graph(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
+                   int64_t* kernels) {
+  int dev = 0;
+  QGX_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxCholDevices) return QGX_ERR_UNSUPPORTED;
+  const CholKey key{A, n, lda, info, status, work, dev};
+  std::lock_guard<std::mutex> lock(g_chol_graph_mutex);
+  CholGraph* hit = nullptr;
+  for (auto& e : g_chol_graphs)
+    if (e.key == key) hit = &e;
+  if (!hit) {
+    if (!g_chol_capture[dev]) QGX_CHECK_CUDA(cudaStreamCreateWithFlags(&g_chol_capture[dev], cudaStreamNonBlocking));
+    cudaStream_t cs = g_chol_capture[dev];
+    QGX_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+    int64_t count = 0;
+    const int rc = chol_f64(A, n, lda, info, status, work, cs, &count);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+    if (rc != QGX_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return rc;
+    }
+    QGX_CHECK_CUDA(ce);
+    cudaGraphExec_t exec = nullptr;
+    // the look-ahead chain keeps the priority of the stream it was captured from
+    const cudaError_t ie = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(graph);
+    QGX_CHECK_CUDA(ie);
+    if ((int)g_chol_graphs.size() >= kMaxCholGraphs) {  // evict the least recently used (an
+      // executable graph still running is freed when it completes)
+      auto lru = std::min_element(g_chol_graphs.begin(), g_chol_graphs.end(),
+                                  [](const CholGraph& a, const CholGraph& b) { return a.last_use < b.last_use; });
+      cudaGraphExecDestroy(lru->exec);
+      g_chol_graphs.erase(lru);
+    }
+    g_chol_graphs.push_back(CholGraph{key, exec, count, 0});
+    hit = &g_chol_graphs.back();
+  }
+  hit->last_use = ++g_chol_clock;
+  QGX_CHECK_CUDA(cudaGraphLaunch(hit->exec, st));
+  *kernels += hit->kernels;
+  return QGX_OK;
+}
+
 }  // namespace qgx
 
 using namespace qgx;
@@ -633,7 +719,7 @@ int qgx_cholesky(double* A, int64_t n, int64_t lda, int32_t* info, int32_t* stat
   QGX_CHECK_ARG(workspace_bytes >= chol_f64_workspace_bytes(n));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   int64_t kernels = 0;
-  return chol_f64(A, n, lda, info, status, workspace, as_cuda(stream), &kernels);
+  return chol_f64_graph(A, n, lda, info, status, workspace, as_cuda(stream), &kernels);
 }
 
 }  // extern "C"

@@ -79,10 +79,22 @@ __device__ inline void stage_floats(float* dst, const float* src, int64_t n) {
   for (int64_t e = threadIdx.x; e < n; e += blockDim.x) dst[e] = __ldg(src + e);
 }
 
+// c += a * b on a pair of floats with one packed FP32 instruction (each lane is an IEEE fma,
+// the same result as two fmaf calls, in half the issue slots)
+__device__ inline void fma_pair(float2& c, float2 a, float2 b) {
+  unsigned long long cc, aa, bb;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(cc) : "f"(c.x), "f"(c.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(aa) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(bb) : "f"(b.x), "f"(b.y));
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(cc) : "l"(aa), "l"(bb));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(c.x), "=f"(c.y) : "l"(cc));
+}
+
 // out[a][o][r] = act(sum_{i,tap} W[i][tap][o] in[a][i][nbr(r,tap)] + bias[o]); mode 0: gelu and store,
 // mode 1: accumulate into out (residual add). A thread computes the C outputs of SPT sites
 // r = g + k G (G = ceil(N / SPT)), so consecutive threads gather consecutive sites (no bank
-// conflicts) and every broadcast weight load feeds SPT x 4 FMAs.
+// conflicts) and every broadcast weight load feeds SPT x 4 FMAs, issued as packed pairs of
+// output channels (fma.rn.f32x2).
 template <int C, int SPT>
 __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* __restrict__ out,
                                   const float* __restrict__ w, const int16_t* __restrict__ nbr, int N, int S,
@@ -100,29 +112,30 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
 #pragma unroll
       for (int t = 0; t < 9; ++t) nb[k][t] = nbr[rc * 9 + t];
     }
-    float acc[SPT][C];
+    float2 acc[SPT][C / 2];  // output channels (2 h, 2 h + 1)
 #pragma unroll
     for (int k = 0; k < SPT; ++k)
 #pragma unroll
-      for (int o = 0; o < C; ++o) acc[k][o] = bias[o];
+      for (int h = 0; h < C / 2; ++h) acc[k][h] = make_float2(bias[2 * h], bias[2 * h + 1]);
     const float* ina = in + (int64_t)a * C * N;
     for (int i = 0; i < cin; ++i) {
       const float* ini = ina + i * N;
 #pragma unroll
       for (int t = 0; t < 9; ++t) {
-        float v[SPT];
+        float2 v[SPT];
 #pragma unroll
-        for (int k = 0; k < SPT; ++k) v[k] = ini[nb[k][t]];
+        for (int k = 0; k < SPT; ++k) {
+          const float x = ini[nb[k][t]];
+          v[k] = make_float2(x, x);
+        }
         const float4* wp = reinterpret_cast<const float4*>(w + (i * 9 + t) * C);
 #pragma unroll
         for (int o4 = 0; o4 < C / 4; ++o4) {
           const float4 ww = wp[o4];
 #pragma unroll
           for (int k = 0; k < SPT; ++k) {
-            acc[k][4 * o4] = fmaf(v[k], ww.x, acc[k][4 * o4]);
-            acc[k][4 * o4 + 1] = fmaf(v[k], ww.y, acc[k][4 * o4 + 1]);
-            acc[k][4 * o4 + 2] = fmaf(v[k], ww.z, acc[k][4 * o4 + 2]);
-            acc[k][4 * o4 + 3] = fmaf(v[k], ww.w, acc[k][4 * o4 + 3]);
+            fma_pair(acc[k][2 * o4], v[k], make_float2(ww.x, ww.y));
+            fma_pair(acc[k][2 * o4 + 1], v[k], make_float2(ww.z, ww.w));
           }
         }
       }
@@ -133,10 +146,16 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
       float* oa = out + (int64_t)a * C * N + r[k];
       if (mode == 0) {
 #pragma unroll
-        for (int o = 0; o < C; ++o) oa[o * N] = gelu_tanh(acc[k][o]);
+        for (int h = 0; h < C / 2; ++h) {
+          oa[2 * h * N] = gelu_tanh(acc[k][h].x);
+          oa[(2 * h + 1) * N] = gelu_tanh(acc[k][h].y);
+        }
       } else {
 #pragma unroll
-        for (int o = 0; o < C; ++o) oa[o * N] += acc[k][o];
+        for (int h = 0; h < C / 2; ++h) {
+          oa[2 * h * N] += acc[k][h].x;
+          oa[(2 * h + 1) * N] += acc[k][h].y;
+        }
       }
     }
   }
@@ -538,7 +557,9 @@ __device__ inline void input_grads(const float* __restrict__ g, const float* __r
         }
       }
     }
-    for (int i = 0; i < cin; ++i) gin[((int64_t)k * C + i) * N + r] = acc[i];
+#pragma unroll
+    for (int i = 0; i < C; ++i)  // constant indices keep acc in registers
+      if (i < cin) gin[((int64_t)k * C + i) * N + r] = acc[i];
   }
 }
 

@@ -21,6 +21,9 @@ int trsv_chol_error(int64_t n, void* work, int* host_err, cudaStream_t st);
 int64_t chol_f64_workspace_bytes(int64_t n);
 int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
              int64_t* kernels);
+// chol_f64 captured once per set of buffers into a CUDA graph and replayed (chol.cu)
+int chol_f64_graph(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
+                   int64_t* kernels);
 
 namespace {
 
@@ -598,7 +601,7 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     if (method == QGX_SOLVE_SHIFT) {
       // this library's factorisation: L in the row-major lower triangle = the column-major
       // upper factor cuSOLVER's potrs takes
-      if ((rc = chol_f64(T, n, n, dinfo, nullptr, ws.chol, st, &g_kernels)) != QGX_OK) return rc;
+      if ((rc = chol_f64_graph(T, n, n, dinfo, nullptr, ws.chol, st, &g_kernels)) != QGX_OK) return rc;
       fill = CUBLAS_FILL_MODE_UPPER;
     } else if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus, ws.cus_bytes,
                                 hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS) {

@@ -51,14 +51,14 @@ constexpr int kPanel = 256;                     // columns of one tensor-core tr
 constexpr int kBlk = 64;                        // columns of one FP64 diagonal block
 constexpr int kSlices = 8;                      // BF16 digits per element
 constexpr int kFixBits = 56;                    // kSlices * 7 fraction bits of the sliced rows
-constexpr int kOzM = 128, kOzN = 64, kOzKB = 32;  // tile rows, tile columns, K per stage
-constexpr int kOzStages = 2;
+constexpr int kOzM = 128, kOzN = 32, kOzKB = 32;  // tile rows, tile columns, K per stage
+constexpr int kOzStages = 1;  // two CTAs per SM: one CTA's epilogue overlaps the other's MMAs
 constexpr int kOzABytes = kSlices * kOzM * kOzKB * 2;  // 64 KB
-constexpr int kOzBBytes = kSlices * kOzN * kOzKB * 2;  // 32 KB
+constexpr int kOzBBytes = kSlices * kOzN * kOzKB * 2;  // 16 KB
 constexpr int kOzStageBytes = kOzABytes + kOzBBytes;
 constexpr int kOzThreads = 192;
 constexpr size_t kOzSmem = 1024 + (size_t)kOzStages * kOzStageBytes + 256;
-constexpr uint32_t kOzTmemCols = 512;  // eight 64-column FP32 level accumulators
+constexpr uint32_t kOzTmemCols = kSlices * kOzN;  // eight 32-column FP32 level accumulators
 constexpr int kOzDLd = kOzN + 1;       // doubles per row of the epilogue's transpose tile
 
 inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
@@ -187,15 +187,16 @@ __device__ inline uint64_t desc_sw64(uint32_t saddr) {
   return d;
 }
 
-// BF16 x BF16 -> FP32, K-major A and B, M = 128, N = 64
-constexpr uint32_t kOzIdesc =
-    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzN >> 3) << 17) | ((uint32_t)(kOzM >> 4) << 24);
+// BF16 x BF16 -> FP32, K-major A and B, M = 128, N = n (a multiple of 16, at most 256)
+constexpr uint32_t oz_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kOzM >> 4) << 24);
+}
 
-__device__ inline void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ inline void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kOzIdesc), "r"(accumulate));
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
 __device__ inline void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
@@ -239,7 +240,7 @@ __device__ inline double pow2(int x) {
 // C[i][j] -= sum_k P[a0 + i][k] P[b0 + j][k] for the m x ncols region at C (ldc), where slice
 // row r is the panel's row r; only entries with a0 + i >= b0 + j (on or below the diagonal of the
 // whole matrix) are updated
-__global__ void __launch_bounds__(kOzThreads, 1)
+__global__ void __launch_bounds__(kOzThreads, 2)
     ozaki_syrk_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       const int* __restrict__ ex, int64_t m, int64_t ncols, int a0, int b0, int nkb,
                       double* __restrict__ C, int64_t ldc, int32_t* __restrict__ status) {
@@ -304,14 +305,17 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         const uint32_t base = smem_u32(smem + s * kOzStageBytes);
 #pragma unroll 1
         for (int kk = 0; kk < kOzKB / 16; ++kk) {  // 32 bytes of K per instruction
+          // one MMA per A slice t: B is the slices u = 0 .. 7 - t of the column rows, contiguous
+          // in shared memory (slice u at rows kOzN u ..), so D's column block u is S_t S_u^T and
+          // lands in the accumulator of level t + u (columns kOzN (t + u) ..): levels t .. 7
+          // are one contiguous N = kOzN (8 - t) range. Every level sum stays an integer below
+          // 2^24, so the FP32 accumulation is exact in any order.
+          const uint64_t db = desc_sw64(base + kOzABytes + kk * 32);
 #pragma unroll
           for (int t = 0; t < kSlices; ++t) {
             const uint64_t da = desc_sw64(base + t * (kOzM * kOzKB * 2) + kk * 32);
-#pragma unroll
-            for (int u = 0; u < kSlices - t; ++u) {
-              const uint64_t db = desc_sw64(base + kOzABytes + u * (kOzN * kOzKB * 2) + kk * 32);
-              mma_bf16(tmem + (uint32_t)(kOzN * (t + u)), da, db, (kb == 0 && kk == 0 && t == 0) ? 0u : 1u);
-            }
+            mma_bf16(tmem + (uint32_t)(kOzN * t), da, db, oz_idesc(kOzN * (kSlices - t)),
+                     (kb == 0 && kk == 0 && t == 0) ? 0u : 1u);
           }
         }
         mma_commit(&empty[s]);
@@ -329,7 +333,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       const int64_t i = row0 + rr;
       if (i >= m) break;
       // lanes 0-3: the cache lines holding columns 16 lane .. of the row (every address lies in C)
-      if (lane < 4 && col0 + 16 * lane < ncols)
+      if (lane < kOzN / 16 && col0 + 16 * lane < ncols)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(C + i * ldc + col0 + 16 * lane));
     }
     if (!mbar_wait(acc_full, 0)) *fail = 1;

@@ -781,8 +781,11 @@ int rc_smem_bytes(const ConvNet& net, int S) {
 template <int C>
 int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                      float2* out, cudaStream_t st) {
-  const int S = kFwdSamples;
+  // kFwdSamples per CTA, fewer where their buffers would not fit (L = 16: 4)
+  int S = kFwdSamples;
+  while (S > 1 && rc_smem_bytes(net, S) > device_max_smem_optin()) --S;
   const int smem = rc_smem_bytes(net, S);
+  if (smem > device_max_smem_optin()) return QGX_ERR_UNSUPPORTED;
   auto k = rc_forward_kernel<C>;
   if (smem > 48 * 1024) QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   int per_sm = 0;

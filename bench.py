@@ -719,7 +719,9 @@ def main():
                 "frac_of_mode_peak": None if rate is None else achieved / (bf16 * rate),
                 "traffic": GRAM_TRAFFIC_BYTES.get((wl, gram)),
                 "traffic_unit": ("bytes per launch (ncu dram__bytes_read + write"
-                                 + (", scaled from 8192 rows by the square of the row count)" if wl == "resconv" else ")")),
+                                 + (", the 16384-row capture scaled by (32768 / 16384)^2; "
+                                    "profiles/gram_tc_3xtf32_rows8192_k16640.md)" if wl == "resconv"
+                                    else "; profiles/gram_tc_3xtf32_rows8192_k16640.md)")),
                 "algorithmic": (f"2 Ns^2 Np = {gram_flop:.3e} FLOP per launch (Ns = {ns} rows, Np = {npar}); operand "
                                 f"{ns * npar * 4:.3e} B read, T {ns * ns * 8:.3e} B written"),
                 "duration": "CUDA events around the Gram phase (one launch) of every timed step, mean",

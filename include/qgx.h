@@ -149,6 +149,41 @@ int qgx_rbm_sweep(const float* table, int32_t n, int32_t m, uint32_t* spins, flo
  * generated in-kernel (Operator.Oloc, quantax/operator/operator.py:510-562). */
 int qgx_rbm_eloc(const float* table, int32_t n, int32_t m, const qgx_operator_t* op,
                  const uint32_t* spins, int64_t ns, double* eloc, qgx_stream_t stream);
+
+/* ---- batched RBM sweeps and local energies ---------------------------------------- */
+/* The serving loop's RBM jobs of one step in few launches: every job of one class (hidden-unit
+ * width class, whether its table fits shared memory, proposal kind) runs in one launch, with
+ * the job table passed as a kernel parameter. Each job's results (spins, log psi, accepts;
+ * local energies) are bit-identical to its own qgx_rbm_sweep / qgx_rbm_eloc call. At most
+ * QGX_RBM_BATCH_MAX_JOBS jobs per call; the structs and the operators they point to are read on
+ * the host during the call only. */
+#define QGX_RBM_BATCH_MAX_JOBS 64
+typedef struct {
+  const float* table; /* qgx_rbm_prepare's table */
+  int32_t n, m;
+  uint32_t* spins;    /* ns packed configurations, in / out */
+  float* log_psi;     /* ns, out */
+  int32_t* accepts;   /* ns accept counts, out (may be NULL) */
+  int64_t ns;
+  int32_t nsteps;
+  int32_t proposal;   /* QGX_PROPOSAL_* */
+  uint64_t seed, step0;
+  float reweight;
+  const int32_t* nbr; /* SpinExchange neighbour table (NULL for LocalFlip) */
+  int32_t z, hop;
+} qgx_rbm_sweep_job_t;
+/* launches (may be NULL): the number of kernel launches made */
+int qgx_rbm_sweep_batched(const qgx_rbm_sweep_job_t* jobs, int32_t njobs, int32_t* launches,
+                          qgx_stream_t stream);
+typedef struct {
+  const float* table;
+  int32_t n, m;
+  const qgx_operator_t* op; /* host struct of device tables */
+  const uint32_t* spins;
+  int64_t ns;
+  double* eloc;             /* ns, out */
+} qgx_rbm_eloc_job_t;
+int qgx_rbm_eloc_batched(const qgx_rbm_eloc_job_t* jobs, int32_t njobs, int32_t* launches, qgx_stream_t stream);
 /* Per-sample log-derivatives O (ns x np, row stride ldo floats), np = m*n + m (+ n with
  * the visible bias), parameter order W (row-major), b, a (Variational.jacobian,
  * quantax/state/variational.py:424-511). */

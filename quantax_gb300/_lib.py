@@ -62,6 +62,24 @@ class Symm(C.Structure):
     _fields_ = [("perm", vp), ("weight", vp), ("nperm", i32), ("z2", i32)]
 
 
+class RbmSweepJob(C.Structure):
+    """qgx_rbm_sweep_job_t"""
+    _fields_ = [
+        ("table", vp), ("n", i32), ("m", i32), ("spins", vp), ("log_psi", vp), ("accepts", vp), ("ns", i64),
+        ("nsteps", i32), ("proposal", i32), ("seed", u64), ("step0", u64), ("reweight", f32), ("nbr", vp),
+        ("z", i32), ("hop", i32),
+    ]
+
+
+class RbmElocJob(C.Structure):
+    """qgx_rbm_eloc_job_t"""
+    _fields_ = [("table", vp), ("n", i32), ("m", i32), ("op", C.POINTER(Operator)), ("spins", vp), ("ns", i64),
+                ("eloc", vp)]
+
+
+RBM_BATCH_MAX_JOBS = 64  # QGX_RBM_BATCH_MAX_JOBS
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "qgx_abi_version": (C.c_int, []),
@@ -79,6 +97,8 @@ SIGNATURES = {
     "qgx_rbm_log_psi": (C.c_int, [vp, i32, i32, vp, i64, vp, vp]),
     "qgx_rbm_sweep": (C.c_int, [vp, i32, i32, vp, vp, vp, i64, i32, u64, u64, f32, i32, vp, i32, i32, vp]),
     "qgx_rbm_eloc": (C.c_int, [vp, i32, i32, C.POINTER(Operator), vp, i64, vp, vp]),
+    "qgx_rbm_sweep_batched": (C.c_int, [C.POINTER(RbmSweepJob), i32, C.POINTER(i32), vp]),
+    "qgx_rbm_eloc_batched": (C.c_int, [C.POINTER(RbmElocJob), i32, C.POINTER(i32), vp]),
     "qgx_rbm_jacobian": (C.c_int, [vp, i32, i32, i32, vp, i64, vp, i64, vp]),
     "qgx_rbm_obar_workspace_bytes": (i64, [i32, i32, i64]),
     "qgx_rbm_obar": (C.c_int, [vp, i32, i32, i32, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
@@ -169,6 +189,8 @@ def _kernels(name, args):
         return 3 + (int(args[1]) - 1) // 65535 + 1 if int(args[1]) > 0 else 0
     if name == "qgx_scale_columns":
         return 1 + (int(args[1]) - 1) // 65535 if int(args[1]) > 0 and int(args[2]) > 0 else 0
+    if name in ("qgx_rbm_sweep_batched", "qgx_rbm_eloc_batched"):  # the count the call reports
+        return int(args[2]._obj.value) if args[2] is not None else 0
     if name == "qgx_resconv_sweep":
         return 2 + 3 * int(args[10])  # step base, forward, then propose / forward / accept per step
     if name == "qgx_resconv_sweep_symm":

@@ -379,11 +379,12 @@ __global__ void __launch_bounds__(kOzThreads, 2)
   __syncthreads();  // deltas complete; every role has left its loop
   if (*fail) {
     if (threadIdx.x == 0 && status) atomicExch(status, QGX_ERR_TIMEOUT);
-  } else if (warp < 4) {
-    // C[i][j] -= 2^(e_i + e_j - 52) V_ij on or below the diagonal: warp q takes rows q, q + 4,
-    // ..., eight rows at a time with all their loads of C issued before the first update, so
-    // the loads' latencies overlap (lane l holds columns l and l + 32 of each row)
-    constexpr int kBatch = 8;
+  } else {
+    // C[i][j] -= 2^(e_i + e_j - 52) V_ij on or below the diagonal, by all six warps (the
+    // producer and MMA warps are idle by now): warp w takes rows w, w + 6, ..., eight rows at a
+    // time with all their loads of C issued before the first update, so the loads' latencies
+    // overlap (lane l holds column l of each row)
+    constexpr int kBatch = 8, kRmwWarps = kOzThreads / 32;
     int ej[kOzN / 32];
     bool jin[kOzN / 32];
 #pragma unroll
@@ -393,24 +394,25 @@ __global__ void __launch_bounds__(kOzThreads, 2)
       ej[h] = jin[h] ? ex[b0 + j] : 0;
     }
 #pragma unroll 1
-    for (int rb = q; rb < kOzM; rb += 4 * kBatch) {
+    for (int rb = warp; rb < kOzM; rb += kRmwWarps * kBatch) {
       double cv[kBatch][kOzN / 32];
       bool ok[kBatch][kOzN / 32];
 #pragma unroll
       for (int r = 0; r < kBatch; ++r) {
-        const int64_t i = row0 + rb + 4 * r;
+        const int rr = rb + kRmwWarps * r;  // a row of this tile (rr < kOzM) and of the matrix
+        const int64_t i = row0 + rr;
 #pragma unroll
         for (int h = 0; h < kOzN / 32; ++h) {
           const int64_t j = col0 + 32 * h + lane;
-          ok[r][h] = i < m && jin[h] && b0 + j <= a0 + i;
+          ok[r][h] = rr < kOzM && i < m && jin[h] && b0 + j <= a0 + i;
           cv[r][h] = ok[r][h] ? C[i * ldc + j] : 0.0;
         }
       }
 #pragma unroll
       for (int r = 0; r < kBatch; ++r) {
-        const int rr = rb + 4 * r;
+        const int rr = rb + kRmwWarps * r;
         const int64_t i = row0 + rr;
-        const int ei = i < m ? ex[a0 + i] : 0;
+        const int ei = rr < kOzM && i < m ? ex[a0 + i] : 0;
 #pragma unroll
         for (int h = 0; h < kOzN / 32; ++h) {
           if (!ok[r][h]) continue;

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 
 #include "qgx_colstats.cuh"
@@ -179,15 +180,14 @@ __device__ inline float lane_log_flip2(const RbmTable& T, int mp, int i, float s
 }
 
 // ---------------------------------------------------------------------------------------
-// Metropolis sweep: one warp per chain.
+// Metropolis sweep: one warp per chain. CTA `cta` of `nctas` takes chains cta, cta + nctas, ...
+// (a chain's result depends only on its own configuration and Philox stream, not on the CTA).
 template <int JT, bool SMEM, int NT, int PROP>
-__global__ void __launch_bounds__(NT, 1)
-    sweep_kernel(const float* __restrict__ table, int n, int mp, uint32_t* __restrict__ spins,
-                 float* __restrict__ log_psi, int32_t* __restrict__ accepts, int64_t ns, int nsteps, uint64_t seed,
-                 uint64_t step0, float reweight, const int32_t* __restrict__ nbr, int z, int hop,
-                 int64_t table_nf) {
-  extern __shared__ float4 smem4[];
-  float* sm = reinterpret_cast<float*>(smem4);
+__device__ inline void sweep_body(float* sm, const float* __restrict__ table, int n, int mp,
+                                  uint32_t* __restrict__ spins, float* __restrict__ log_psi,
+                                  int32_t* __restrict__ accepts, int64_t ns, int nsteps, uint64_t seed, uint64_t step0,
+                                  float reweight, const int32_t* __restrict__ nbr, int z, int hop, int64_t table_nf,
+                                  int cta, int nctas) {
   constexpr int kWarps = NT / 32;
   uint32_t* sp_all = reinterpret_cast<uint32_t*>(sm + (SMEM ? table_nf : 0));
   RbmTable T;
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(NT, 1)
   const int nw = words_for(n);
 
   for (int64_t slot = warp;; slot += kWarps) {
-    const int64_t c = slot * gridDim.x + blockIdx.x;
+    const int64_t c = slot * nctas + cta;
     if (c >= ns) break;
     if (lane < nw) sp[lane] = spins[c * nw + lane];
     __syncwarp();
@@ -311,16 +311,25 @@ __global__ void __launch_bounds__(NT, 1)
   }
 }
 
+template <int JT, bool SMEM, int NT, int PROP>
+__global__ void __launch_bounds__(NT, 1)
+    sweep_kernel(const float* __restrict__ table, int n, int mp, uint32_t* __restrict__ spins,
+                 float* __restrict__ log_psi, int32_t* __restrict__ accepts, int64_t ns, int nsteps, uint64_t seed,
+                 uint64_t step0, float reweight, const int32_t* __restrict__ nbr, int z, int hop,
+                 int64_t table_nf) {
+  extern __shared__ float4 smem4[];
+  sweep_body<JT, SMEM, NT, PROP>(reinterpret_cast<float*>(smem4), table, n, mp, spins, log_psi, accepts, ns, nsteps,
+                                 seed, step0, reweight, nbr, z, hop, table_nf, blockIdx.x, gridDim.x);
+}
+
 // ---------------------------------------------------------------------------------------
 // Local energies: one warp per sample, connected configurations generated in-kernel.
 __device__ inline int bit_of(const uint32_t* sp, int k) { return (int)((sp[k >> 5] >> (k & 31)) & 1u); }
 
 template <int JT, bool SMEM, int NT>
-__global__ void __launch_bounds__(NT, 1)
-    eloc_kernel(const float* __restrict__ table, int n, int mp, qgx_operator_t op, const uint32_t* __restrict__ spins,
-                int64_t ns, double* __restrict__ eloc, int64_t table_nf) {
-  extern __shared__ float4 smem4[];
-  float* sm = reinterpret_cast<float*>(smem4);
+__device__ inline void eloc_body(float* sm, const float* __restrict__ table, int n, int mp, const qgx_operator_t& op,
+                                 const uint32_t* __restrict__ spins, int64_t ns, double* __restrict__ eloc,
+                                 int64_t table_nf, int cta, int nctas) {
   constexpr int kWarps = NT / 32;
   uint32_t* sp_all = reinterpret_cast<uint32_t*>(sm + (SMEM ? table_nf : 0));
   RbmTable T;
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(NT, 1)
   uint32_t* sp = sp_all + 32 * warp;
   const int nw = words_for(n);
   for (int64_t slot = warp;; slot += kWarps) {
-    const int64_t c = slot * gridDim.x + blockIdx.x;
+    const int64_t c = slot * nctas + cta;
     if (c >= ns) break;
     if (lane < nw) sp[lane] = spins[c * nw + lane];
     __syncwarp();
@@ -376,6 +385,81 @@ __global__ void __launch_bounds__(NT, 1)
     if (lane == 0) eloc[c] = op.c0 + ed + eo;
     __syncwarp();
   }
+}
+
+template <int JT, bool SMEM, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    eloc_kernel(const float* __restrict__ table, int n, int mp, qgx_operator_t op, const uint32_t* __restrict__ spins,
+                int64_t ns, double* __restrict__ eloc, int64_t table_nf) {
+  extern __shared__ float4 smem4[];
+  eloc_body<JT, SMEM, NT>(reinterpret_cast<float*>(smem4), table, n, mp, op, spins, ns, eloc, table_nf, blockIdx.x,
+                          gridDim.x);
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched sweeps and local energies: one launch serves the jobs of several independent states
+// (a serving loop's RBM jobs of one hidden-unit width class). The job table travels as a kernel
+// parameter; CTAs [cta0[j], cta0[j + 1]) run job j exactly as its own launch would (same
+// device function, its own chains, Philox streams and table), so every job's results are
+// bit-identical to a separate call.
+constexpr int kBatchJobs = QGX_RBM_BATCH_MAX_JOBS;
+
+struct SweepJob {
+  const float* table;
+  uint32_t* spins;
+  float* log_psi;
+  int32_t* accepts;
+  const int32_t* nbr;
+  int64_t ns, table_nf;
+  uint64_t seed, step0;
+  float reweight;
+  int n, mp, nsteps, z, hop;
+};
+
+struct SweepBatch {
+  int njobs;
+  int cta0[kBatchJobs + 1];
+  SweepJob job[kBatchJobs];
+};
+
+struct ElocJob {
+  qgx_operator_t op;
+  const float* table;
+  const uint32_t* spins;
+  double* eloc;
+  int64_t ns, table_nf;
+  int n, mp;
+};
+
+struct ElocBatch {
+  int njobs;
+  int cta0[kBatchJobs + 1];
+  ElocJob job[kBatchJobs];
+};
+
+__device__ inline int batch_job_of(const int* cta0, int njobs) {
+  int j = 0;
+  while (j + 1 < njobs && cta0[j + 1] <= (int)blockIdx.x) ++j;
+  return j;
+}
+
+template <int JT, bool SMEM, int NT, int PROP>
+__global__ void __launch_bounds__(NT, 1) sweep_batch_kernel(const __grid_constant__ SweepBatch b) {
+  extern __shared__ float4 smem4[];
+  const int j = batch_job_of(b.cta0, b.njobs);
+  const SweepJob& J = b.job[j];
+  sweep_body<JT, SMEM, NT, PROP>(reinterpret_cast<float*>(smem4), J.table, J.n, J.mp, J.spins, J.log_psi, J.accepts,
+                                 J.ns, J.nsteps, J.seed, J.step0, J.reweight, J.nbr, J.z, J.hop, J.table_nf,
+                                 (int)blockIdx.x - b.cta0[j], b.cta0[j + 1] - b.cta0[j]);
+}
+
+template <int JT, bool SMEM, int NT>
+__global__ void __launch_bounds__(NT, 1) eloc_batch_kernel(const __grid_constant__ ElocBatch b) {
+  extern __shared__ float4 smem4[];
+  const int j = batch_job_of(b.cta0, b.njobs);
+  const ElocJob& J = b.job[j];
+  eloc_body<JT, SMEM, NT>(reinterpret_cast<float*>(smem4), J.table, J.n, J.mp, J.op, J.spins, J.ns, J.eloc, J.table_nf,
+                          (int)blockIdx.x - b.cta0[j], b.cta0[j + 1] - b.cta0[j]);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -796,6 +880,104 @@ inline bool mp_supported(int mp) {
   return jt == 1 || jt == 2 || jt == 3 || jt == 4 || jt == 8 || jt == 16;
 }
 
+// CTA ranges of a batch: job j gets min(resident capacity, ceil(ns_j / warps per CTA)) CTAs
+// (one chain per warp where the GPU holds them all); false when the grid would overflow int
+template <typename K>
+int batch_grid(K kernel, int nthreads, size_t smem, const int64_t* ns, int njobs, int* cta0) {
+  if (smem > 48 * 1024)
+    QGX_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  QGX_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nthreads, smem));
+  if (per_sm < 1) return QGX_ERR_UNSUPPORTED;
+  const int64_t cap = (int64_t)device_sm_count() * per_sm, warps = nthreads / 32;
+  int64_t acc = 0;
+  for (int j = 0; j < njobs; ++j) {
+    cta0[j] = (int)acc;
+    acc += std::max<int64_t>(1, std::min<int64_t>(cap, (ns[j] + warps - 1) / warps));
+    if (acc > 0x7fffffffLL) return QGX_ERR_UNSUPPORTED;
+  }
+  cta0[njobs] = (int)acc;
+  return QGX_OK;
+}
+
+// one launch for the jobs idx[0..cnt) (all of width class JT, shared-memory staging SMEM and
+// proposal PROP)
+template <int JT, bool SMEM, int PROP>
+int launch_sweep_batch(const qgx_rbm_sweep_job_t* jobs, const int* idx, int cnt, cudaStream_t st) {
+  constexpr int NT = threads_for<JT>();
+  auto k = sweep_batch_kernel<JT, SMEM, NT, PROP>;
+  SweepBatch b;
+  std::memset(&b, 0, sizeof(b));
+  b.njobs = cnt;
+  size_t smem = 0;
+  int64_t ns[kBatchJobs];
+  for (int q = 0; q < cnt; ++q) {
+    const qgx_rbm_sweep_job_t& J = jobs[idx[q]];
+    const int mp = padded_m(J.m);
+    size_t bytes;
+    fits_smem(NT, table_floats(J.n, mp), 32, &bytes);
+    smem = std::max(smem, bytes);
+    b.job[q] = SweepJob{J.table, J.spins, J.log_psi, J.accepts, J.nbr, J.ns, table_floats(J.n, mp), J.seed, J.step0,
+                        J.reweight, J.n, mp, J.nsteps, J.z, J.hop};
+    ns[q] = J.ns;
+  }
+  int rc = batch_grid(k, NT, smem, ns, cnt, b.cta0);
+  if (rc != QGX_OK) return rc;
+  k<<<b.cta0[cnt], NT, smem, st>>>(b);
+  return launch_status();
+}
+
+template <int JT, bool SMEM>
+int launch_eloc_batch(const qgx_rbm_eloc_job_t* jobs, const int* idx, int cnt, cudaStream_t st) {
+  constexpr int NT = threads_for<JT>();
+  auto k = eloc_batch_kernel<JT, SMEM, NT>;
+  ElocBatch b;
+  std::memset(&b, 0, sizeof(b));
+  b.njobs = cnt;
+  size_t smem = 0;
+  int64_t ns[kBatchJobs];
+  for (int q = 0; q < cnt; ++q) {
+    const qgx_rbm_eloc_job_t& J = jobs[idx[q]];
+    const int mp = padded_m(J.m);
+    size_t bytes;
+    fits_smem(NT, table_floats(J.n, mp), 32, &bytes);
+    smem = std::max(smem, bytes);
+    b.job[q] = ElocJob{*J.op, J.table, J.spins, J.eloc, J.ns, table_floats(J.n, mp), J.n, mp};
+    ns[q] = J.ns;
+  }
+  int rc = batch_grid(k, NT, smem, ns, cnt, b.cta0);
+  if (rc != QGX_OK) return rc;
+  k<<<b.cta0[cnt], NT, smem, st>>>(b);
+  return launch_status();
+}
+
+// the class of a job: width JT, shared-memory staging of its table, proposal
+struct BatchClass {
+  int jt, smem, prop;
+  bool operator==(const BatchClass& o) const { return jt == o.jt && smem == o.smem && prop == o.prop; }
+};
+
+template <int JT>
+int sweep_batch_jt(const qgx_rbm_sweep_job_t* jobs, const int* idx, int cnt, bool sm, int prop, cudaStream_t st) {
+  if (prop == QGX_PROPOSAL_LOCAL_FLIP)
+    return sm ? launch_sweep_batch<JT, true, QGX_PROPOSAL_LOCAL_FLIP>(jobs, idx, cnt, st)
+              : launch_sweep_batch<JT, false, QGX_PROPOSAL_LOCAL_FLIP>(jobs, idx, cnt, st);
+  return sm ? launch_sweep_batch<JT, true, QGX_PROPOSAL_SPIN_EXCHANGE>(jobs, idx, cnt, st)
+            : launch_sweep_batch<JT, false, QGX_PROPOSAL_SPIN_EXCHANGE>(jobs, idx, cnt, st);
+}
+
+template <int JT>
+int eloc_batch_jt(const qgx_rbm_eloc_job_t* jobs, const int* idx, int cnt, bool sm, cudaStream_t st) {
+  return sm ? launch_eloc_batch<JT, true>(jobs, idx, cnt, st) : launch_eloc_batch<JT, false>(jobs, idx, cnt, st);
+}
+
+// whether job (n, mp)'s table is staged in shared memory by the kernels of width JT
+inline bool stages_in_smem(int jt, int n, int mp) {
+  size_t bytes;
+  const int nt = jt <= 2 ? 1024 : (jt == 4 ? 512 : 256);  // threads_for<JT>()
+  return fits_smem(nt, table_floats(n, mp), 32, &bytes);
+}
+
 }  // namespace
 }  // namespace qgx
 
@@ -885,6 +1067,92 @@ int qgx_rbm_sweep(const float* table, int32_t n, int32_t m, uint32_t* spins, flo
   launch_sweep<JT>(table, n, mp, spins, log_psi, accepts, ns, nsteps, seed, step0, reweight, proposal, nbr, z, hop, as_cuda(stream))
   QGX_DISPATCH_JT(mp, CALL)
 #undef CALL
+}
+
+int qgx_rbm_sweep_batched(const qgx_rbm_sweep_job_t* jobs, int32_t njobs, int32_t* launches,
+                         qgx_stream_t stream) {
+  QGX_CHECK_ARG(njobs >= 0 && njobs <= QGX_RBM_BATCH_MAX_JOBS && (njobs == 0 || jobs));
+  if (launches) *launches = 0;
+  BatchClass cls[kBatchJobs];
+  bool live[kBatchJobs] = {};
+  for (int j = 0; j < njobs; ++j) {
+    const qgx_rbm_sweep_job_t& J = jobs[j];
+    QGX_CHECK_ARG(J.n > 0 && J.m > 0 && J.n <= kMaxSites && J.ns >= 0 && J.nsteps >= 0);
+    QGX_CHECK_ARG(J.proposal == QGX_PROPOSAL_LOCAL_FLIP || J.proposal == QGX_PROPOSAL_SPIN_EXCHANGE);
+    if (J.proposal == QGX_PROPOSAL_SPIN_EXCHANGE) QGX_CHECK_ARG(J.nbr && J.z > 0 && (J.hop == 1 || J.hop == -1));
+    if (J.ns == 0) continue;
+    QGX_CHECK_ARG(J.table && J.spins && J.log_psi);
+    const int mp = padded_m(J.m);
+    if (!mp_supported(mp)) return QGX_ERR_UNSUPPORTED;
+    cls[j] = BatchClass{mp / 128, stages_in_smem(mp / 128, J.n, mp) ? 1 : 0, J.proposal};
+    live[j] = true;
+  }
+  const cudaStream_t st = as_cuda(stream);
+  for (int j = 0; j < njobs; ++j) {
+    if (!live[j]) continue;
+    int idx[kBatchJobs], cnt = 0;
+    for (int q = j; q < njobs; ++q)
+      if (live[q] && cls[q] == cls[j]) {
+        idx[cnt++] = q;
+        live[q] = false;
+      }
+    const bool sm = cls[j].smem != 0;
+    int rc = QGX_ERR_UNSUPPORTED;
+    switch (cls[j].jt) {
+      case 1: rc = sweep_batch_jt<1>(jobs, idx, cnt, sm, cls[j].prop, st); break;
+      case 2: rc = sweep_batch_jt<2>(jobs, idx, cnt, sm, cls[j].prop, st); break;
+      case 3: rc = sweep_batch_jt<3>(jobs, idx, cnt, sm, cls[j].prop, st); break;
+      case 4: rc = sweep_batch_jt<4>(jobs, idx, cnt, sm, cls[j].prop, st); break;
+      case 8: rc = sweep_batch_jt<8>(jobs, idx, cnt, sm, cls[j].prop, st); break;
+      case 16: rc = sweep_batch_jt<16>(jobs, idx, cnt, sm, cls[j].prop, st); break;
+      default: break;
+    }
+    if (rc != QGX_OK) return rc;
+    if (launches) ++*launches;
+  }
+  return QGX_OK;
+}
+
+int qgx_rbm_eloc_batched(const qgx_rbm_eloc_job_t* jobs, int32_t njobs, int32_t* launches,
+                         qgx_stream_t stream) {
+  QGX_CHECK_ARG(njobs >= 0 && njobs <= QGX_RBM_BATCH_MAX_JOBS && (njobs == 0 || jobs));
+  if (launches) *launches = 0;
+  BatchClass cls[kBatchJobs];
+  bool live[kBatchJobs] = {};
+  for (int j = 0; j < njobs; ++j) {
+    const qgx_rbm_eloc_job_t& J = jobs[j];
+    QGX_CHECK_ARG(J.op && J.n > 0 && J.m > 0 && J.n <= kMaxSites && J.ns >= 0);
+    if (J.ns == 0) continue;
+    QGX_CHECK_ARG(J.table && J.spins && J.eloc);
+    const int mp = padded_m(J.m);
+    if (!mp_supported(mp)) return QGX_ERR_UNSUPPORTED;
+    cls[j] = BatchClass{mp / 128, stages_in_smem(mp / 128, J.n, mp) ? 1 : 0, 0};
+    live[j] = true;
+  }
+  const cudaStream_t st = as_cuda(stream);
+  for (int j = 0; j < njobs; ++j) {
+    if (!live[j]) continue;
+    int idx[kBatchJobs], cnt = 0;
+    for (int q = j; q < njobs; ++q)
+      if (live[q] && cls[q] == cls[j]) {
+        idx[cnt++] = q;
+        live[q] = false;
+      }
+    const bool sm = cls[j].smem != 0;
+    int rc = QGX_ERR_UNSUPPORTED;
+    switch (cls[j].jt) {
+      case 1: rc = eloc_batch_jt<1>(jobs, idx, cnt, sm, st); break;
+      case 2: rc = eloc_batch_jt<2>(jobs, idx, cnt, sm, st); break;
+      case 3: rc = eloc_batch_jt<3>(jobs, idx, cnt, sm, st); break;
+      case 4: rc = eloc_batch_jt<4>(jobs, idx, cnt, sm, st); break;
+      case 8: rc = eloc_batch_jt<8>(jobs, idx, cnt, sm, st); break;
+      case 16: rc = eloc_batch_jt<16>(jobs, idx, cnt, sm, st); break;
+      default: break;
+    }
+    if (rc != QGX_OK) return rc;
+    if (launches) ++*launches;
+  }
+  return QGX_OK;
 }
 
 int qgx_rbm_eloc(const float* table, int32_t n, int32_t m, const qgx_operator_t* op, const uint32_t* spins,

@@ -268,6 +268,36 @@ class Operator:
             samples = Samples.from_spins(samples)
         return state.local_energy(self, samples)
 
+    @staticmethod
+    def Oloc_batched(terms) -> list:
+        """Oloc of several (operator, state, samples) triples: the RBM states' local energies in
+        as few launches as their shapes allow (qgx_rbm_eloc_batched, one per hidden-unit width
+        class), each bit for bit its own Oloc; other states are evaluated one by one."""
+        from .sampler import Samples
+        out = [None] * len(terms)
+        jobs, keep = [], []
+        for k, (op, state, samples) in enumerate(terms):
+            if not isinstance(samples, Samples):
+                samples = Samples.from_spins(samples)
+            if state.model.kind != "rbm":
+                out[k] = state.local_energy(op, samples)
+                continue
+            comp = op.compiled()
+            if comp.max_site >= state.Nmodes:
+                raise ValueError("the operator acts on sites beyond the state's lattice")
+            e = torch.empty(samples.nsamples, dtype=torch.float64, device=state.params.device)
+            out[k] = e
+            keep.append(comp)
+            jobs.append(_lib.RbmElocJob(_lib.ptr(state.table), state.model.N, state.model.M,
+                                        C.pointer(comp.struct), _lib.ptr(samples.packed), samples.nsamples,
+                                        _lib.ptr(e)))
+        for i in range(0, len(jobs), _lib.RBM_BATCH_MAX_JOBS):
+            chunk = jobs[i:i + _lib.RBM_BATCH_MAX_JOBS]
+            arr = (_lib.RbmElocJob * len(chunk))(*chunk)
+            launches = C.c_int32(0)
+            _lib.call("qgx_rbm_eloc_batched", arr, len(chunk), C.byref(launches), _lib.stream_ptr())
+        return out
+
     def expectation(self, state, samples, return_var: bool = False):
         r = samples.reweight_factor
         E = self.Oloc(state, samples)

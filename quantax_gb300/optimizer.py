@@ -333,8 +333,9 @@ class QNGD:
             ev.record()
             self.marks.append((name, ev))
 
-    def get_step(self, samples) -> torch.Tensor:
-        Ebar = self.get_Ebar(samples)
+    def get_step(self, samples, local_energies: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """local_energies: the samples' E_loc when already computed (a batched evaluation)."""
+        Ebar = self.get_Ebar(samples) if local_energies is None else self.get_Ebar(samples, local_energies)
         Obar = self.get_Obar(samples)
         return self.solve(Obar, Ebar)
 
@@ -365,9 +366,10 @@ class SR(QNGD):
         """Device tensor [Re energy, Im energy, VarE] of the last step (no sync)."""
         return self._stats
 
-    def get_Ebar(self, samples) -> torch.Tensor:
-        """Ebar = (E - <E>) sqrt(r / Ns); energy and VarE kept on the device (sr.py:180-195)."""
-        E = self._hamiltonian.Oloc(self._state, samples)
+    def get_Ebar(self, samples, local_energies: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Ebar = (E - <E>) sqrt(r / Ns); energy and VarE kept on the device (sr.py:180-195).
+        local_energies: E_loc of the samples when already computed."""
+        E = self._hamiltonian.Oloc(self._state, samples) if local_energies is None else local_energies
         ns = samples.nsamples
         stats = self._buffer("stats", (3,), torch.float64)
         cplx = E.is_complex()

@@ -8,9 +8,10 @@ run is reproducible from the global seed and independent of launch geometry.
 """
 from __future__ import annotations
 
+import ctypes as C
 import warnings
 from dataclasses import dataclass
-from typing import Optional, Sequence, Union
+from typing import List, Optional, Sequence, Union
 
 import numpy as np
 import torch
@@ -275,8 +276,47 @@ class Metropolis(Sampler):
     def sweep(self, nsweeps: Optional[int] = None) -> Samples:
         """nsweeps proposals per chain (metropolis.py:171-215); default sweep_steps."""
         n = self._sweep_steps if nsweeps is None else int(nsweeps)
-        st = self._state
         self._run_proposals(n)
+        return self._finish_sweep(n)
+
+    def _batch_job(self, n: int):
+        """The qgx_rbm_sweep_job_t of this sampler's next n proposals, or None when the sweep
+        cannot join a batched launch (ResConv states, mixtures of proposal kinds)."""
+        if self._resconv or type(self)._run_proposals is not Metropolis._run_proposals or self.proposal is None:
+            return None
+        st = self._state
+        m = st.model
+        return _lib.RbmSweepJob(_lib.ptr(st.table), m.N, m.M, _lib.ptr(self._packed), _lib.ptr(self._log_psi),
+                                _lib.ptr(self._accepts), self._nsamples, int(n), int(self.proposal), int(self._seed),
+                                int(self._step), float(self._reweight), _lib.ptr(self._nbr), int(self._z),
+                                int(self._hop))
+
+    @staticmethod
+    def sweep_batched(samplers: Sequence["Metropolis"], nsweeps: Optional[int] = None) -> List[Samples]:
+        """sweep() of several independent RBM samplers with their Metropolis steps in as few
+        kernel launches as their shapes allow (qgx_rbm_sweep_batched: one per hidden-unit width
+        class); each sampler's chains, log psi and accept counts are bit for bit those of its own
+        sweep(). Samplers that cannot join a batch (ResConv, MixSampler) sweep on their own."""
+        ns = [smp._sweep_steps if nsweeps is None else int(nsweeps) for smp in samplers]
+        jobs, members = [], []
+        for smp, n in zip(samplers, ns):
+            job = smp._batch_job(n)
+            if job is None:
+                smp._run_proposals(n)
+            else:
+                jobs.append(job)
+                members.append(smp)
+        for i in range(0, len(jobs), _lib.RBM_BATCH_MAX_JOBS):
+            chunk = jobs[i:i + _lib.RBM_BATCH_MAX_JOBS]
+            arr = (_lib.RbmSweepJob * len(chunk))(*chunk)
+            launches = C.c_int32(0)
+            _lib.call("qgx_rbm_sweep_batched", arr, len(chunk), C.byref(launches), _lib.stream_ptr())
+        return [smp._finish_sweep(n) for smp, n in zip(samplers, ns)]
+
+    def _finish_sweep(self, n: int) -> Samples:
+        """The bookkeeping after n proposals: the psi check of local updates, the step counter,
+        the reweighting factors and the Samples."""
+        st = self._state
         if self._resconv:
             lp_real = self._log_psi[:, 0].contiguous()
             # complex output, or a real state that can be negative (symmetry projection,

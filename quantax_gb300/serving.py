@@ -141,19 +141,40 @@ class Job:
         self.status = "ok"
         self._checked = 0  # steps whose energy has been checked for finiteness
         self._host_energy: List[torch.Tensor] = []
+        self._e0 = None    # the running step's start event
+        self._pre = None   # (samples, local energies) of the running step from a batched launch
+
+    @property
+    def batchable(self) -> bool:
+        """Whether the job's sweeps and local energies can share launches with other jobs'
+        (RBM states: qgx_rbm_sweep_batched / qgx_rbm_eloc_batched)."""
+        return self.spec.kind == "tfim"
+
+    def begin(self) -> None:
+        """Mark the start of the next SR step on the job's stream (step() does it when not done)."""
+        with torch.cuda.stream(self.stream):
+            self._e0 = torch.cuda.Event(enable_timing=True)
+            self._e0.record()
 
     @property
     def done(self) -> bool:
         return self.step_index >= self.spec.steps
 
     def step(self) -> None:
-        """Enqueue one SR step on the job's stream (returns without waiting)."""
+        """Enqueue one SR step on the job's stream (returns without waiting). A step whose sweep
+        and local energies came from a batched launch (VMCServer._batched_front) starts from
+        them."""
+        if self._e0 is None:
+            self.begin()
         with torch.cuda.stream(self.stream):
-            e0 = torch.cuda.Event(enable_timing=True)
+            e0, self._e0 = self._e0, None
             e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            samples = self.sampler.sweep()
-            step = self.opt.get_step(samples)
+            if self._pre is not None:
+                (samples, E), self._pre = self._pre, None
+                step = self.opt.get_step(samples, E)
+            else:
+                samples = self.sampler.sweep()
+                step = self.opt.get_step(samples)
             self.state.update(step * self.spec.lr)
             self.stats.append(self.opt.stats.clone())
             host = torch.empty(1, dtype=torch.float64).pin_memory()
@@ -194,7 +215,7 @@ class _Pending:
 class VMCServer:
     """Admits jobs by HBM budget, runs their SR steps interleaved on per-job streams."""
 
-    def __init__(self, hbm_budget_bytes: Optional[int] = None, max_active: int = 16):
+    def __init__(self, hbm_budget_bytes: Optional[int] = None, max_active: int = 16, batch: bool = True):
         if hbm_budget_bytes is None:
             free, _ = torch.cuda.mem_get_info()
             hbm_budget_bytes = int(free * 0.8)
@@ -204,6 +225,9 @@ class VMCServer:
         self._order = 0
         self._rejected: List[dict] = []
         self._cancel = set()
+        self.batch = batch  # batched sweeps and local energies of the RBM jobs of a round
+        self._batch_stream = None
+        self.batched_rounds = 0
 
     def submit(self, spec: JobSpec) -> str:
         """Queue a job; returns "queued", or "rejected: <reason>" for a spec that cannot run
@@ -221,6 +245,35 @@ class VMCServer:
         heapq.heappush(self._pending, _Pending(spec.arrival, self._order, spec))
         self._order += 1
         return "queued"
+
+    def _batched_front(self, jobs: List[Job]) -> None:
+        """The sweeps and local energies of this round's RBM jobs in shared launches, on a
+        stream that waits for each job's previous step; each job's stream then waits for them,
+        and the job's own step goes on from its samples and local energies."""
+        from .operator import Operator
+        from .sampler import Metropolis
+        if self._batch_stream is None:
+            self._batch_stream = torch.cuda.Stream()
+        bs = self._batch_stream
+        for job in jobs:
+            job.begin()
+            ready = torch.cuda.Event()
+            ready.record(job.stream)
+            bs.wait_event(ready)
+        with torch.cuda.stream(bs):
+            samples = Metropolis.sweep_batched([job.sampler for job in jobs])
+            energies = Operator.Oloc_batched([(job.opt.hamiltonian, job.state, smp)
+                                              for job, smp in zip(jobs, samples)])
+            done = torch.cuda.Event()
+            done.record()
+        for job, smp, E in zip(jobs, samples, energies):
+            job.stream.wait_event(done)
+            # made on the batch stream, used on the job's: not reused before the job is done
+            for t in (smp.packed, smp.log_psi, smp.reweight_factor, E):
+                if isinstance(t, torch.Tensor):
+                    t.record_stream(job.stream)
+            job._pre = (smp, E)
+        self.batched_rounds += 1
 
     def cancel(self, name: str) -> None:
         """Retire the job at its next step boundary (or drop it if it has not started)."""
@@ -256,6 +309,9 @@ class VMCServer:
             if not active:
                 time.sleep(min(0.01, max(0.0, self._pending[0].arrival - now)))
                 continue
+            batch = [job for job in active if job.batchable] if self.batch else []
+            if len(batch) >= 2:
+                self._batched_front(batch)
             for job in active:
                 job.step()
             if on_round is not None:

@@ -566,9 +566,11 @@ int64_t chol_f64_workspace_bytes(int64_t n) { return n > 0 ? chol_layout(n, null
 // and the rest. The panel chain (FP64 diagonal blocks, triangular solves, the in-panel updates),
 // the panel's slicing and the strip run on a high-priority internal stream; the rest runs on the
 // caller's stream, so the next panel's FP64 chain overlaps the large tensor-core update. Panel
-// k's chain waits for the rest update of panel k - 2 (the last one touching its columns); two
-// slice buffers alternate between panels. The caller's stream waits for the internal one at
-// the end, so the factor is complete in stream order.
+// k's chain waits for the rest update of panel k - 2, and panel k's strip for the rest update of
+// panel k - 1: every update of a column block is ordered after the previous one (the strip and
+// the previous panel's rest both update the next panel's columns below its diagonal). Two slice
+// buffers alternate between panels. The caller's stream waits for the internal one at the end,
+// so the factor is complete in stream order.
 int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void* work, cudaStream_t st,
              int64_t* kernels) {
   if ((reinterpret_cast<uintptr_t>(work) & 255) != 0) return QGX_ERR_ARG;
@@ -609,8 +611,12 @@ int chol_f64(double* A, int64_t n, int64_t lda, int* info, int32_t* status, void
     // the panel's trailing update (K = 256): the strip on the internal stream, the rest on st
     const int b = (int)(k & 1);
     const int64_t ms = n - pe, pe2 = std::min<int64_t>(pe + kPanel, n);
-    if ((rc = slice_panel(A, lda, pe, c0, ms, kPanel, ws.s_panel[b], ws.e_panel[b], aux, kernels)) != QGX_OK ||
-        (rc = ozaki_region(A, lda, ws.s_panel[b], ws.e_panel[b], ms, pe, kPanel, pe, ms, pe, pe2 - pe, status, aux,
+    if ((rc = slice_panel(A, lda, pe, c0, ms, kPanel, ws.s_panel[b], ws.e_panel[b], aux, kernels)) != QGX_OK)
+      return rc;
+    // the strip updates the next panel's columns, which the previous panel's rest update (on st)
+    // also updates: both read-modify-write the same entries, so the strip waits for it
+    if (k >= 1) QGX_CHECK_CUDA(cudaStreamWaitEvent(aux, la->rest_done[(k - 1) & 1], 0));
+    if ((rc = ozaki_region(A, lda, ws.s_panel[b], ws.e_panel[b], ms, pe, kPanel, pe, ms, pe, pe2 - pe, status, aux,
                            kernels)) != QGX_OK)
       return rc;
     if (pe2 < n) {

@@ -79,6 +79,20 @@ __device__ inline void stage_floats(float* dst, const float* src, int64_t n) {
   for (int64_t e = threadIdx.x; e < n; e += blockDim.x) dst[e] = __ldg(src + e);
 }
 
+// Floats between consecutive samples' activations in the forward's shared memory: C N padded to
+// G = ceil(N / kFwdSPT) modulo 32, so that work item a G + g (sample a, site group g) falls in
+// bank (a G + g) mod 32 and a warp whose 32 consecutive items span two samples touches 32
+// different banks (with a stride of C N, a multiple of 32 at L = 10, the two samples' items
+// collide on up to 16 banks).
+__host__ __device__ inline int rc_sample_stride(int C, int N) {
+  const int G = (N + kFwdSPT - 1) / kFwdSPT;
+  return C * N + (((G - C * N) % 32) + 32) % 32;
+}
+
+// floats before the layer weights in the forward's shared memory: the three activation buffers,
+// rounded up to a multiple of 4 (the sample stride need not be one)
+__host__ __device__ inline int64_t rc_weights_offset(int S, int SS) { return (3LL * S * SS + 3) / 4 * 4; }
+
 // c += a * b on a pair of floats with one packed FP32 instruction (each lane is an IEEE fma,
 // the same result as two fmaf calls, in half the issue slots)
 __device__ inline void fma_pair(float2& c, float2 a, float2 b) {
@@ -98,7 +112,7 @@ __device__ inline void fma_pair(float2& c, float2 a, float2 b) {
 template <int C, int SPT>
 __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* __restrict__ out,
                                   const float* __restrict__ w, const int16_t* __restrict__ nbr, int N, int S,
-                                  int mode) {
+                                  int mode, int ss) {  // ss: floats between samples' activations
   const float* bias = w + cin * 9 * C;
   const int G = (N + SPT - 1) / SPT;
   for (int it = threadIdx.x; it < S * G; it += blockDim.x) {
@@ -117,7 +131,7 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
     for (int k = 0; k < SPT; ++k)
 #pragma unroll
       for (int h = 0; h < C / 2; ++h) acc[k][h] = make_float2(bias[2 * h], bias[2 * h + 1]);
-    const float* ina = in + (int64_t)a * C * N;
+    const float* ina = in + (int64_t)a * ss;
     for (int i = 0; i < cin; ++i) {
       const float* ini = ina + i * N;
 #pragma unroll
@@ -143,7 +157,7 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
       if (r[k] >= N) continue;
-      float* oa = out + (int64_t)a * C * N + r[k];
+      float* oa = out + (int64_t)a * ss + r[k];
       if (mode == 0) {
 #pragma unroll
         for (int h = 0; h < C / 2; ++h) {
@@ -180,10 +194,11 @@ __global__ void __launch_bounds__(kFwdThreads)
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int N = net.N, nw = words_for(N);
+  const int SS = rc_sample_stride(C, N);
   float* X = sm;
-  float* P = X + (int64_t)S * C * N;
-  float* Q = P + (int64_t)S * C * N;
-  float* Wl = Q + (int64_t)S * C * N;
+  float* P = X + (int64_t)S * SS;
+  float* Q = P + (int64_t)S * SS;
+  float* Wl = sm + rc_weights_offset(S, SS);  // 16-byte aligned: the weights are read as float4
   int16_t* nbr = reinterpret_cast<int16_t*>(Wl + C * 9 * C + C);
   build_nbr(nbr, net.L);
   const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
@@ -195,7 +210,7 @@ __global__ void __launch_bounds__(kFwdThreads)
       const int a = e / N, r = e % N;
       float v = 0.0f;
       if (a < s_here) v = ((cfg[(base + a) * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
-      for (int c = 0; c < C; ++c) X[((int64_t)a * C + c) * N + r] = v;
+      for (int c = 0; c < C; ++c) X[(int64_t)a * SS + c * N + r] = v;
     }
     for (int b = 0; b < net.B; ++b) {
       const float scale = rsqrtf((float)(b + 1)) * (b == 0 ? 0.70710678118654752f : 1.0f);
@@ -203,23 +218,23 @@ __global__ void __launch_bounds__(kFwdThreads)
       __syncthreads();
       for (int e = threadIdx.x; e < S * cin * N; e += blockDim.x) {
         const int a = e / (cin * N), rem = e % (cin * N);
-        const float v = X[(int64_t)a * C * N + rem] * scale;
-        P[(int64_t)a * C * N + rem] = b == 0 ? v : gelu_tanh(v);
+        const float v = X[(int64_t)a * SS + rem] * scale;
+        P[(int64_t)a * SS + rem] = b == 0 ? v : gelu_tanh(v);
       }
       stage_floats(Wl, table + layer_offset(2 * b, C), layer_floats(2 * b, C));
       __syncthreads();
-      conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0);
+      conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0, SS);
       __syncthreads();
       stage_floats(Wl, table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
       __syncthreads();
-      conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1);
+      conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1, SS);
     }
     __syncthreads();
     // log of the mean final activation over (channel, site) per sample, one warp per sample
     const float fs = rsqrtf((float)(net.B + 1));
     const int cp = net.cplx ? C / 2 : C;
     for (int a = warp; a < s_here; a += kFwdThreads / 32) {
-      const float2 lp = rc_warp_log_psi(X + (int64_t)a * C * N, cp * N, fs, net.cplx, net.sinhp1, lane);
+      const float2 lp = rc_warp_log_psi(X + (int64_t)a * SS, cp * N, fs, net.cplx, net.sinhp1, lane);
       if (lane == 0) out[base + a] = lp;
     }
   }
@@ -636,7 +651,7 @@ __global__ void __launch_bounds__(kJacThreads)
       // A = conv1(P) + b1 (pre-activation kept: conv_layer mode 1 on a zeroed buffer)
       for (int e = threadIdx.x; e < CN; e += blockDim.x) Qa[e] = 0.0f;
       __syncthreads();
-      conv_layer<C, 1>(P, cin, Qa, W, nbr, N, 1, 1);
+      conv_layer<C, 1>(P, cin, Qa, W, nbr, N, 1, 1, C * N);
       __syncthreads();
       for (int e = threadIdx.x; e < CN; e += blockDim.x) {
         xs[CN + e] = Qa[e];
@@ -644,7 +659,7 @@ __global__ void __launch_bounds__(kJacThreads)
       }
       stage_layer<C>(table, 2 * b + 1, W, WT);
       __syncthreads();
-      conv_layer<C, 1>(Qa, C, X, W, nbr, N, 1, 1);
+      conv_layer<C, 1>(Qa, C, X, W, nbr, N, 1, 1, C * N);
     }
     __syncthreads();
     // ---- output cotangents: w_e = f'(z_e) / sum f, f = exp (exp_by_scale) or sinh + 1
@@ -774,7 +789,7 @@ int launch_jacobian_c(const float* table, const ConvNet& net, const uint32_t* sp
 }
 
 int rc_smem_bytes(const ConvNet& net, int S) {
-  const int64_t f = 3LL * S * net.C * net.N + (int64_t)net.C * 9 * net.C + net.C;
+  const int64_t f = rc_weights_offset(S, rc_sample_stride(net.C, net.N)) + (int64_t)net.C * 9 * net.C + net.C;
   return (int)(f * 4 + (int64_t)net.N * 9 * 2 + 16);
 }
 

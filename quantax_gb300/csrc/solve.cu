@@ -46,6 +46,25 @@ int solver_for_current_device(cusolverDnHandle_t* h, cusolverDnParams_t* p) {
   return QGX_OK;
 }
 
+// cuSOLVER's routines use scratch memory that belongs to the handle (its internal cuBLAS
+// workspace), and one handle serves every stream of the device: two solves on different streams
+// (the jobs of a serving loop) could run at once on the same scratch. So the device's cuSOLVER
+// calls are ordered on the GPU: each call's stream first waits for the event recorded after
+// the previous call (on whatever stream), then records it again. Callers hold g_solver_mutex.
+cudaEvent_t g_cus_done[kMaxDevices] = {};
+
+template <typename F>
+int cus_ordered(cudaStream_t st, F&& call) {
+  int dev = 0;
+  QGX_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return QGX_ERR_UNSUPPORTED;
+  if (!g_cus_done[dev]) QGX_CHECK_CUDA(cudaEventCreateWithFlags(&g_cus_done[dev], cudaEventDisableTiming));
+  QGX_CHECK_CUDA(cudaStreamWaitEvent(st, g_cus_done[dev], 0));  // no-op before the first record
+  const cusolverStatus_t s = call();
+  QGX_CHECK_CUDA(cudaEventRecord(g_cus_done[dev], st));
+  return s == CUSOLVER_STATUS_SUCCESS ? QGX_OK : QGX_ERR_SOLVER;
+}
+
 constexpr int kProjRows = 256;  // rows per partial sum of the projection x = A^T y
 
 inline int64_t al256(int64_t b) { return (b + 255) / 256 * 256; }
@@ -603,16 +622,19 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
       // upper factor cuSOLVER's potrs takes
       if ((rc = chol_f64_graph(T, n, n, dinfo, nullptr, ws.chol, st, &g_kernels)) != QGX_OK) return rc;
       fill = CUBLAS_FILL_MODE_UPPER;
-    } else if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus, ws.cus_bytes,
-                                hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS) {
-      return QGX_ERR_SOLVER;
+    } else if ((rc = cus_ordered(st, [&] {
+                  return cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus,
+                                          ws.cus_bytes, hws, g_host_ws.size(), dinfo);
+                })) != QGX_OK) {
+      return rc;
     }
     QGX_CHECK_CUDA(cudaMemcpyAsync(ws.y, b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     // Xpotrs reports only argument errors; it writes its own word so that the factorisation's
     // info (> 0: leading minor not positive definite) reaches the caller
-    if (cusolverDnXpotrs(h, p, fill, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, ws.info + 1) !=
-        CUSOLVER_STATUS_SUCCESS)
-      return QGX_ERR_SOLVER;
+    if ((rc = cus_ordered(st, [&] {
+           return cusolverDnXpotrs(h, p, fill, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, ws.info + 1);
+         })) != QGX_OK)
+      return rc;
     ++g_kernels;
     nan_if_failed_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, st>>>(ws.y, n, dinfo);
     return launch_status();
@@ -634,9 +656,11 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
       if ((rc = launch_status()) != QGX_OK) return rc;
       {
         Fp32EmulationScope emu(h, true);
-        if (cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.cus, ws.cus_bytes,
-                             hws, g_host_ws.size(), ws.info) != CUSOLVER_STATUS_SUCCESS)
-          return QGX_ERR_SOLVER;
+        if ((rc = cus_ordered(st, [&] {
+               return cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.cus,
+                                       ws.cus_bytes, hws, g_host_ws.size(), ws.info);
+             })) != QGX_OK)
+          return rc;
       }
       QGX_CHECK_CUDA(cudaMemcpyAsync(&hinfo, ws.info, sizeof(int), cudaMemcpyDeviceToHost, st));
       QGX_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -713,9 +737,11 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     }
     return launch_status();
   }
-  if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.w,
-                       CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(), dinfo) != CUSOLVER_STATUS_SUCCESS)
-    return QGX_ERR_SOLVER;
+  if ((rc = cus_ordered(st, [&] {
+         return cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n,
+                                 CUDA_R_64F, ws.w, CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(), dinfo);
+       })) != QGX_OK)
+    return rc;
   ++g_kernels;
   eigs_inv_kernel<<<1, 1024, 0, st>>>(ws.w, n, rtol, atol, ws.inv);
   ++g_kernels;
@@ -783,10 +809,12 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
     if ((rc = solver_for_current_device(&h, &p)) != QGX_OK) return rc;
     if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
     void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
-    if (cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, np, CUDA_R_64F, S, np, CUDA_R_64F,
-                         ws.w, CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(),
-                         info ? info : ws.info) != CUSOLVER_STATUS_SUCCESS)
-      return QGX_ERR_SOLVER;
+    if ((rc = cus_ordered(st, [&] {
+           return cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, np, CUDA_R_64F, S, np,
+                                   CUDA_R_64F, ws.w, CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(),
+                                   info ? info : ws.info);
+         })) != QGX_OK)
+      return rc;
     ++g_kernels;
     eigs_inv_kernel<<<1, 1024, 0, st>>>(ws.w, np, rtol, atol, ws.inv);
     const int64_t nchunk = (n + kSnrRows - 1) / kSnrRows;

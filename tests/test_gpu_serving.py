@@ -88,3 +88,23 @@ def test_failures_stay_with_their_job(cuda):
         j = res[spec.name]
         assert j["status"] == "ok"
         assert np.all(np.abs(np.array(j["energies"]) - np.array(alone[spec.name])) <= 1e-12 * np.abs(alone[spec.name]))
+
+
+def test_serving_repeats_exactly_across_runs(cuda):
+    """The same Poisson stream of jobs served three times in one process (the runs' timing
+    differs: the first can include kernel loading, graph captures and workspace allocation, so
+    the jobs' admission rounds and overlaps differ) gives every job the same energies bit for
+    bit, with and without the batched launches: no job's result depends on when the others run. The device's cuSOLVER calls are
+    ordered because the handle's scratch is shared by every stream (two jobs' triangular
+    solves at once gave timing-dependent energies)."""
+    from quantax_gb300.serving import VMCServer, poisson_jobs
+    runs = []
+    for batch in (True, True, False):
+        srv = VMCServer(max_active=6, batch=batch)
+        for sp in poisson_jobs(6, seed=77, rate_per_s=20.0, steps=6):
+            srv.submit(sp)
+        runs.append({j["name"]: np.array(j["energies"]) for j in srv.run()["jobs"]})
+    for other in runs[1:]:
+        assert set(other) == set(runs[0])
+        for name, e in runs[0].items():
+            assert np.array_equal(e, other[name]), name

@@ -94,9 +94,9 @@ def test_serving_repeats_exactly_across_runs(cuda):
     """The same Poisson stream of jobs served three times in one process (the runs' timing
     differs: the first can include kernel loading, graph captures and workspace allocation, so
     the jobs' admission rounds and overlaps differ) gives every job the same energies bit for
-    bit, with and without the batched launches: no job's result depends on when the others run. The device's cuSOLVER calls are
-    ordered because the handle's scratch is shared by every stream (two jobs' triangular
-    solves at once gave timing-dependent energies)."""
+    bit, with and without the batched launches: no job's result depends on when the others run.
+    Under this load the FP64 Cholesky once lost an update (its look-ahead strip and the previous
+    panel's trailing update were unordered), which only timing revealed."""
     from quantax_gb300.serving import VMCServer, poisson_jobs
     runs = []
     for batch in (True, True, False):

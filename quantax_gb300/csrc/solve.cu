@@ -46,23 +46,57 @@ int solver_for_current_device(cusolverDnHandle_t* h, cusolverDnParams_t* p) {
   return QGX_OK;
 }
 
-// cuSOLVER's routines use scratch memory that belongs to the handle (its internal cuBLAS
-// workspace), and one handle serves every stream of the device: two solves on different streams
-// (the jobs of a serving loop) could run at once on the same scratch. So the device's cuSOLVER
-// calls are ordered on the GPU: each call's stream first waits for the event recorded after
-// the previous call (on whatever stream), then records it again. Callers hold g_solver_mutex.
-cudaEvent_t g_cus_done[kMaxDevices] = {};
+// One cuSOLVER handle per stream for the solves themselves: a handle's routines keep scratch
+// memory that belongs to the handle (its internal cuBLAS workspace), so callers on different
+// streams (the jobs of a serving loop) each get their own handle and never share it, with no
+// ordering between their streams. At most kMaxStreamSolvers handles are kept (least recently
+// used destroyed first); the handle's stream is set on every use, since a stream's address can
+// be reused by a later stream. Callers hold g_solver_mutex.
+struct StreamSolver {
+  int dev;
+  cudaStream_t st;
+  cusolverDnHandle_t h;
+  cusolverDnParams_t p;
+  uint64_t last_use;
+};
+constexpr size_t kMaxStreamSolvers = 32;
+std::vector<StreamSolver> g_stream_solvers;
+uint64_t g_solver_clock = 0;
 
-template <typename F>
-int cus_ordered(cudaStream_t st, F&& call) {
+int solver_for_stream(cudaStream_t st, cusolverDnHandle_t* h, cusolverDnParams_t* p) {
   int dev = 0;
   QGX_CHECK_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return QGX_ERR_UNSUPPORTED;
-  if (!g_cus_done[dev]) QGX_CHECK_CUDA(cudaEventCreateWithFlags(&g_cus_done[dev], cudaEventDisableTiming));
-  QGX_CHECK_CUDA(cudaStreamWaitEvent(st, g_cus_done[dev], 0));  // no-op before the first record
-  const cusolverStatus_t s = call();
-  QGX_CHECK_CUDA(cudaEventRecord(g_cus_done[dev], st));
-  return s == CUSOLVER_STATUS_SUCCESS ? QGX_OK : QGX_ERR_SOLVER;
+  StreamSolver* hit = nullptr;
+  for (auto& e : g_stream_solvers)
+    if (e.dev == dev && e.st == st) hit = &e;
+  if (!hit) {
+    if (g_stream_solvers.size() >= kMaxStreamSolvers) {
+      auto lru = std::min_element(g_stream_solvers.begin(), g_stream_solvers.end(),
+                                  [](const StreamSolver& a, const StreamSolver& b) { return a.last_use < b.last_use; });
+      cusolverDnDestroyParams(lru->p);
+      cusolverDnDestroy(lru->h);
+      g_stream_solvers.erase(lru);
+    }
+    StreamSolver e{dev, st, nullptr, nullptr, 0};
+    if (cusolverDnCreate(&e.h) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+    if (cusolverDnCreateParams(&e.p) != CUSOLVER_STATUS_SUCCESS) {
+      cusolverDnDestroy(e.h);
+      return QGX_ERR_SOLVER;
+    }
+    g_stream_solvers.push_back(e);
+    hit = &g_stream_solvers.back();
+  }
+  hit->last_use = ++g_solver_clock;
+  if (cusolverDnSetStream(hit->h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+  *h = hit->h;
+  *p = hit->p;
+  return QGX_OK;
+}
+
+// a cuSOLVER call's status as a qgx status
+template <typename F>
+int cus_status(F&& call) {
+  return call() == CUSOLVER_STATUS_SUCCESS ? QGX_OK : QGX_ERR_SOLVER;
 }
 
 constexpr int kProjRows = 256;  // rows per partial sum of the projection x = A^T y
@@ -607,9 +641,8 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
                double tol_snr, const SolveWs& ws, int32_t* info, cudaStream_t st) {
   cusolverDnHandle_t h;
   cusolverDnParams_t p;
-  int rc = solver_for_current_device(&h, &p);
+  int rc = solver_for_stream(st, &h, &p);
   if (rc != QGX_OK) return rc;
-  if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
   int* dinfo = info ? info : ws.info;
   void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
   if (method == QGX_SOLVE_SHIFT || method == QGX_SOLVE_SHIFT_LIB) {
@@ -622,7 +655,7 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
       // upper factor cuSOLVER's potrs takes
       if ((rc = chol_f64_graph(T, n, n, dinfo, nullptr, ws.chol, st, &g_kernels)) != QGX_OK) return rc;
       fill = CUBLAS_FILL_MODE_UPPER;
-    } else if ((rc = cus_ordered(st, [&] {
+    } else if ((rc = cus_status([&] {
                   return cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n, CUDA_R_64F, ws.cus,
                                           ws.cus_bytes, hws, g_host_ws.size(), dinfo);
                 })) != QGX_OK) {
@@ -631,7 +664,7 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     QGX_CHECK_CUDA(cudaMemcpyAsync(ws.y, b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     // Xpotrs reports only argument errors; it writes its own word so that the factorisation's
     // info (> 0: leading minor not positive definite) reaches the caller
-    if ((rc = cus_ordered(st, [&] {
+    if ((rc = cus_status([&] {
            return cusolverDnXpotrs(h, p, fill, n, 1, CUDA_R_64F, T, n, CUDA_R_64F, ws.y, n, ws.info + 1);
          })) != QGX_OK)
       return rc;
@@ -656,7 +689,7 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
       if ((rc = launch_status()) != QGX_OK) return rc;
       {
         Fp32EmulationScope emu(h, true);
-        if ((rc = cus_ordered(st, [&] {
+        if ((rc = cus_status([&] {
                return cusolverDnXpotrf(h, p, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_32F, ws.t32, n, CUDA_R_32F, ws.cus,
                                        ws.cus_bytes, hws, g_host_ws.size(), ws.info);
              })) != QGX_OK)
@@ -737,7 +770,7 @@ int solve_gram(double* T, int64_t n, const double* b, int method, double rshift,
     }
     return launch_status();
   }
-  if ((rc = cus_ordered(st, [&] {
+  if ((rc = cus_status([&] {
          return cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F, T, n,
                                  CUDA_R_64F, ws.w, CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(), dinfo);
        })) != QGX_OK)
@@ -806,10 +839,9 @@ int qgx_sr_solve(double* S, int64_t np, const float* A, int64_t n, int64_t lda, 
     // terms b[s] (A V)[s, k], x = V diag(l+) rho
     cusolverDnHandle_t h;
     cusolverDnParams_t p;
-    if ((rc = solver_for_current_device(&h, &p)) != QGX_OK) return rc;
-    if (cusolverDnSetStream(h, st) != CUSOLVER_STATUS_SUCCESS) return QGX_ERR_SOLVER;
+    if ((rc = solver_for_stream(st, &h, &p)) != QGX_OK) return rc;
     void* hws = g_host_ws.empty() ? nullptr : g_host_ws.data();
-    if ((rc = cus_ordered(st, [&] {
+    if ((rc = cus_status([&] {
            return cusolverDnXsyevd(h, p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, np, CUDA_R_64F, S, np,
                                    CUDA_R_64F, ws.w, CUDA_R_64F, ws.cus, ws.cus_bytes, hws, g_host_ws.size(),
                                    info ? info : ws.info);

@@ -104,27 +104,32 @@ __device__ inline void sinhp1_shifted(float a, float b, float m, bool cplx, floa
   *gi = sh * sn;
 }
 
-// log psi = log mean_e f(z_e) of one configuration, one warp: z_e = scale * za[e] for
-// e < cpN (real parts), imaginary parts at za[cpN + e] when cplx. exp_by_scale
+// log psi = log mean_e f(z_e) of one configuration, one warp: z_e = scale * za[at(e)] for
+// e < cpN (real parts), imaginary parts at za[cpN + at(e)] when cplx; at maps an element of the
+// site order to its place in storage (the identity, or a permutation within each channel plane).
+// The terms are summed in the order of e whatever the storage. exp_by_scale
 // (nn/activation.py:26-32) shifts by max Re z, sinhp1_by_scale by max |Re z|. (re, im) of log psi.
-__device__ inline float2 rc_warp_log_psi(const float* za, int cpN, float scale, bool cplx, bool sinhp1, int lane) {
+template <class At>
+__device__ inline float2 rc_warp_log_psi_at(const float* za, int cpN, float scale, bool cplx, bool sinhp1, int lane,
+                                            At at) {
   float m = -INFINITY;
   for (int e = lane; e < cpN; e += 32) {
-    const float a = za[e] * scale;
+    const float a = za[at(e)] * scale;
     m = fmaxf(m, sinhp1 ? fabsf(a) : a);
   }
   m = warp_max(m);
   float sr = 0.0f, si = 0.0f;
   for (int e = lane; e < cpN; e += 32) {
+    const int k = at(e);
     if (sinhp1) {
       float fr, fi, gr, gi;
-      sinhp1_shifted(za[e] * scale, cplx ? za[cpN + e] * scale : 0.0f, m, cplx, &fr, &fi, &gr, &gi);
+      sinhp1_shifted(za[k] * scale, cplx ? za[cpN + k] * scale : 0.0f, m, cplx, &fr, &fi, &gr, &gi);
       sr += fr;
       si += fi;
     } else {
-      const float ex = expf(za[e] * scale - m);
+      const float ex = expf(za[k] * scale - m);
       float sn = 0.0f, cs = 1.0f;
-      if (cplx) sincosf(za[cpN + e] * scale, &sn, &cs);
+      if (cplx) sincosf(za[cpN + k] * scale, &sn, &cs);
       sr = fmaf(ex, cs, sr);
       si = fmaf(ex, sn, si);
     }
@@ -132,6 +137,14 @@ __device__ inline float2 rc_warp_log_psi(const float* za, int cpN, float scale, 
   sr = warp_sum(sr);
   si = warp_sum(si);
   return make_float2(m + 0.5f * logf(sr * sr + si * si) - logf((float)cpN), atan2f(si, sr));
+}
+
+struct RcSiteOrder {
+  __device__ int operator()(int e) const { return e; }
+};
+
+__device__ inline float2 rc_warp_log_psi(const float* za, int cpN, float scale, bool cplx, bool sinhp1, int lane) {
+  return rc_warp_log_psi_at(za, cpN, scale, cplx, sinhp1, lane, RcSiteOrder{});
 }
 
 }  // namespace

@@ -80,13 +80,23 @@ __device__ inline void stage_floats(float* dst, const float* src, int64_t n) {
 }
 
 // Floats between consecutive samples' activations in the forward's shared memory: C N padded to
-// G = ceil(N / kFwdSPT) modulo 32, so that work item a G + g (sample a, site group g) falls in
+// G modulo 32, G the work items per sample (site groups ceil(N / kFwdSPT) in site order, 2 x 2
+// blocks N / 4 in blocked order), so that item a G + g (sample a, group or block g) falls in
 // bank (a G + g) mod 32 and a warp whose 32 consecutive items span two samples touches 32
 // different banks (with a stride of C N, a multiple of 32 at L = 10, the two samples' items
 // collide on up to 16 banks).
-__host__ __device__ inline int rc_sample_stride(int C, int N) {
-  const int G = (N + kFwdSPT - 1) / kFwdSPT;
+__host__ __device__ inline int rc_sample_stride(int C, int N, bool blocked) {
+  const int G = blocked ? N / 4 : (N + kFwdSPT - 1) / kFwdSPT;
   return C * N + (((G - C * N) % 32) + 32) % 32;
+}
+
+// Blocked site order of the FP32 forward at even L: the lattice is cut into N / 4 blocks of
+// 2 x 2 sites, block (by, bx) = by L/2 + bx, and site (y, x) of a channel plane is stored at
+// ((y & 1) 2 + (x & 1)) N/4 + block: four planes of N / 4 floats, one per position in the block.
+// A thread then owns the four sites of one block; for a fixed tap, the 32 lanes of a warp read
+// 32 different blocks of one plane (consecutive addresses up to the periodic wrap).
+__host__ __device__ inline int rc_blocked_site(int y, int x, int L) {
+  return ((y & 1) * 2 + (x & 1)) * (L * L / 4) + (y >> 1) * (L / 2) + (x >> 1);
 }
 
 // floats before the layer weights in the forward's shared memory: the three activation buffers,
@@ -175,6 +185,93 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
   }
 }
 
+// out[a][o][b] = act(sum_{i,tap} W[i][tap][o] in[a][i][b + tap] + bias[o]) in the blocked site
+// order (rc_blocked_site), same modes as conv_layer. A thread computes CO output channels
+// (group h of C / CO) of the four sites of one 2 x 2 block: per input channel it gathers the
+// block's 4 x 4 input patch (16 loads; patch[k] = in[nbr[16 block + k]]) and per tap reads CO
+// broadcast weights that feed 4 sites. Per multiply-add that is 0.6 times the shared-memory
+// reads of conv_layer<C, 2> (34 against 54 per input channel for 144 packed FMAs). Each output
+// sums bias, then input channels in order, taps in order: the same operations in the same
+// order as conv_layer, so both give the same floats. Items of one channel group fill whole
+// warps, so a warp's weight loads are broadcasts.
+template <int C, int CO>
+__device__ inline void conv_layer_blocked(const float* __restrict__ in, int cin, float* __restrict__ out,
+                                          const float* __restrict__ w, const int16_t* __restrict__ nbr, int N,
+                                          int S, int mode, int ss) {
+  static_assert(C % CO == 0 && CO % 4 == 0, "output channel groups of 4k channels");
+  constexpr int H = C / CO;
+  const float* bias = w + cin * 9 * C;
+  const int NB = N >> 2;
+  const int items = S * NB;
+  const int per = (items + 31) & ~31;  // items of one channel group, rounded to whole warps
+  for (int it = threadIdx.x; it < H * per; it += blockDim.x) {
+    const int h = it / per, j = it - h * per;
+    if (j >= items) continue;
+    const int a = j / NB, g = j - a * NB;
+    const int o0 = h * CO;
+    int nb[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) nb[k] = nbr[g * 16 + k];
+    float2 acc[4][CO / 2];  // block position q = 2 py + px; output channels (o0 + 2 e, o0 + 2 e + 1)
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int e = 0; e < CO / 2; ++e) acc[q][e] = make_float2(bias[o0 + 2 * e], bias[o0 + 2 * e + 1]);
+    const float* ina = in + (int64_t)a * ss;
+    for (int i = 0; i < cin; ++i) {
+      const float* ini = ina + i * N;
+      float d[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) d[k] = ini[nb[k]];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const int dy = t / 3, dx = t % 3;
+        const float4* wp = reinterpret_cast<const float4*>(w + (i * 9 + t) * C + o0);
+#pragma unroll
+        for (int o4 = 0; o4 < CO / 4; ++o4) {
+          const float4 ww = wp[o4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float x = d[((q >> 1) + dy) * 4 + (q & 1) + dx];
+            fma_pair(acc[q][2 * o4], make_float2(x, x), make_float2(ww.x, ww.y));
+            fma_pair(acc[q][2 * o4 + 1], make_float2(x, x), make_float2(ww.z, ww.w));
+          }
+        }
+      }
+    }
+    float* oa = out + (int64_t)a * ss + (int64_t)o0 * N + g;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float* oq = oa + q * NB;
+      if (mode == 0) {
+#pragma unroll
+        for (int e = 0; e < CO / 2; ++e) {
+          oq[2 * e * N] = gelu_tanh(acc[q][e].x);
+          oq[(2 * e + 1) * N] = gelu_tanh(acc[q][e].y);
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < CO / 2; ++e) {
+          oq[2 * e * N] += acc[q][e].x;
+          oq[(2 * e + 1) * N] += acc[q][e].y;
+        }
+      }
+    }
+  }
+}
+
+// 4 x 4 input patches of the 2 x 2 blocks (rows 2 by - 1 .. 2 by + 2, columns 2 bx - 1 .. 2 bx + 2,
+// periodic) as blocked indices, and the blocked index of every site r = y L + x
+__device__ inline void build_blocked_tables(int16_t* patch, int16_t* site, int L) {
+  const int N = L * L, NB = N / 4, Lh = L / 2;
+  for (int e = threadIdx.x; e < NB * 16; e += blockDim.x) {
+    const int g = e >> 4, u = (e >> 2) & 3, v = e & 3;
+    const int y = (2 * (g / Lh) - 1 + u + L) % L, x = (2 * (g % Lh) - 1 + v + L) % L;
+    patch[e] = (int16_t)rc_blocked_site(y, x, L);
+  }
+  for (int r = threadIdx.x; r < N; r += blockDim.x) site[r] = (int16_t)rc_blocked_site(r / L, r % L, L);
+}
+
 __device__ inline void build_nbr(int16_t* nbr, int L) {
   const int N = L * L;
   for (int e = threadIdx.x; e < N * 9; e += blockDim.x) {
@@ -185,22 +282,42 @@ __device__ inline void build_nbr(int16_t* nbr, int L) {
   }
 }
 
+struct RcBlockedOrder {  // element c N + r of the site order -> its place in the blocked order
+  const int16_t* site;
+  int N;
+  __device__ int operator()(int e) const {
+    const int c = e / N;
+    return c * N + site[e - c * N];
+  }
+};
+
+// output channels per thread in conv_layer_blocked: 8 where C allows (two groups at C = 16)
+template <int C>
+constexpr int rc_blocked_co() { return C % 8 == 0 ? 8 : 4; }
+
 // Forward of ncfg packed configurations (nw words each). n_live (device, may be NULL)
 // caps the count at run time. out: (re, im) of log psi per configuration.
-template <int C>
-__global__ void __launch_bounds__(kFwdThreads)
+// BLK (even L): activations in the blocked site order and conv_layer_blocked; otherwise site
+// order and conv_layer. Both give the same floats: every convolution output is the same chain
+// of operations, and the final sum runs over the site order in both.
+template <int C, bool BLK>
+__global__ void __launch_bounds__(kFwdThreads, 2)
     rc_forward_kernel(const float* __restrict__ table, ConvNet net, const uint32_t* __restrict__ cfg, int64_t ncfg,
                       const int64_t* __restrict__ n_live, float2* __restrict__ out, int S) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int N = net.N, nw = words_for(N);
-  const int SS = rc_sample_stride(C, N);
+  const int SS = rc_sample_stride(C, N, BLK);
   float* X = sm;
   float* P = X + (int64_t)S * SS;
   float* Q = P + (int64_t)S * SS;
   float* Wl = sm + rc_weights_offset(S, SS);  // 16-byte aligned: the weights are read as float4
   int16_t* nbr = reinterpret_cast<int16_t*>(Wl + C * 9 * C + C);
-  build_nbr(nbr, net.L);
+  int16_t* site = nbr + (BLK ? N * 4 : 0);  // blocked index of each site (BLK only)
+  if (BLK)
+    build_blocked_tables(nbr, site, net.L);
+  else
+    build_nbr(nbr, net.L);
   const int64_t total = n_live ? min(ncfg, *n_live) : ncfg;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t base = (int64_t)blockIdx.x * S; base < total; base += (int64_t)gridDim.x * S) {
@@ -210,7 +327,8 @@ __global__ void __launch_bounds__(kFwdThreads)
       const int a = e / N, r = e % N;
       float v = 0.0f;
       if (a < s_here) v = ((cfg[(base + a) * nw + (r >> 5)] >> (r & 31)) & 1u) ? 1.0f : -1.0f;
-      for (int c = 0; c < C; ++c) X[(int64_t)a * SS + c * N + r] = v;
+      const int k = BLK ? site[r] : r;
+      for (int c = 0; c < C; ++c) X[(int64_t)a * SS + c * N + k] = v;
     }
     for (int b = 0; b < net.B; ++b) {
       const float scale = rsqrtf((float)(b + 1)) * (b == 0 ? 0.70710678118654752f : 1.0f);
@@ -223,18 +341,26 @@ __global__ void __launch_bounds__(kFwdThreads)
       }
       stage_floats(Wl, table + layer_offset(2 * b, C), layer_floats(2 * b, C));
       __syncthreads();
-      conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0, SS);
+      if (BLK)
+        conv_layer_blocked<C, rc_blocked_co<C>()>(P, cin, Q, Wl, nbr, N, S, 0, SS);
+      else
+        conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0, SS);
       __syncthreads();
       stage_floats(Wl, table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
       __syncthreads();
-      conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1, SS);
+      if (BLK)
+        conv_layer_blocked<C, rc_blocked_co<C>()>(Q, C, X, Wl, nbr, N, S, 1, SS);
+      else
+        conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1, SS);
     }
     __syncthreads();
     // log of the mean final activation over (channel, site) per sample, one warp per sample
     const float fs = rsqrtf((float)(net.B + 1));
     const int cp = net.cplx ? C / 2 : C;
     for (int a = warp; a < s_here; a += kFwdThreads / 32) {
-      const float2 lp = rc_warp_log_psi(X + (int64_t)a * SS, cp * N, fs, net.cplx, net.sinhp1, lane);
+      const float* za = X + (int64_t)a * SS;
+      const float2 lp = BLK ? rc_warp_log_psi_at(za, cp * N, fs, net.cplx, net.sinhp1, lane, RcBlockedOrder{site, N})
+                            : rc_warp_log_psi(za, cp * N, fs, net.cplx, net.sinhp1, lane);
       if (lane == 0) out[base + a] = lp;
     }
   }
@@ -788,20 +914,52 @@ int launch_jacobian_c(const float* table, const ConvNet& net, const uint32_t* sp
   return launch_status();
 }
 
+// the blocked site order (conv_layer_blocked) at even L, the site order otherwise
+inline bool rc_blocked(const ConvNet& net) { return net.L % 2 == 0; }
+
 int rc_smem_bytes(const ConvNet& net, int S) {
-  const int64_t f = rc_weights_offset(S, rc_sample_stride(net.C, net.N)) + (int64_t)net.C * 9 * net.C + net.C;
-  return (int)(f * 4 + (int64_t)net.N * 9 * 2 + 16);
+  const bool blk = rc_blocked(net);
+  const int64_t f = rc_weights_offset(S, rc_sample_stride(net.C, net.N, blk)) + (int64_t)net.C * 9 * net.C + net.C;
+  const int64_t tables = blk ? (int64_t)net.N * 4 + net.N : (int64_t)net.N * 9;  // int16 entries
+  return (int)(f * 4 + tables * 2 + 16);
+}
+
+// samples per CTA in the blocked order: the count whose work items (channel groups x samples x
+// blocks, each group rounded to whole warps) fill the 256 threads' passes best, among the counts
+// whose shared memory leaves room for two CTAs per SM (any count that fits, if none does): 5 at
+// L = 10 with 16 channels (2 x 128 items, 250 of them used), 32 at L = 4
+template <int C>
+int rc_blocked_samples(const ConvNet& net) {
+  constexpr int H = C / rc_blocked_co<C>();
+  const int NB = net.N / 4;
+  const int cap = device_max_smem_optin();
+  const int two = (cap + 1024) / 2 - 1024;  // 1 KB of each CTA's shared memory is reserved
+  for (int limit : {two, cap}) {
+    int best = 0;
+    double best_fill = 0.0;
+    for (int s = 1; s <= 64 && rc_smem_bytes(net, s) <= limit; ++s) {
+      const int per = (s * NB + 31) & ~31;
+      const int passes = (H * per + kFwdThreads - 1) / kFwdThreads;
+      const double fill = (double)H * s * NB / ((double)passes * kFwdThreads);
+      if (fill > best_fill + 1e-9) best_fill = fill, best = s;
+    }
+    if (best > 0) return best;
+  }
+  return 1;
 }
 
 template <int C>
 int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                      float2* out, cudaStream_t st) {
-  // kFwdSamples per CTA, fewer where their buffers would not fit (L = 16: 4)
+  const bool blk = rc_blocked(net);
+  // site order: kFwdSamples per CTA (5 x 50 site pairs fill 256 threads at L = 10), fewer where
+  // their buffers would not fit (L = 16: 4)
   int S = kFwdSamples;
   while (S > 1 && rc_smem_bytes(net, S) > device_max_smem_optin()) --S;
+  if (blk) S = rc_blocked_samples<C>(net);
   const int smem = rc_smem_bytes(net, S);
   if (smem > device_max_smem_optin()) return QGX_ERR_UNSUPPORTED;
-  auto k = rc_forward_kernel<C>;
+  auto k = blk ? rc_forward_kernel<C, true> : rc_forward_kernel<C, false>;
   if (smem > 48 * 1024) QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   int per_sm = 0;
   QGX_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kFwdThreads, smem));

@@ -193,11 +193,14 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
 // reads of conv_layer<C, 2> (34 against 54 per input channel for 144 packed FMAs). Each output
 // sums bias, then input channels in order, taps in order: the same operations in the same
 // order as conv_layer, so both give the same floats. Items of one channel group fill whole
-// warps, so a warp's weight loads are broadcasts.
+// warps, so a warp's weight loads are broadcasts. In mode 1 with pnext, the updated residual x
+// is also written as the next block's pre-activation pnext = gelu(x pscale) (the separate pass
+// of the site-order kernel, the same floats).
 template <int C, int CO>
 __device__ inline void conv_layer_blocked(const float* __restrict__ in, int cin, float* __restrict__ out,
                                           const float* __restrict__ w, const int16_t* __restrict__ nbr, int N,
-                                          int S, int mode, int ss) {
+                                          int S, int mode, int ss, float* __restrict__ pnext = nullptr,
+                                          float pscale = 1.0f) {
   static_assert(C % CO == 0 && CO % 4 == 0, "output channel groups of 4k channels");
   constexpr int H = C / CO;
   const float* bias = w + cin * 9 * C;
@@ -249,14 +252,36 @@ __device__ inline void conv_layer_blocked(const float* __restrict__ in, int cin,
           oq[2 * e * N] = gelu_tanh(acc[q][e].x);
           oq[(2 * e + 1) * N] = gelu_tanh(acc[q][e].y);
         }
-      } else {
+      } else if (pnext == nullptr) {
 #pragma unroll
         for (int e = 0; e < CO / 2; ++e) {
           oq[2 * e * N] += acc[q][e].x;
           oq[(2 * e + 1) * N] += acc[q][e].y;
         }
+      } else {
+        float* pq = pnext + (oq - out);
+#pragma unroll
+        for (int e = 0; e < CO / 2; ++e) {
+          const float x0 = oq[2 * e * N] + acc[q][e].x, x1 = oq[(2 * e + 1) * N] + acc[q][e].y;
+          oq[2 * e * N] = x0;
+          oq[(2 * e + 1) * N] = x1;
+          pq[2 * e * N] = gelu_tanh(x0 * pscale);
+          pq[(2 * e + 1) * N] = gelu_tanh(x1 * pscale);
+        }
       }
     }
+  }
+}
+
+// Asks L1 for the 128-byte lines of the n floats at src, one prefetch per line, every address
+// inside [src, src + n). Issued for the next layer's weights before a convolution, so that the
+// staging after it reads L1 rather than L2.
+__device__ inline void prefetch_l1(const float* src, int64_t n) {
+  const size_t a0 = __cvta_generic_to_global(src), a1 = __cvta_generic_to_global(src + n);
+  for (size_t k = threadIdx.x;; k += blockDim.x) {
+    const size_t a = k == 0 ? a0 : (a0 & ~size_t(127)) + 128 * k;
+    if (a >= a1) break;
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
   }
 }
 
@@ -334,12 +359,15 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
       const float scale = rsqrtf((float)(b + 1)) * (b == 0 ? 0.70710678118654752f : 1.0f);
       const int cin = b == 0 ? 1 : C;
       __syncthreads();
-      for (int e = threadIdx.x; e < S * cin * N; e += blockDim.x) {
-        const int a = e / (cin * N), rem = e % (cin * N);
-        const float v = X[(int64_t)a * SS + rem] * scale;
-        P[(int64_t)a * SS + rem] = b == 0 ? v : gelu_tanh(v);
+      if (!BLK || b == 0) {  // blocked: blocks b >= 1 get P from the previous block's second convolution
+        for (int e = threadIdx.x; e < S * cin * N; e += blockDim.x) {
+          const int a = e / (cin * N), rem = e % (cin * N);
+          const float v = X[(int64_t)a * SS + rem] * scale;
+          P[(int64_t)a * SS + rem] = b == 0 ? v : gelu_tanh(v);
+        }
       }
       stage_floats(Wl, table + layer_offset(2 * b, C), layer_floats(2 * b, C));
+      if (BLK) prefetch_l1(table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
       __syncthreads();
       if (BLK)
         conv_layer_blocked<C, rc_blocked_co<C>()>(P, cin, Q, Wl, nbr, N, S, 0, SS);
@@ -347,9 +375,13 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
         conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0, SS);
       __syncthreads();
       stage_floats(Wl, table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
+      // the next layer in order: the next block's first convolution, or block 0's for the next samples
+      const int lnext = b + 1 < net.B ? 2 * b + 2 : 0;
+      if (BLK) prefetch_l1(table + layer_offset(lnext, C), layer_floats(lnext, C));
       __syncthreads();
       if (BLK)
-        conv_layer_blocked<C, rc_blocked_co<C>()>(Q, C, X, Wl, nbr, N, S, 1, SS);
+        conv_layer_blocked<C, rc_blocked_co<C>()>(Q, C, X, Wl, nbr, N, S, 1, SS, b + 1 < net.B ? P : nullptr,
+                                                  rsqrtf((float)(b + 2)));
       else
         conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1, SS);
     }

@@ -350,6 +350,38 @@ int qgx_resconv_jacobian_symm(const float* table, int32_t L, int32_t nblocks, in
                               float* O_re, float* O_im, int64_t ldo, void* workspace,
                               int64_t workspace_bytes, qgx_stream_t stream);
 
+/* The projected RBM_Dense (Variational(RBM_Dense, symm=...): the reference projects any model,
+ * quantax/state/variational.py:261-266). The table is qgx_rbm_prepare's; n <= 256 sites,
+ * m <= 2048 hidden units. Every T_g s runs through the RBM's own forward and closed-form
+ * log-derivatives; the projection itself is the ResConv entry points' pipeline. log_psi holds
+ * (re, im) pairs: psi_symm is complex for complex characters and signed for real ones. */
+int64_t qgx_rbm_log_psi_symm_workspace_bytes(int32_t n, int64_t ns, int32_t nsymm);
+int qgx_rbm_log_psi_symm(const float* table, int32_t n, int32_t m, const qgx_symm_t* symm,
+                         const uint32_t* spins, int64_t ns, float* log_psi, void* workspace,
+                         int64_t workspace_bytes, qgx_stream_t stream);
+int64_t qgx_rbm_sweep_symm_workspace_bytes(int32_t n, int64_t ns, int32_t nsymm);
+/* Metropolis sweep of the projected RBM (metropolis.py:246-322): per step every chain
+ * proposes (LocalFlip: one uniform site, Philox word 0; SpinExchange as qgx_rbm_sweep, nbr may
+ * be NULL for LocalFlip), the changed proposals are evaluated as one projected batch and
+ * accepted in log space on the shared Philox stream. log_psi: (re, im) pairs, out. */
+int qgx_rbm_sweep_symm(const float* table, int32_t n, int32_t m, const qgx_symm_t* symm, uint32_t* spins,
+                       float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed,
+                       uint64_t step0, float reweight, int32_t proposal, const int32_t* nbr, int32_t z,
+                       int32_t hop, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+int64_t qgx_rbm_eloc_symm_workspace_bytes(int32_t n, int64_t ns, int32_t max_conn, int32_t nsymm);
+/* E_loc of the projected RBM (operator.py:510-562): eloc_im may be NULL for real characters. */
+int qgx_rbm_eloc_symm(const float* table, int32_t n, int32_t m, const qgx_symm_t* symm,
+                      const qgx_operator_t* op, const uint32_t* spins, int64_t ns, double* eloc_re,
+                      double* eloc_im, void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+int64_t qgx_rbm_jacobian_symm_workspace_bytes(int32_t n, int32_t m, int32_t has_vbias, int64_t ns,
+                                              int32_t nsymm);
+/* d log psi_symm / d params = sum_g v_g O(T_g s), v_g = w_g psi(T_g s) / psi_symm(s): the images'
+ * closed-form O rows (qgx_rbm_jacobian's) combined per sample in FP32, Re to O_re, Im to O_im
+ * (may be NULL), parameter order as qgx_rbm_jacobian. */
+int qgx_rbm_jacobian_symm(const float* table, int32_t n, int32_t m, int32_t has_vbias, const qgx_symm_t* symm,
+                          const uint32_t* spins, int64_t ns, float* O_re, float* O_im, int64_t ldo,
+                          void* workspace, int64_t workspace_bytes, qgx_stream_t stream);
+
 /* ---- statistics and centring (quantax/optimizer/sr.py:76-88, 180-195) ----------------- */
 /* energy = Re mean(E r), VarE = mean(|E - energy|^2 r) with compensated FP64 sums;
  * ebar = (E - mean E) sqrt(r / ns). E_im / ebar_im may be NULL for real E.

@@ -143,6 +143,16 @@ SIGNATURES = {
     "qgx_resconv_jacobian_symm_workspace_bytes": (i64, [i32, i32, i32, i64, i32]),
     "qgx_resconv_jacobian_symm": (C.c_int, [vp, i32, i32, i32, i32, C.POINTER(Symm), vp, i64, vp, vp, i64, vp, i64,
                                             vp]),
+    "qgx_rbm_log_psi_symm_workspace_bytes": (i64, [i32, i64, i32]),
+    "qgx_rbm_log_psi_symm": (C.c_int, [vp, i32, i32, C.POINTER(Symm), vp, i64, vp, vp, i64, vp]),
+    "qgx_rbm_sweep_symm_workspace_bytes": (i64, [i32, i64, i32]),
+    "qgx_rbm_sweep_symm": (C.c_int, [vp, i32, i32, C.POINTER(Symm), vp, vp, vp, i64, i32, u64, u64, f32, i32, vp, i32,
+                                     i32, vp, i64, vp]),
+    "qgx_rbm_eloc_symm_workspace_bytes": (i64, [i32, i64, i32, i32]),
+    "qgx_rbm_eloc_symm": (C.c_int, [vp, i32, i32, C.POINTER(Symm), C.POINTER(Operator), vp, i64, vp, vp, vp, i64,
+                                    vp]),
+    "qgx_rbm_jacobian_symm_workspace_bytes": (i64, [i32, i32, i32, i64, i32]),
+    "qgx_rbm_jacobian_symm": (C.c_int, [vp, i32, i32, i32, C.POINTER(Symm), vp, i64, vp, vp, i64, vp, i64, vp]),
     "qgx_rbm_conv_table_floats": (i64, [i32, i32, i32]),
     "qgx_rbm_conv_prepare": (C.c_int, [vp, i32, i32, i32, vp, vp]),
     "qgx_rbm_conv_jacobian": (C.c_int, [vp, i32, i32, i32, vp, i64, vp, i64, vp]),
@@ -173,7 +183,7 @@ KERNELS_PER_CALL = {
     "qgx_spins_pack": 1, "qgx_operator_diag": 1, "qgx_rbm_prepare": 1, "qgx_rbm_log_psi": 1, "qgx_rbm_sweep": 1,
     "qgx_rbm_eloc": 1, "qgx_rbm_jacobian": 1, "qgx_rbm_obar": 4, "qgx_rbm_obar_noalloc": 4, "qgx_resconv_prepare": 2,
     "qgx_resconv_log_psi": 1, "qgx_resconv_eloc": 6, "qgx_resconv_log_psi_symm": 3, "qgx_resconv_eloc_symm": 10,
-    "qgx_resconv_jacobian_symm": 4,
+    "qgx_resconv_jacobian_symm": 4, "qgx_rbm_log_psi_symm": 3, "qgx_rbm_eloc_symm": 10,
     "qgx_resconv_jacobian": 1, "qgx_energy_stats": 1, "qgx_reweight_factor": 1,
     "qgx_gram": 1, "qgx_gram_t": 1, "qgx_gram_tc": 1, "qgx_f32_to_bf16": 1, "qgx_transpose": 1, "qgx_obar_matvec": 1, "qgx_obar_rmatvec": 2, "qgx_rbm_conv_prepare": 1, "qgx_column_sumsq": 2,
     "qgx_rbm_conv_jacobian": 1, "qgx_apply_update": 2, "qgx_csr_matvec": 1, "qgx_er_weight_rows": 1, "qgx_exact_draw": 1,
@@ -185,8 +195,8 @@ launch_count = 0
 def _kernels(name, args):
     if name in ("qgx_minsr_solve", "qgx_sr_solve", "qgx_sym_solve"):
         return int(lib().qgx_last_solve_kernels())
-    if name == "qgx_center_columns":  # partial sums, reduction, mean split, then 65535 rows per centring launch
-        return 3 + (int(args[1]) - 1) // 65535 + 1 if int(args[1]) > 0 else 0
+    if name == "qgx_center_columns":  # partial sums, reduction, mean split, centring
+        return 4 if int(args[1]) > 0 else 0
     if name == "qgx_scale_columns":
         return 1 + (int(args[1]) - 1) // 65535 if int(args[1]) > 0 and int(args[2]) > 0 else 0
     if name in ("qgx_rbm_sweep_batched", "qgx_rbm_eloc_batched"):  # the count the call reports
@@ -195,6 +205,15 @@ def _kernels(name, args):
         return 2 + 3 * int(args[10])  # step base, forward, then propose / forward / accept per step
     if name == "qgx_resconv_sweep_symm":
         return 4 + 5 * int(args[11])  # each forward is expand / forward / combine
+    if name == "qgx_rbm_sweep_symm":
+        return 4 + 5 * int(args[8])
+    if name == "qgx_rbm_jacobian_symm":  # the projected forward, then per chunk of samples the rows and their sum
+        n, m, vb, ns = int(args[1]), int(args[2]), int(args[3]), int(args[6])
+        sym = args[4]._obj
+        nsymm = sym.nperm * (2 if sym.z2 else 1)
+        npar = m * n + m + (n if vb else 0)
+        cs = max(1, min(min(ns, 65535), (1 << 26) // (nsymm * npar)))
+        return 3 + 2 * ((ns + cs - 1) // cs) if ns > 0 else 0
     return KERNELS_PER_CALL.get(name, 0)
 
 

@@ -152,6 +152,13 @@ __device__ inline float2 rc_warp_log_psi(const float* za, int cpN, float scale, 
 // writes both tensor-core weight images from the FP32 part of the table (resconv_tc.cu)
 int rc_prepare_tc_images(float* table, int B, int C, cudaStream_t st);
 
+// RBM_Dense on the images of a projected RBM (rbm.cu): log psi as (log psi, 0) pairs of ncfg
+// configurations (n_live: device run-time cap, may be NULL), and the uncentred O rows
+int rbm_log_psi_pairs(const float* table, int n, int m, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
+                      float2* out, cudaStream_t st);
+int rbm_jacobian_rows(const float* table, int n, int m, int has_vbias, const uint32_t* cfg, int64_t rows, float* O,
+                      int64_t ldo, cudaStream_t st);
+
 // tensor-core forward (resconv_tc.cu); kind 0: TF32 operands, 1: BF16 operands (grouped: the
 // warp-specialised kernel, where its shape fits)
 int rc_launch_forward_tc(const float* table, int L, int B, int C, bool cplx, bool sinhp1, const uint32_t* cfg,

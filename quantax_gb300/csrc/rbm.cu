@@ -482,10 +482,13 @@ __device__ inline RbmTable stage_forward(float* sm, const float* table, int n, i
   return S;
 }
 
+// log psi of ns configurations (n_live, device, may be NULL: a run-time cap on the count);
+// written to log_psi[c], or as the pair (log psi, 0) to pairs[c] when pairs is set
 template <int JT, bool SMEM, int NT>
 __global__ void __launch_bounds__(NT)
     log_psi_kernel(const float* __restrict__ table, int n, int mp, const uint32_t* __restrict__ spins, int64_t ns,
-                   float* __restrict__ log_psi, int64_t fwd_nf) {
+                   float* __restrict__ log_psi, int64_t fwd_nf, const int64_t* __restrict__ n_live = nullptr,
+                   float2* __restrict__ pairs = nullptr) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   constexpr int kWarps = NT / 32;
@@ -493,15 +496,21 @@ __global__ void __launch_bounds__(NT)
   uint32_t* sp = reinterpret_cast<uint32_t*>(sm + (SMEM ? fwd_nf : 0)) + 32 * (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = words_for(n);
+  const int64_t total = n_live ? min(ns, *n_live) : ns;
   for (int64_t slot = warp;; slot += kWarps) {
     const int64_t c = slot * gridDim.x + blockIdx.x;
-    if (c >= ns) break;
+    if (c >= total) break;
     if (lane < nw) sp[lane] = spins[c * nw + lane];
     __syncwarp();
     float th[JT][4];
     compute_theta<JT>(T, n, mp, sp, lane, th);
     const float lp = sum_logcosh<JT>(th) + visible_dot(T.a, n, sp, lane);
-    if (lane == 0) log_psi[c] = lp;
+    if (lane == 0) {
+      if (pairs)
+        pairs[c] = make_float2(lp, 0.0f);
+      else
+        log_psi[c] = lp;
+    }
     __syncwarp();
   }
 }
@@ -810,18 +819,18 @@ constexpr int kFwdThreads = 256;
 
 template <int JT>
 int launch_log_psi(const float* table, int n, int mp, const uint32_t* spins, int64_t ns, float* log_psi,
-                   cudaStream_t st) {
+                   cudaStream_t st, const int64_t* n_live = nullptr, float2* pairs = nullptr) {
   const int64_t ff = fwd_floats(n, mp);
   size_t smem;
   int grid, rc;
   if (fits_smem(kFwdThreads, ff, 32, &smem)) {
     auto k = log_psi_kernel<JT, true, kFwdThreads>;
     if ((rc = configure(k, kFwdThreads, smem, (ns + 7) / 8, &grid)) != QGX_OK) return rc;
-    k<<<grid, kFwdThreads, smem, st>>>(table, n, mp, spins, ns, log_psi, ff);
+    k<<<grid, kFwdThreads, smem, st>>>(table, n, mp, spins, ns, log_psi, ff, n_live, pairs);
   } else {
     auto k = log_psi_kernel<JT, false, kFwdThreads>;
     if ((rc = configure(k, kFwdThreads, smem, (ns + 7) / 8, &grid)) != QGX_OK) return rc;
-    k<<<grid, kFwdThreads, smem, st>>>(table, n, mp, spins, ns, log_psi, ff);
+    k<<<grid, kFwdThreads, smem, st>>>(table, n, mp, spins, ns, log_psi, ff, n_live, pairs);
   }
   return launch_status();
 }
@@ -979,6 +988,26 @@ inline bool stages_in_smem(int jt, int n, int mp) {
 }
 
 }  // namespace
+
+// The RBM forward and log-derivatives that the symmetrised pipelines of resconv.cu run on the
+// images T_g s of a projected RBM: log psi as (log psi, 0) pairs with a run-time live count,
+// and the O rows of every image (closed form, uncentred).
+int rbm_log_psi_pairs(const float* table, int n, int m, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
+                      float2* out, cudaStream_t st) {
+  const int mp = padded_m(m);
+#define CALL(JT) launch_log_psi<JT>(table, n, mp, cfg, ncfg, nullptr, st, n_live, out)
+  QGX_DISPATCH_JT(mp, CALL)
+#undef CALL
+}
+
+int rbm_jacobian_rows(const float* table, int n, int m, int has_vbias, const uint32_t* cfg, int64_t rows, float* O,
+                      int64_t ldo, cudaStream_t st) {
+  const int mp = padded_m(m);
+#define CALL(JT) launch_jacobian<JT>(table, n, m, mp, has_vbias, cfg, rows, O, ldo, false, nullptr, nullptr, st)
+  QGX_DISPATCH_JT(mp, CALL)
+#undef CALL
+}
+
 }  // namespace qgx
 
 using namespace qgx;

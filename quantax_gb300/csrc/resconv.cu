@@ -36,7 +36,18 @@ struct ConvNet {
   int prec;     // QGX_CONV_*: arithmetic of the forward convolutions
   bool sinhp1;  // final activation sinhp1_by_scale instead of exp_by_scale
   bool grouped;  // QGX_CONV_GROUPED: the warp-specialised BF16 kernel
+  // rbm_m > 0: not a ResConv but RBM_Dense with rbm_m hidden units on N sites (the symmetrised
+  // pipelines below evaluate its images T_g s); rbm_vbias: its table holds a visible bias
+  int rbm_m = 0;
+  int rbm_vbias = 0;
 };
+
+inline ConvNet make_rbm_net(int n, int m, int has_vbias) {
+  ConvNet net{0, n, 0, 0, false, QGX_CONV_FP32, false, false};
+  net.rbm_m = m;
+  net.rbm_vbias = has_vbias != 0;
+  return net;
+}
 
 // the complex_out argument of the entry points: QGX_RESCONV_COMPLEX | QGX_RESCONV_SINHP1
 inline ConvNet make_net(int L, int B, int C, int out_flags, int prec) {
@@ -408,7 +419,7 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
 __global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* __restrict__ comp,
                                   int32_t* __restrict__ comp_idx, unsigned long long* __restrict__ n_live, int64_t ns,
                                   int n, uint64_t seed, const uint64_t* __restrict__ step_base, int t,
-                                  const int32_t* __restrict__ nbr, int z, int hop) {
+                                  const int32_t* __restrict__ nbr, int z, int hop, int proposal) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ns) return;
   const uint64_t step = *step_base + (uint64_t)t;
@@ -416,7 +427,11 @@ __global__ void rc_propose_kernel(const uint32_t* __restrict__ spins, uint32_t* 
   uint32_t w[8];
   for (int k = 0; k < nw; ++k) w[k] = spins[c * nw + k];
   const u32x4 r = draw(seed, (uint64_t)c, step, kTagPropose);
-  if (!propose_exchange(w, n, nw, r, nbr, z, hop)) {
+  if (proposal == QGX_PROPOSAL_LOCAL_FLIP) {
+    // LocalFlip (common_samplers.py:28-33): one uniform site, always a change
+    const int k = (int)bounded(r.x, (uint32_t)n);
+    w[k >> 5] ^= 1u << (k & 31);
+  } else if (!propose_exchange(w, n, nw, r, nbr, z, hop)) {
     comp_idx[c] = -1;
     return;
   }
@@ -1004,6 +1019,7 @@ int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg
 
 int launch_forward(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                    float2* out, cudaStream_t st) {
+  if (net.rbm_m > 0) return rbm_log_psi_pairs(table, net.N, net.rbm_m, cfg, ncfg, n_live, out, st);
   if (net.prec != QGX_CONV_FP32)
     return rc_launch_forward_tc(table, net.L, net.B, net.C, net.cplx, net.sinhp1, cfg, ncfg, n_live, out,
                                 net.prec == QGX_CONV_BF16 ? 1 : 0, net.grouped, st);
@@ -1053,7 +1069,7 @@ struct SweepKey {
   const void *table, *spins, *lp, *acc, *nbr, *ws, *perm, *weight;
   int64_t nperm_nsymm;
   int64_t ns;
-  int nsteps, L, B, C, cplx, prec, z, hop, device;
+  int nsteps, L, N, B, C, cplx, prec, z, hop, device, rbm_m, rbm_vbias, proposal;
   uint64_t seed;
   float reweight;
   bool operator==(const SweepKey& o) const { return std::memcmp(this, &o, sizeof(SweepKey)) == 0; }
@@ -1091,6 +1107,64 @@ bool to_symm(const qgx_symm_t* s, SymmDev* d) {
   d->nperm = s->nperm;
   d->nsymm = s->nperm * (s->z2 != 0 ? 2 : 1);
   return d->nsymm <= kMaxSymm;
+}
+
+// ---- the projected RBM (Variational(RBM_Dense, symm=...)) ------------------------------------
+// RBM_Dense sizes the symmetrised pipelines take: a packed configuration of at most 8 words
+// (the proposal kernel's registers) and the RBM kernels' hidden-unit widths
+bool valid_rbm_symm(int n, int m) { return n >= 1 && n <= kMaxSitesConv && m >= 1 && m <= 2048; }
+
+int64_t eloc_scratch_bytes(int n, int64_t ns, int max_conn) {
+  const int nw = words_for(n);
+  const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
+  return al256(ns * 8) + al256((ns + 1) * 8) + al256(nc * nw * 4) + al256(nc * 8) + al256(nc * 8) + al256(ns * 8);
+}
+
+int64_t sweep_scratch_bytes(int n, int64_t ns) {
+  const int nw = words_for(n);
+  return al256(ns * nw * 4) + al256(ns * 8) + al256(ns * 4) + al256(16);
+}
+
+// samples per pass of the projected RBM's log-derivatives: their images' O rows (nsymm x np
+// floats each) fill at most 2^26 floats, at least one sample
+int64_t rbm_symm_chunk(int64_t ns, int nsymm, int64_t np) {
+  const int64_t per = (int64_t)nsymm * np;
+  return std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(ns, 65535), (int64_t(1) << 26) / per));
+}
+
+// O_symm[c][p] = sum_g v_g O(T_g s_c)[p], v_g = w_g psi(T_g s_c) / psi_symm(s_c) (the cotangents
+// of variational.py:441-477 for a holomorphic-free real model), from the images' rows
+// rows[(c - c0) nsymm + g][p] of the samples c0 .. c0 + gridDim.y - 1; Re to O_re, Im to O_im
+// (may be NULL). FP32 sums over the group in its order.
+__global__ void __launch_bounds__(256)
+    rbm_symm_rows_kernel(const float* __restrict__ rows, int64_t np, int64_t c0, int nsymm,
+                         const float2* __restrict__ lp_g, const float2* __restrict__ lp_sym,
+                         const double* __restrict__ weight, float* __restrict__ O_re, float* __restrict__ O_im,
+                         int64_t ldo) {
+  extern __shared__ float2 v[];
+  const int64_t cl = blockIdx.y, c = c0 + cl;
+  const float2 ls = lp_sym[c];
+  for (int g = threadIdx.x; g < nsymm; g += blockDim.x) {
+    const float2 lg = lp_g[c * nsymm + g];
+    const float e = expf(lg.x - ls.x);
+    float sn, cs;
+    sincosf(lg.y - ls.y, &sn, &cs);
+    const float ar = e * cs, ai = e * sn;
+    const float wr = (float)weight[2 * g], wi = (float)weight[2 * g + 1];
+    v[g] = make_float2(wr * ar - wi * ai, wr * ai + wi * ar);
+  }
+  __syncthreads();
+  const float* base = rows + cl * nsymm * np;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+    float re = 0.0f, im = 0.0f;
+    for (int g = 0; g < nsymm; ++g) {
+      const float o = base[(int64_t)g * np + p];
+      re = fmaf(v[g].x, o, re);
+      im = fmaf(v[g].y, o, im);
+    }
+    O_re[c * ldo + p] = re;
+    if (O_im) O_im[c * ldo + p] = im;
+  }
 }
 
 }  // namespace
@@ -1141,11 +1215,11 @@ int64_t qgx_resconv_sweep_workspace_bytes(int32_t L, int64_t ns) {
 namespace qgx {
 namespace {
 
-int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-               int32_t conv_precision, const SymmDev* sym, uint32_t* spins, float* log_psi, int32_t* accepts,
-               int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0, float reweight, const int32_t* nbr, int32_t z,
-               int32_t hop, void* workspace, cudaStream_t st) {
-  const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
+// out_flags: the ResConv output flags (0 for an RBM); proposal: QGX_PROPOSAL_*
+int sweep_impl(const float* table, const ConvNet& net, int32_t out_flags, const SymmDev* sym, uint32_t* spins,
+               float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0,
+               float reweight, int32_t proposal, const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
+               cudaStream_t st) {
   const int nw = words_for(net.N);
   char* ws = static_cast<char*>(workspace);
   uint32_t* comp = reinterpret_cast<uint32_t*>(ws);
@@ -1163,7 +1237,7 @@ int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels,
     if (accepts) QGX_CHECK_CUDA(cudaMemsetAsync(accepts, 0, ns * sizeof(int32_t), s));
     for (int t = 0; t < nsteps; ++t) {
       rc_propose_kernel<<<g, 128, 0, s>>>(spins, comp, comp_idx, n_live, ns, net.N, seed, step_base, t, nbr, z,
-                                          hop);
+                                          hop, proposal);
       rc = symm_forward(table, net, sym, comp, ns, reinterpret_cast<const int64_t*>(n_live), lp_comp, sscratch, s);
       if (rc != QGX_OK) return rc;
       rc_accept_kernel<<<g, 128, 0, s>>>(spins, lp, comp, lp_comp, comp_idx, n_live, accepts, ns, net.N, seed,
@@ -1191,11 +1265,15 @@ int sweep_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels,
   }
   key.ns = ns;
   key.nsteps = nsteps;
-  key.L = L;
-  key.B = nblocks;
-  key.C = channels;
-  key.cplx = complex_out;  // the output flags
-  key.prec = conv_precision;
+  key.L = net.L;
+  key.N = net.N;
+  key.B = net.B;
+  key.C = net.C;
+  key.cplx = out_flags;
+  key.prec = net.prec | (net.grouped ? QGX_CONV_GROUPED : 0);
+  key.rbm_m = net.rbm_m;
+  key.rbm_vbias = net.rbm_vbias;
+  key.proposal = proposal;
   key.z = z;
   key.hop = hop;
   key.device = dev;
@@ -1251,8 +1329,9 @@ int qgx_resconv_sweep(const float* table, int32_t L, int32_t nblocks, int32_t ch
   QGX_CHECK_ARG(table && spins && log_psi && workspace);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_workspace_bytes(L, ns));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  return sweep_impl(table, L, nblocks, channels, complex_out, conv_precision, nullptr, spins, log_psi, accepts, ns,
-                    nsteps, seed, step0, reweight, nbr, z, hop, workspace, as_cuda(stream));
+  return sweep_impl(table, make_net(L, nblocks, channels, complex_out, conv_precision), complex_out, nullptr, spins,
+                    log_psi, accepts, ns, nsteps, seed, step0, reweight, QGX_PROPOSAL_SPIN_EXCHANGE, nbr, z, hop,
+                    workspace, as_cuda(stream));
 }
 
 int64_t qgx_resconv_sweep_symm_workspace_bytes(int32_t L, int64_t ns, int32_t nsymm) {
@@ -1274,8 +1353,9 @@ int qgx_resconv_sweep_symm(const float* table, int32_t L, int32_t nblocks, int32
   QGX_CHECK_ARG(table && spins && log_psi && workspace);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_sweep_symm_workspace_bytes(L, ns, sym.nsymm));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  return sweep_impl(table, L, nblocks, channels, complex_out, conv_precision, &sym, spins, log_psi, accepts, ns,
-                    nsteps, seed, step0, reweight, nbr, z, hop, workspace, as_cuda(stream));
+  return sweep_impl(table, make_net(L, nblocks, channels, complex_out, conv_precision), complex_out, &sym, spins,
+                    log_psi, accepts, ns, nsteps, seed, step0, reweight, QGX_PROPOSAL_SPIN_EXCHANGE, nbr, z, hop,
+                    workspace, as_cuda(stream));
 }
 
 int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn) {
@@ -1290,11 +1370,9 @@ int64_t qgx_resconv_eloc_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn
 namespace qgx {
 namespace {
 
-int eloc_impl(const float* table, int32_t L, int32_t nblocks, int32_t channels, int32_t complex_out,
-              int32_t conv_precision, const SymmDev* sym, const qgx_operator_t* op, const uint32_t* spins, int64_t ns,
-              double* eloc_re, double* eloc_im, void* workspace, cudaStream_t st) {
+int eloc_impl(const float* table, const ConvNet& net, const SymmDev* sym, const qgx_operator_t* op,
+              const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im, void* workspace, cudaStream_t st) {
   const int max_conn = op->n_f1 + op->n_f2;
-  const ConvNet net = make_net(L, nblocks, channels, complex_out, conv_precision);
   const int nw = words_for(net.N);
   const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
   char* ws = static_cast<char*>(workspace);
@@ -1366,8 +1444,8 @@ int qgx_resconv_eloc(const float* table, int32_t L, int32_t nblocks, int32_t cha
   QGX_CHECK_ARG(table && spins && eloc_re && workspace);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_workspace_bytes(L, ns, op->n_f1 + op->n_f2));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  return eloc_impl(table, L, nblocks, channels, complex_out, conv_precision, nullptr, op, spins, ns, eloc_re, eloc_im,
-                   workspace, as_cuda(stream));
+  return eloc_impl(table, make_net(L, nblocks, channels, complex_out, conv_precision), nullptr, op, spins, ns,
+                   eloc_re, eloc_im, workspace, as_cuda(stream));
 }
 
 int64_t qgx_resconv_eloc_symm_workspace_bytes(int32_t L, int64_t ns, int32_t max_conn, int32_t nsymm) {
@@ -1387,8 +1465,8 @@ int qgx_resconv_eloc_symm(const float* table, int32_t L, int32_t nblocks, int32_
   QGX_CHECK_ARG(table && spins && eloc_re && workspace);
   QGX_CHECK_ARG(workspace_bytes >= qgx_resconv_eloc_symm_workspace_bytes(L, ns, op->n_f1 + op->n_f2, sym.nsymm));
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
-  return eloc_impl(table, L, nblocks, channels, complex_out, conv_precision, &sym, op, spins, ns, eloc_re, eloc_im,
-                   workspace, as_cuda(stream));
+  return eloc_impl(table, make_net(L, nblocks, channels, complex_out, conv_precision), &sym, op, spins, ns,
+                   eloc_re, eloc_im, workspace, as_cuda(stream));
 }
 
 int64_t qgx_resconv_log_psi_symm_workspace_bytes(int32_t L, int64_t ns, int32_t nsymm) {
@@ -1450,6 +1528,110 @@ int qgx_resconv_jacobian_symm(const float* table, int32_t L, int32_t nblocks, in
   QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
   return jacobian_impl(table, L, nblocks, channels, complex_out, &sym, spins, ns, O_re, O_im, ldo, workspace,
                        workspace_bytes, as_cuda(stream));
+}
+
+// ---- the projected RBM: psi_symm(s) = sum_g w_g psi(T_g s) for RBM_Dense (symmetry.py:325-392 on
+// any model, variational.py:261-266); the images run through the RBM forward and closed-form
+// log-derivatives, everything else is the ResConv projection's pipeline
+int64_t qgx_rbm_log_psi_symm_workspace_bytes(int32_t n, int64_t ns, int32_t nsymm) {
+  if (n < 1 || ns < 1 || nsymm < 1) return 0;
+  return symm_scratch_bytes(ns, words_for(n), nsymm);
+}
+
+int qgx_rbm_log_psi_symm(const float* table, int32_t n, int32_t m, const qgx_symm_t* symm, const uint32_t* spins,
+                         int64_t ns, float* log_psi, void* workspace, int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(valid_rbm_symm(n, m) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_rbm_log_psi_symm_workspace_bytes(n, ns, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return symm_forward(table, make_rbm_net(n, m, 0), &sym, spins, ns, nullptr, reinterpret_cast<float2*>(log_psi),
+                      static_cast<char*>(workspace), as_cuda(stream));
+}
+
+int64_t qgx_rbm_sweep_symm_workspace_bytes(int32_t n, int64_t ns, int32_t nsymm) {
+  if (n < 1 || ns < 1 || nsymm < 1) return 0;
+  return sweep_scratch_bytes(n, ns) + symm_scratch_bytes(ns, words_for(n), nsymm);
+}
+
+int qgx_rbm_sweep_symm(const float* table, int32_t n, int32_t m, const qgx_symm_t* symm, uint32_t* spins,
+                       float* log_psi, int32_t* accepts, int64_t ns, int32_t nsteps, uint64_t seed, uint64_t step0,
+                       float reweight, int32_t proposal, const int32_t* nbr, int32_t z, int32_t hop, void* workspace,
+                       int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(valid_rbm_symm(n, m) && ns >= 0 && nsteps >= 0);
+  QGX_CHECK_ARG(proposal == QGX_PROPOSAL_LOCAL_FLIP || proposal == QGX_PROPOSAL_SPIN_EXCHANGE);
+  if (proposal == QGX_PROPOSAL_SPIN_EXCHANGE) QGX_CHECK_ARG(nbr && z > 0 && (hop == 1 || hop == -1));
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && log_psi && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_rbm_sweep_symm_workspace_bytes(n, ns, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return sweep_impl(table, make_rbm_net(n, m, 0), 0, &sym, spins, log_psi, accepts, ns, nsteps, seed, step0,
+                    reweight, proposal, nbr, z, hop, workspace, as_cuda(stream));
+}
+
+int64_t qgx_rbm_eloc_symm_workspace_bytes(int32_t n, int64_t ns, int32_t max_conn, int32_t nsymm) {
+  if (n < 1 || ns < 1 || max_conn < 0 || nsymm < 1) return 0;
+  const int64_t nc = ns * (int64_t)std::max(max_conn, 1);
+  return eloc_scratch_bytes(n, ns, max_conn) + symm_scratch_bytes(nc, words_for(n), nsymm);
+}
+
+int qgx_rbm_eloc_symm(const float* table, int32_t n, int32_t m, const qgx_symm_t* symm, const qgx_operator_t* op,
+                      const uint32_t* spins, int64_t ns, double* eloc_re, double* eloc_im, void* workspace,
+                      int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(op && valid_rbm_symm(n, m) && ns >= 0);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && eloc_re && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_rbm_eloc_symm_workspace_bytes(n, ns, op->n_f1 + op->n_f2, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  return eloc_impl(table, make_rbm_net(n, m, 0), &sym, op, spins, ns, eloc_re, eloc_im, workspace, as_cuda(stream));
+}
+
+int64_t qgx_rbm_jacobian_symm_workspace_bytes(int32_t n, int32_t m, int32_t has_vbias, int64_t ns, int32_t nsymm) {
+  if (n < 1 || m < 1 || ns < 1 || nsymm < 1) return 0;
+  const int64_t np = (int64_t)m * n + m + (has_vbias ? n : 0);
+  return symm_scratch_bytes(ns, words_for(n), nsymm) + al256(ns * 8) +
+         al256(rbm_symm_chunk(ns, nsymm, np) * nsymm * np * 4);
+}
+
+int qgx_rbm_jacobian_symm(const float* table, int32_t n, int32_t m, int32_t has_vbias, const qgx_symm_t* symm,
+                          const uint32_t* spins, int64_t ns, float* O_re, float* O_im, int64_t ldo, void* workspace,
+                          int64_t workspace_bytes, qgx_stream_t stream) {
+  SymmDev sym;
+  QGX_CHECK_ARG(to_symm(symm, &sym));
+  QGX_CHECK_ARG(valid_rbm_symm(n, m) && ns >= 0);
+  const int64_t np = (int64_t)m * n + m + (has_vbias ? n : 0);
+  QGX_CHECK_ARG(ldo >= np);
+  if (ns == 0) return QGX_OK;
+  QGX_CHECK_ARG(table && spins && O_re && workspace);
+  QGX_CHECK_ARG(workspace_bytes >= qgx_rbm_jacobian_symm_workspace_bytes(n, m, has_vbias, ns, sym.nsymm));
+  QGX_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0);
+  cudaStream_t st = as_cuda(stream);
+  const int nw = words_for(n);
+  char* ws = static_cast<char*>(workspace);
+  const int64_t sb = symm_scratch_bytes(ns, nw, sym.nsymm);
+  float2* lp_sym = reinterpret_cast<float2*>(ws + sb);
+  float* rows = reinterpret_cast<float*>(ws + sb + al256(ns * 8));
+  float2* lp_g = nullptr;
+  const uint32_t* cfg = nullptr;
+  int rc = symm_forward(table, make_rbm_net(n, m, has_vbias), &sym, spins, ns, nullptr, lp_sym, ws, st, &lp_g, &cfg);
+  if (rc != QGX_OK) return rc;
+  const int64_t cs = rbm_symm_chunk(ns, sym.nsymm, np);
+  const unsigned gx = (unsigned)std::min<int64_t>((np + 255) / 256, 1024);
+  for (int64_t c0 = 0; c0 < ns; c0 += cs) {
+    const int64_t cn = std::min(cs, ns - c0);
+    rc = rbm_jacobian_rows(table, n, m, has_vbias, cfg + c0 * sym.nsymm * nw, cn * sym.nsymm, rows, np, st);
+    if (rc != QGX_OK) return rc;
+    rbm_symm_rows_kernel<<<dim3(gx, (unsigned)cn), 256, sym.nsymm * sizeof(float2), st>>>(
+        rows, np, c0, sym.nsymm, lp_g, lp_sym, sym.weight, O_re, O_im, ldo);
+    if ((rc = launch_status()) != QGX_OK) return rc;
+  }
+  return QGX_OK;
 }
 
 }  // extern "C"

@@ -128,6 +128,43 @@ class RBM_Dense:
     def obar_workspace_bytes(self, ns: int) -> int:
         return int(_lib.lib().qgx_rbm_obar_workspace_bytes(self.N, self.M, ns))
 
+    # ---- the projected state (symm: a non-identity quantax_gb300.symmetry.Symmetry) ---------
+    def log_psi_symm_workspace_bytes(self, ns, symm):
+        return int(_lib.lib().qgx_rbm_log_psi_symm_workspace_bytes(self.N, ns, symm.nsymm))
+
+    def log_psi_symm(self, table, packed, out, symm, workspace):
+        """log psi_symm as (re, im) pairs into out ((ns, 2) float32)."""
+        _lib.call("qgx_rbm_log_psi_symm", _lib.ptr(table), self.N, self.M, C.byref(symm.device_struct()),
+                  _lib.ptr(packed), packed.shape[0], _lib.ptr(out), _lib.ptr(workspace), workspace.numel(),
+                  _lib.stream_ptr())
+
+    def sweep_symm_workspace_bytes(self, ns, symm):
+        return int(_lib.lib().qgx_rbm_sweep_symm_workspace_bytes(self.N, ns, symm.nsymm))
+
+    def sweep_symm(self, table, packed, log_psi, accepts, nsteps, seed, step0, reweight, proposal, nbr, z, hop,
+                   workspace, symm):
+        _lib.call("qgx_rbm_sweep_symm", _lib.ptr(table), self.N, self.M, C.byref(symm.device_struct()),
+                  _lib.ptr(packed), _lib.ptr(log_psi), _lib.ptr(accepts), packed.shape[0], int(nsteps), int(seed),
+                  int(step0), float(reweight), int(proposal), _lib.ptr(nbr), int(z), int(hop), _lib.ptr(workspace),
+                  workspace.numel(), _lib.stream_ptr())
+
+    def eloc_symm_workspace_bytes(self, ns, max_conn, symm):
+        return int(_lib.lib().qgx_rbm_eloc_symm_workspace_bytes(self.N, ns, max_conn, symm.nsymm))
+
+    def eloc_symm(self, table, compiled_op, packed, out_re, out_im, workspace, symm):
+        _lib.call("qgx_rbm_eloc_symm", _lib.ptr(table), self.N, self.M, C.byref(symm.device_struct()),
+                  C.byref(compiled_op.struct), _lib.ptr(packed), packed.shape[0], _lib.ptr(out_re), _lib.ptr(out_im),
+                  _lib.ptr(workspace), workspace.numel(), _lib.stream_ptr())
+
+    def jacobian_symm_workspace_bytes(self, ns, symm):
+        return int(_lib.lib().qgx_rbm_jacobian_symm_workspace_bytes(self.N, self.M, int(self.visible_bias), ns,
+                                                                      symm.nsymm))
+
+    def jacobian_symm(self, table, packed, o_re, o_im, ldo, workspace, symm):
+        _lib.call("qgx_rbm_jacobian_symm", _lib.ptr(table), self.N, self.M, int(self.visible_bias),
+                  C.byref(symm.device_struct()), _lib.ptr(packed), packed.shape[0], _lib.ptr(o_re), _lib.ptr(o_im),
+                  int(ldo), _lib.ptr(workspace), workspace.numel(), _lib.stream_ptr())
+
     def obar(self, table, packed, r, out, omean, workspace):
         _lib.call("qgx_rbm_obar", _lib.ptr(table), self.N, self.M, int(self.visible_bias), _lib.ptr(packed),
                   _lib.ptr(r), packed.shape[0], _lib.ptr(out), out.stride(0), _lib.ptr(omean), _lib.ptr(workspace),

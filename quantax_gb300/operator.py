@@ -279,7 +279,7 @@ class Operator:
         for k, (op, state, samples) in enumerate(terms):
             if not isinstance(samples, Samples):
                 samples = Samples.from_spins(samples)
-            if state.model.kind != "rbm":
+            if state.model.kind != "rbm" or state.symm_dev is not None:
                 out[k] = state.local_energy(op, samples)
                 continue
             comp = op.compiled()

@@ -183,7 +183,9 @@ class Metropolis(Sampler):
         self._step = 0
         self._initial_spins = initial_spins
         dev = state.params.device
-        self._resconv = state.model.kind == "resconv"
+        # log psi as (re, im) pairs, the sweep through the batched-forward pipeline: ResConv
+        # states and projected ones
+        self._resconv = state.model.kind == "resconv" or state.symm_dev is not None
         shape = (self._nsamples, 2) if self._resconv else (self._nsamples,)
         self._log_psi = torch.empty(shape, dtype=torch.float32, device=dev)
         self._accepts = torch.empty(self._nsamples, dtype=torch.int32, device=dev)
@@ -231,7 +233,11 @@ class Metropolis(Sampler):
     def _device_sweep(self, nsteps: int, step0: int, proposal, nbr, z: int, hop: int) -> None:
         """nsteps proposals of one kind for every chain, Philox steps step0 .. step0 + nsteps - 1."""
         st = self._state
-        if self._resconv:
+        if self._resconv and st.model.kind == "rbm":
+            ws = st.workspace("sweep", st.model.sweep_symm_workspace_bytes(self._nsamples, st.symm_dev))
+            st.model.sweep_symm(st.table, self._packed, self._log_psi, self._accepts, nsteps, self._seed, step0,
+                                self._reweight, proposal, nbr, z, hop, ws, st.symm_dev)
+        elif self._resconv:
             ws = st.workspace("sweep", st.model.sweep_workspace_bytes(self._nsamples, st.symm_dev))
             st.model.sweep(st.table, self._packed, self._log_psi, self._accepts, nsteps, self._seed, step0,
                            self._reweight, proposal, nbr, z, hop, ws, st.symm_dev)

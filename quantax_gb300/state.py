@@ -51,8 +51,8 @@ class Variational:
         if self._symm.Nmodes != get_sites().Nmodes:
             raise ValueError("the symmetry was built for another lattice")
         self._sym = None if self._symm.is_identity else self._symm
-        if self._sym is not None and model.kind != "resconv":
-            raise NotImplementedError("symmetry projection is built for the ResConv model")
+        if self._sym is not None and getattr(model, "conv", False):
+            raise NotImplementedError("symmetry projection is built for ResConv and RBM_Dense")
         self._model = model
         self._dev = device()
         self._sites = get_sites()  # the lattice this state was built on (kept, not re-read)
@@ -69,7 +69,11 @@ class Variational:
         self._use_ref = use_ref
         if getattr(model, "complex_output", False) and not is_default_cpl():
             raise ValueError("a complex-output model needs set_default_dtype(np.complex128) (VS_TYPE real_to_complex)")
-        is_cpl = is_default_cpl() and getattr(model, "complex_output", False)
+        # a projected RBM with complex characters has a complex psi_symm: its O rows are [Re; Im]
+        # when the computation dtype is complex (VS_TYPE real_to_complex, variational.py:245-255)
+        self._rbm_symm_cpl = (self._sym is not None and model.kind == "rbm" and is_default_cpl()
+                              and bool(np.any(np.imag(self._symm.weights()) != 0)))
+        is_cpl = is_default_cpl() and getattr(model, "complex_output", False) or self._rbm_symm_cpl
         self._vs_type = VS_TYPE.real_to_complex if is_cpl else VS_TYPE.real_or_holomorphic
         self._ws = {}
         self._refresh()
@@ -136,16 +140,19 @@ class Variational:
     # ---- forward ------------------------------------------------------------------------
     @property
     def is_complex(self) -> bool:
-        return bool(getattr(self._model, "complex_output", False))
+        return bool(getattr(self._model, "complex_output", False)) or self._rbm_symm_cpl
 
     def log_psi_packed(self, packed: torch.Tensor) -> torch.Tensor:
         """log psi of packed configurations: float32, or complex64 for complex-output models."""
-        if self._model.kind == "rbm":
+        if self._model.kind == "rbm" and self._sym is None:
             out = torch.empty(packed.shape[0], dtype=torch.float32, device=self._dev)
             self._model.log_psi(self._table, packed, out)
             return out
         out = torch.empty((packed.shape[0], 2), dtype=torch.float32, device=self._dev)
-        if self._sym is None:
+        if self._model.kind == "rbm":
+            ws = self.workspace("fwd_symm", self._model.log_psi_symm_workspace_bytes(packed.shape[0], self._sym))
+            self._model.log_psi_symm(self._table, packed, out, self._sym, ws)
+        elif self._sym is None:
             self._model.log_psi(self._table, packed, out)
         else:
             ws = self.workspace("fwd_symm", self._model.log_psi_workspace_bytes(packed.shape[0], self._sym))
@@ -175,13 +182,17 @@ class Variational:
             raise ValueError("the operator acts on sites beyond the state's lattice")
         ns = samples.nsamples
         out = torch.empty(ns, dtype=torch.float64, device=self._dev)
-        if self._model.kind == "rbm":
+        if self._model.kind == "rbm" and self._sym is None:
             self._model.eloc(self._table, comp, samples.packed, out)
             return out
         out_im = torch.empty(ns, dtype=torch.float64, device=self._dev) if self.is_complex else None
         max_conn = len(comp.host["f1"]) + len(comp.host["f2"])
-        ws = self.workspace("eloc", self._model.eloc_workspace_bytes(ns, max_conn, self._sym))
-        self._model.eloc(self._table, comp, samples.packed, out, out_im, ws, self._sym)
+        if self._model.kind == "rbm":
+            ws = self.workspace("eloc", self._model.eloc_symm_workspace_bytes(ns, max_conn, self._sym))
+            self._model.eloc_symm(self._table, comp, samples.packed, out, out_im, ws, self._sym)
+        else:
+            ws = self.workspace("eloc", self._model.eloc_workspace_bytes(ns, max_conn, self._sym))
+            self._model.eloc(self._table, comp, samples.packed, out, out_im, ws, self._sym)
         return torch.complex(out, out_im) if out_im is not None else out
 
     def jacobian(self, s) -> torch.Tensor:
@@ -197,8 +208,13 @@ class Variational:
         """O of packed configurations written into out (obar_rows(ns) x nparams float32, any row
         stride): the rows [Re O; Im O] for complex output."""
         ns = packed.shape[0]
-        if self._model.kind == "rbm":
+        if self._model.kind == "rbm" and self._sym is None:
             self._model.jacobian(self._table, packed, out)
+            return out
+        if self._model.kind == "rbm":
+            ws = self.workspace("jac", self._model.jacobian_symm_workspace_bytes(ns, self._sym))
+            self._model.jacobian_symm(self._table, packed, out[:ns], out[ns:] if self.is_complex else None,
+                                      out.stride(0), ws, self._sym)
             return out
         ws = self.workspace("jac", self._model.jacobian_workspace_bytes(ns, self._sym))
         self._model.jacobian(self._table, packed, out[:ns], out[ns:] if self.is_complex else None, out.stride(0), ws,
@@ -215,15 +231,14 @@ class Variational:
         ns = samples.nsamples
         if out is None:
             out = torch.empty((self.obar_rows(ns), self.nparams), dtype=torch.float32, device=self._dev)
-        if self._model.kind == "rbm":
+        if self._model.kind == "rbm" and self._sym is None:
             omean = torch.empty(self.nparams, dtype=torch.float64, device=self._dev)
             ws = self.workspace("obar", self._model.obar_workspace_bytes(ns))
             self._model.obar(self._table, samples.packed, samples.reweight_factor, out, omean, ws)
             return out, omean
-        ws = self.workspace("jac", self._model.jacobian_workspace_bytes(ns, self._sym))
         cplx = self.is_complex
         ld = out.stride(0)
-        self._model.jacobian(self._table, samples.packed, out[:ns], out[ns:] if cplx else None, ld, ws, self._sym)
+        self.jacobian_rows(samples.packed, out)
         cws = self.workspace("center", _lib.lib().qgx_center_columns_workspace_bytes(ns, self.nparams))
         halves = [out[:ns], out[ns:]] if cplx else [out]
         means = []

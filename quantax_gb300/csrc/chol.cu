@@ -25,12 +25,14 @@
 // The products with t + u >= 8 are dropped: with the digits' own truncation the update's error
 // is a few 2^-56 K 2^(e_i + e_j), below FP64's own rounding of a K-term dot product.
 //
-// The tensor-core kernel: one CTA per 128 x 64 tile of C on or below the diagonal; warp 4
-// loads the 8 digit slices of the tile's 128 A rows and 64 B rows, 32 K-elements per stage
-// (3D TMA box, 64-byte swizzle, two stages); warp 5 issues the 36 tcgen05.mma (M 128, N 64,
-// K 16, BF16 -> FP32) of each 16-element K step into the eight 64-column level accumulators
-// (all 512 TMEM columns); warps 0-3 read the levels back, fold them in int64 and apply the
-// update to C through a shared-memory transpose (coalesced row writes). Every mbarrier wait is
+// The tensor-core kernel: one CTA per 128 x 32 tile of C on or below the diagonal, two CTAs
+// per SM (one CTA's epilogue overlaps the other's MMAs). Warp 4 loads the 8 digit slices of the
+// tile's 128 A rows and 32 B rows, 32 K-elements per stage (3D TMA box, 64-byte swizzle, one
+// stage); warp 5 issues, per 16-element K step, one tcgen05.mma per A slice t (M 128,
+// N = 32 (8 - t), K 16, BF16 -> FP32) against the B slices 0 .. 7 - t side by side, so the
+// eight 32-column level accumulators (256 TMEM columns) each collect their level's products;
+// warps 0-3 read the levels back and fold them in int64 into a shared-memory tile of FP64
+// deltas, and all six warps apply the update to C in coalesced rows. Every mbarrier wait is
 // bounded (2 s); a wait that runs out records QGX_ERR_TIMEOUT, the CTA frees its TMEM and
 // leaves C alone.
 #include <cuda.h>

@@ -59,6 +59,24 @@ def test_argument_errors_are_reported_without_a_device(qgx_built):
     assert L.qgx_er_weight_rows(None, 4, 8, 4, None, 0, None) == _lib.QGX_ERR_ARG  # ldo < cols
     assert L.qgx_er_center(None, 4, 8, 8, None, 1, None, None) == _lib.QGX_ERR_ARG
     assert L.qgx_column_sumsq(None, 4, 8, 4, None, None, 0, None) == _lib.QGX_ERR_ARG
+    # the projected RBM: a missing or malformed group, sizes past the kernels' limits, an
+    # unknown proposal, SpinExchange without a neighbour table
+    import ctypes as C
+    perm = (C.c_int16 * 16)(*range(16))
+    w = (C.c_double * 2)(1.0, 0.0)
+    sym = _lib.Symm(C.cast(perm, C.c_void_p), C.cast(w, C.c_void_p), 1, 0)
+    bad = _lib.Symm(None, C.cast(w, C.c_void_p), 1, 0)
+    assert L.qgx_rbm_log_psi_symm(None, 16, 32, None, None, 4, None, None, 0, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_rbm_log_psi_symm(None, 16, 32, C.byref(bad), None, 4, None, None, 0, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_rbm_log_psi_symm(None, 300, 32, C.byref(sym), None, 4, None, None, 0, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_rbm_log_psi_symm(None, 16, 32, C.byref(sym), None, 0, None, None, 0, None) == _lib.QGX_OK
+    assert L.qgx_rbm_sweep_symm(None, 16, 32, C.byref(sym), None, None, None, 4, 1, 0, 0, 2.0, 7, None, 0, 1,
+                                None, 0, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_rbm_sweep_symm(None, 16, 32, C.byref(sym), None, None, None, 4, 1, 0, 0, 2.0,
+                                _lib.PROPOSAL_SPIN_EXCHANGE, None, 0, 1, None, 0, None) == _lib.QGX_ERR_ARG
+    assert L.qgx_rbm_jacobian_symm(None, 16, 32, 0, C.byref(sym), None, 4, None, None, 100, None, 0,
+                                   None) == _lib.QGX_ERR_ARG  # ldo below the 560 parameters
+    assert L.qgx_rbm_log_psi_symm_workspace_bytes(16, 4, 1) > 0
 
 
 def test_no_cpu_fallback_without_library(tmp_path):

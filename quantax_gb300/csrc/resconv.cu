@@ -206,14 +206,18 @@ __device__ inline void conv_layer(const float* __restrict__ in, int cin, float* 
 // order as conv_layer, so both give the same floats. Items of one channel group fill whole
 // warps, so a warp's weight loads are broadcasts. In mode 1 with pnext, the updated residual x
 // is also written as the next block's pre-activation pnext = gelu(x pscale) (the separate pass
-// of the site-order kernel, the same floats).
-template <int C, int CO>
-__device__ inline void conv_layer_blocked(const float* __restrict__ in, int cin, float* __restrict__ out,
+// of the site-order kernel, the same floats). CIN > 0 fixes the input channel count at compile
+// time (the C-channel layers); the input-channel loop is unrolled four times either way
+// (measured: 2.77 ms per 16384 forwards at L = 10 against 2.93 without; eight and sixteen were
+// slower).
+template <int C, int CO, int CIN = 0>
+__device__ inline void conv_layer_blocked(const float* __restrict__ in, int cin_rt, float* __restrict__ out,
                                           const float* __restrict__ w, const int16_t* __restrict__ nbr, int N,
                                           int S, int mode, int ss, float* __restrict__ pnext = nullptr,
                                           float pscale = 1.0f) {
   static_assert(C % CO == 0 && CO % 4 == 0, "output channel groups of 4k channels");
   constexpr int H = C / CO;
+  const int cin = CIN > 0 ? CIN : cin_rt;
   const float* bias = w + cin * 9 * C;
   const int NB = N >> 2;
   const int items = S * NB;
@@ -232,6 +236,7 @@ __device__ inline void conv_layer_blocked(const float* __restrict__ in, int cin,
 #pragma unroll
       for (int e = 0; e < CO / 2; ++e) acc[q][e] = make_float2(bias[o0 + 2 * e], bias[o0 + 2 * e + 1]);
     const float* ina = in + (int64_t)a * ss;
+#pragma unroll 4
     for (int i = 0; i < cin; ++i) {
       const float* ini = ina + i * N;
       float d[16];
@@ -380,7 +385,9 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
       stage_floats(Wl, table + layer_offset(2 * b, C), layer_floats(2 * b, C));
       if (BLK) prefetch_l1(table + layer_offset(2 * b + 1, C), layer_floats(2 * b + 1, C));
       __syncthreads();
-      if (BLK)
+      if (BLK && cin == C)
+        conv_layer_blocked<C, rc_blocked_co<C>(), C>(P, C, Q, Wl, nbr, N, S, 0, SS);
+      else if (BLK)
         conv_layer_blocked<C, rc_blocked_co<C>()>(P, cin, Q, Wl, nbr, N, S, 0, SS);
       else
         conv_layer<C, kFwdSPT>(P, cin, Q, Wl, nbr, N, S, 0, SS);
@@ -391,8 +398,8 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
       if (BLK) prefetch_l1(table + layer_offset(lnext, C), layer_floats(lnext, C));
       __syncthreads();
       if (BLK)
-        conv_layer_blocked<C, rc_blocked_co<C>()>(Q, C, X, Wl, nbr, N, S, 1, SS, b + 1 < net.B ? P : nullptr,
-                                                  rsqrtf((float)(b + 2)));
+        conv_layer_blocked<C, rc_blocked_co<C>(), C>(Q, C, X, Wl, nbr, N, S, 1, SS, b + 1 < net.B ? P : nullptr,
+                                                     rsqrtf((float)(b + 2)));
       else
         conv_layer<C, kFwdSPT>(Q, C, X, Wl, nbr, N, S, 1, SS);
     }

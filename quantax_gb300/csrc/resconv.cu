@@ -968,11 +968,9 @@ int launch_jacobian_c(const float* table, const ConvNet& net, const uint32_t* sp
   return launch_status();
 }
 
-// the blocked site order (conv_layer_blocked) at even L, the site order otherwise
-inline bool rc_blocked(const ConvNet& net) { return net.L % 2 == 0; }
-
-int rc_smem_bytes(const ConvNet& net, int S) {
-  const bool blk = rc_blocked(net);
+// shared memory of the FP32 forward with S samples per CTA, in the blocked order (blk, even L
+// only) or the site order
+int rc_smem_bytes(const ConvNet& net, int S, bool blk) {
   const int64_t f = rc_weights_offset(S, rc_sample_stride(net.C, net.N, blk)) + (int64_t)net.C * 9 * net.C + net.C;
   const int64_t tables = blk ? (int64_t)net.N * 4 + net.N : (int64_t)net.N * 9;  // int16 entries
   return (int)(f * 4 + tables * 2 + 16);
@@ -991,7 +989,7 @@ int rc_blocked_samples(const ConvNet& net) {
   for (int limit : {two, cap}) {
     int best = 0;
     double best_fill = 0.0;
-    for (int s = 1; s <= 64 && rc_smem_bytes(net, s) <= limit; ++s) {
+    for (int s = 1; s <= 64 && rc_smem_bytes(net, s, true) <= limit; ++s) {
       const int per = (s * NB + 31) & ~31;
       const int passes = (H * per + kFwdThreads - 1) / kFwdThreads;
       const double fill = (double)H * s * NB / ((double)passes * kFwdThreads);
@@ -1005,13 +1003,22 @@ int rc_blocked_samples(const ConvNet& net) {
 template <int C>
 int launch_forward_c(const float* table, const ConvNet& net, const uint32_t* cfg, int64_t ncfg, const int64_t* n_live,
                      float2* out, cudaStream_t st) {
-  const bool blk = rc_blocked(net);
   // site order: kFwdSamples per CTA (5 x 50 site pairs fill 256 threads at L = 10), fewer where
   // their buffers would not fit (L = 16: 4)
   int S = kFwdSamples;
-  while (S > 1 && rc_smem_bytes(net, S) > device_max_smem_optin()) --S;
-  if (blk) S = rc_blocked_samples<C>(net);
-  const int smem = rc_smem_bytes(net, S);
+  while (S > 1 && rc_smem_bytes(net, S, false) > device_max_smem_optin()) --S;
+  // The blocked order (even L) where it does not lengthen a thread's serial work: a thread
+  // computes 4 x CO outputs per layer there against 2 x C in the site order, more at fewer than
+  // 12 channels. That only pays when the batch gives every SM two CTAs (measured at L = 4 with 8
+  // channels: 30 against 15 us for 512 configurations, 84 against 182 us for 32768). Both orders
+  // give the same floats, so the choice never changes a result.
+  bool blk = false;
+  if (net.L % 2 == 0) {
+    const int sb = rc_blocked_samples<C>(net);
+    blk = 4 * rc_blocked_co<C>() <= 2 * C || (ncfg + sb - 1) / sb >= 2LL * device_sm_count();
+    if (blk) S = sb;
+  }
+  const int smem = rc_smem_bytes(net, S, blk);
   if (smem > device_max_smem_optin()) return QGX_ERR_UNSUPPORTED;
   auto k = blk ? rc_forward_kernel<C, true> : rc_forward_kernel<C, false>;
   if (smem > 48 * 1024) QGX_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));

@@ -61,6 +61,20 @@ def test_resconv_log_psi(cuda, L, B, Cc, cplx):
     _close_logpsi(net.log_psi(_pack(s)), net.oracle.log_psi(s), 2e-4)
 
 
+@pytest.mark.parametrize("L,Cc,cplx", [(4, 8, True), (6, 8, False), (4, 4, True)])
+def test_fp32_forward_orders_agree_bitwise(cuda, L, Cc, cplx):
+    """Below 12 channels the FP32 forward keeps the site order for a batch that cannot give every
+    SM two CTAs, and takes the blocked order (2 x 2 site blocks) once it can. The same 512
+    configurations alone (site order) and inside a batch of 32768 (blocked order) must give the
+    same floats."""
+    net = Net(L, 2, Cc, cplx, seed=6, bias_std=0.2)
+    s = metropolis.init_uniform(512, L * L, 3)
+    small = net.log_psi(_pack(s))
+    big = net.log_psi(_pack(np.tile(s, (64, 1))))
+    assert np.array_equal(small, big[:512])
+    assert np.array_equal(big[:512], big[-512:])
+
+
 def test_resconv_spin_exchange_sweep_bit_exact(cuda):
     from quantax_gb300 import _lib as Lb
     L, B, Cc = 4, 2, 8

@@ -45,12 +45,12 @@ UNIT = "SR_steps/s"
 WORKLOADS = {
     "resconv": dict(workload="j1j2_square10_resconv8x16_minsr16384", lattice="Square(10) PBC, Sz=0",
                     hamiltonian="Heisenberg(J=[1, 0.5], n_neighbor=[1, 2], msr=True)",
-                    model="ResConv(8 blocks, 16 channels, complex output)", nparams=34944,
+                    wavefunction="ResConv(8 blocks, 16 channels, complex output)", nparams=34944,
                     sampler="SpinExchange", chains=16384, proposals_per_sweep=200, thermal_proposals=200,
                     solver="minnorm_shift_eig(ashift=1e-4) on the stacked [Re; Im] 32768 x 34944 matrix",
                     l2="inputs larger than L2: Obar (4.6 GB) and T (8.6 GB) exceed the 129 MB L2 every step"),
     "rbm": dict(workload="tfim_chain64_rbm256_minsr8192", lattice="Chain(64) PBC", hamiltonian="Ising(h=1, J=1)",
-                model="RBM_Dense(features=256)", nparams=16640, sampler="LocalFlip", chains=8192,
+                wavefunction="RBM_Dense(features=256)", nparams=16640, sampler="LocalFlip", chains=8192,
                 proposals_per_sweep=64, thermal_proposals=640, solver="minnorm_shift_eig(ashift=1e-4)",
                 l2="inputs larger than L2: Obar (545 MB) and T (537 MB) exceed the 129 MB L2 every step"),
 }

@@ -10,9 +10,11 @@
 // log psi = logsumexp(z) - log(C' N) (exp_by_scale + ConvSymmetrize over translations).
 // Convolutions: 3x3, circular, cross-correlation. gelu: tanh approximation.
 //
-// Work layout: one CTA holds S samples' activations (three C x N buffers per sample) and
-// the current layer's weights in shared memory; a thread computes all C output channels of
-// one (sample, site) pair, so every weight load is a warp-wide broadcast.
+// Work layout of the FP32 forward: one CTA holds S samples' activations (three C x N buffers
+// per sample) and the current layer's weights in shared memory. In the site order a thread
+// computes all C output channels of two sites of one sample; in the blocked order (even L, see
+// rc_blocked_site) it computes 8 (or 4) output channels of a 2 x 2 block of sites. Threads of a
+// warp share their output channels, so every weight load is a warp-wide broadcast.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>

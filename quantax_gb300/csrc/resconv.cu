@@ -741,7 +741,7 @@ __device__ inline void input_grads(const float* __restrict__ g, const float* __r
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
       const int rn = nbr[r * 9 + (8 - t)];
-      for (int o = 0; o < C; ++o) {
+      auto term = [&](int o) {
         const float v = gk[o * N + rn];
         const float4* wp = reinterpret_cast<const float4*>(WT + (t * C + o) * C);
 #pragma unroll
@@ -752,6 +752,14 @@ __device__ inline void input_grads(const float* __restrict__ g, const float* __r
           acc[4 * i4 + 2] = fmaf(v, w.z, acc[4 * i4 + 2]);
           acc[4 * i4 + 3] = fmaf(v, w.w, acc[4 * i4 + 3]);
         }
+      };
+      if constexpr (C <= 8) {
+        // left to itself the compiler unrolls all 8 output channels here and spills 4 KB per
+        // thread; four at a time keeps every value in registers
+#pragma unroll 4
+        for (int o = 0; o < C; ++o) term(o);
+      } else {
+        for (int o = 0; o < C; ++o) term(o);
       }
     }
 #pragma unroll

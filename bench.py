@@ -338,6 +338,23 @@ def run_form(args, rank, world, gram, solve, e2e_steps=0, clocks=None, conv="fp3
     out = dict(elapsed=elapsed, lat=lat, phases=phases, energies=energies, launches=launches, clocks=clk,
                nparams=state.nparams, fallbacks=opt.solve_fallbacks)
 
+    if args.workload == "resconv" and e2e_steps > 0:
+        # the step's dominant kernel on its own: the forward over the chains' current configurations,
+        # CUDA events around 10 launches on the stream they run on (after the timed steps)
+        packed = sampler.sweep(0).packed
+        for _ in range(2):
+            state.log_psi_packed(packed)
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record()
+        for _ in range(10):
+            state.log_psi_packed(packed)
+        f1.record()
+        torch.cuda.synchronize()
+        out["fwd_ms"] = f0.elapsed_time(f1) / 10
+        out["fwd_ncfg"] = int(packed.shape[0])
+
     if e2e_steps > 0:
         # end to end through the public API with host buffers: parameters in from pinned host
         # memory, energy statistics and updated parameters back every step
@@ -727,6 +744,24 @@ def main():
                 "duration": "CUDA events around the Gram phase (one launch) of every timed step, mean",
                 "note": ("split-TF32: each product is hi*hi + hi*lo + lo*hi, so its mode peak is a third of the TF32 "
                          "rate" if gram == "3xtf32" else "")}
+        roof_fwd = None
+        if "fwd_ms" in plain and conv == "fp32":
+            L, nb, ch = 10, 8, 16
+            flop = 2.0 * L * L * 9 * ch * (1 + (2 * nb - 1) * ch)  # 6.94e6 per forward
+            ach = flop * plain["fwd_ncfg"] / (plain["fwd_ms"] / 1000.0) / 1e12
+            fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+            roof_fwd = {"kernel": "rc_forward_kernel (ResConv forward, FP32 on the CUDA cores, blocked site order)",
+                        "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": ach / fp32_peak,
+                        "peak_source": ("nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz "
+                                        "(MEASURED_PEAKS.json holds no FP32 figure)"),
+                        "algorithmic": (f"{flop:.4e} FLOP per forward x {plain['fwd_ncfg']} configurations per "
+                                        "launch"),
+                        "duration": (f"{plain['fwd_ms']:.4f} ms per launch: CUDA events around 10 launches over "
+                                     "the step's chains, after the timed steps"),
+                        "note": ("the plain step's largest kernel (about half its device time: sweep proposals and "
+                                 "local energies, profiles/launches_c3_plain_step.md); `roofline` above is the "
+                                 "tensor-core Gram")}
         elapsed = plain["elapsed"]
         target = None
         if forms:
@@ -748,7 +783,8 @@ def main():
             "energies": [round(e, 6) for e in plain["energies"]],
             "e2e": {"value": world * e2e_steps / plain["e2e_s"], "unit": UNIT, "steps": e2e_steps,
                     "h2d_bytes_per_step": npar * 4, "d2h_bytes_per_step": npar * 4 + 24},
-            "gpu_launches": plain["launches"], "roofline": roof, "clocks": plain["clocks"], "forms": forms,
+            "gpu_launches": plain["launches"], "roofline": roof, "roofline_dominant": roof_fwd,
+            "clocks": plain["clocks"], "forms": forms,
             "target": target,
         }
         if not args.no_cpu_baseline:

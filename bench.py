@@ -384,8 +384,14 @@ def run_form(args, rank, world, gram, solve, e2e_steps=0, clocks=None, conv="fp3
 def run_serving(args, rank):
     """A seeded Poisson stream of VMC jobs (TFIM chains with RBM_Dense, J1-J2 squares with
     ResConv, sample counts 1024-8192), served with continuous batching on one GPU."""
-    from quantax_gb300.serving import VMCServer, poisson_jobs
+    from quantax_gb300.serving import JobSpec, VMCServer, poisson_jobs
     specs = poisson_jobs(args.jobs, seed=2024 + rank, steps=args.job_steps)
+    # warm-up, untimed: one small job of each kind through its own server, so that loading the
+    # solver libraries and first-use module loads do not land in the first timed job's steps
+    warm = VMCServer(max_active=2)
+    warm.submit(JobSpec("warm_tfim", "tfim", 16, 1024, 3, seed=1))
+    warm.submit(JobSpec("warm_j1j2", "j1j2", 4, 1024, 3, seed=2))
+    warm.run()
     srv = VMCServer(max_active=8)
     for sp in specs:
         srv.submit(sp)
@@ -399,7 +405,8 @@ def run_serving(args, rank):
     per_job = {"median": ratios[len(ratios) // 2], "max": ratios[-1]} if ratios else None
     if rank == 0:
         line = {"metric": METRIC, "value": steps / out["wall_s"], "unit": UNIT, "n_gpus": 1, "steps": steps,
-                "warmup": 0, "ms_per_step": 1000.0 * out["wall_s"] / steps, "higher_is_better": True,
+                "warmup": 2, "warmup_note": "two untimed warm-up jobs (3 SR steps each) through a separate server",
+                "ms_per_step": 1000.0 * out["wall_s"] / steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "bf16 conv / bf16 Gram / FP64 solve",
                 "data": "synthetic",
                 "config": {"workload": f"serving: {args.jobs} Poisson jobs x {args.job_steps} SR steps "
